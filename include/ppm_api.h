@@ -1,0 +1,235 @@
+/*
+ * ppm_api.h -- C ABI of the GB300-native ppm-pa hot path (libppmpa_gb300.so).
+ *
+ * Plain C: pointers, sizes and POD structs only; no CUDA or C++ types cross
+ * the boundary.  Every entry point returns a ppm_status (0 = OK); the text
+ * of the last error of a context is ppm_last_error(ctx).  Nothing throws.
+ *
+ * Each entry point names the reference interface it replaces (eijian/ppmpa,
+ * paths relative to that project).  Host buffers are owned by the caller and
+ * copied; device memory is owned by the context.  One context per host
+ * thread; a context is not thread-safe.
+ */
+#ifndef PPM_API_H
+#define PPM_API_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PPM_API_VERSION 1
+
+typedef enum ppm_status {
+    PPM_OK = 0,
+    PPM_ERR_INVALID_ARG = 1,
+    PPM_ERR_OOM = 2,
+    PPM_ERR_CAPACITY = 3,   /* a caller buffer or a device queue is too small */
+    PPM_ERR_TIMEOUT = 4,
+    PPM_ERR_CUDA = 5,
+    PPM_ERR_NOT_READY = 6,  /* e.g. no scene, camera or photon map yet */
+    PPM_ERR_NO_DEVICE = 7
+} ppm_status;
+
+/* ---- scene description (src/ray/geometry.rs, material.rs, surface.rs, light.rs) */
+
+enum { PPM_SHAPE_POINT = 0, PPM_SHAPE_PLAIN = 1, PPM_SHAPE_SPHERE = 2,
+       PPM_SHAPE_POLYGON = 3, PPM_SHAPE_PARALLELOGRAM = 4 };
+enum { PPM_SURF_NOTHING = 0, PPM_SURF_SIMPLE = 1, PPM_SURF_TS = 2 };
+enum { PPM_LIGHT_POINT = 0, PPM_LIGHT_PARALLELOGRAM = 1, PPM_LIGHT_SUN = 2 };
+enum { PPM_FILTER_NONE = 0, PPM_FILTER_CONE = 1, PPM_FILTER_GAUSS = 2 };
+enum { PPM_WL_RED = 0, PPM_WL_GREEN = 1, PPM_WL_BLUE = 2 };
+
+/* Object = Shape + material index (src/ray/object.rs:10-13, geometry.rs:66-90).
+ * Plain: infinite plane nvec.x + dist = 0.  Sphere: position = centre.
+ * Polygon (triangle) / Parallelogram: position = p0, dir1 = p1-p0, dir2 = p2-p0,
+ * nvec = normalize(dir1 x dir2). */
+typedef struct ppm_object {
+    int32_t shape;
+    int32_t material;
+    double position[3];
+    double nvec[3];
+    double dir1[3];
+    double dir2[3];
+    double dist;
+    double radius;
+} ppm_object;
+
+/* Material + Surface (src/ray/material.rs:11-16, surface.rs:16-41).
+ * Simple: color_diff = reflectance, color_spec = specular_refl, scatter = diffuseness.
+ * TS:     color_diff = albedo_diff, color_spec = albedo_spec, scatter = scatterness.
+ * density_pow and alpha are derived: call ppm_material_derive(). */
+typedef struct ppm_material {
+    double emittance[3];
+    double transmittance[3];
+    double ior[3];
+    int32_t surface;
+    int32_t pad_;
+    double color_diff[3];
+    double color_spec[3];
+    double scatter;
+    double metalness;
+    double roughness;
+    double density_pow;
+    double alpha;
+} ppm_material;
+
+/* Light (src/ray/light.rs:16-39).  color is used as given: the reference's
+ * scene code normalises it (Color::normalize) before building the light. */
+typedef struct ppm_light {
+    int32_t kind;
+    int32_t pad_;
+    double color[3];
+    double flux;
+    double pos[3];
+    double nvec[3];
+    double dir1[3];
+    double dir2[3];
+    double dir[3];
+} ppm_light;
+
+/* Camera (src/camera.rs:23-49).  The first block is read_camera's input
+ * (camera.rs:108-146; focal_len in metres); the second block is derived by
+ * ppm_camera_derive() exactly as camera.rs:150-175. */
+typedef struct ppm_camera {
+    int32_t xreso, yreso;
+    int32_t progressive, antialias, blur, use_classic;
+    int32_t pfilter, n_sample_photon;
+    double radius, max_radiance, iso_sens, shut_speed, focal_len, f_number, focus;
+    double ambient[3], eye_pos[3], target[3], upper[3];
+    double eye_dir[3], origin[3], esx[3], esy[3], eex[3], eey[3];
+    double photon_power;
+} ppm_camera;
+
+/* Progressive render configuration (src/bin/ppmpa.rs:15-84 plus the pass loop,
+ * PA radius schedule and average of util/iterator.rb:33-38, util/averager.rb). */
+enum { PPM_PRECISION_PLAIN = 0,   /* FP64 everywhere (reference semantics) */
+       PPM_PRECISION_MIXED = 1 }; /* FP32 trace/gather + Kahan; FP64 radius, average, normalisation */
+
+typedef struct ppm_render_cfg {
+    int64_t nphoton;          /* photons per pass (#photon of ppmpa.rs:15) */
+    int32_t passes;
+    int32_t use_classic;      /* 1 = default, 0 = "-nc" (ppmpa.rs:50-54) */
+    double radius0;           /* initial estimate radius (not squared) */
+    double alpha;             /* PA alpha (iterator.rb:17 uses 0.5) */
+    int32_t schedule_offset;  /* 1: iterator.rb:33-38; 0: radius.rb / averager.rb */
+    int32_t precision;        /* PPM_PRECISION_* */
+    int32_t use_graph;        /* capture one pass as a CUDA graph and replay it */
+    int32_t cell_factor;      /* grid cells per radius (1 or 2; 0 = auto) */
+    uint64_t seed;
+    int32_t first_pass;       /* index of the first pass (for sharded/resumed runs) */
+    int32_t flags;            /* reserved, 0 */
+} ppm_render_cfg;
+
+/* Per-pass statistics of the last rendered pass and accumulated timings. */
+typedef struct ppm_stats {
+    int64_t photons_emitted;   /* last pass */
+    int64_t photons_stored;    /* last pass */
+    int64_t hit_points;        /* last pass */
+    int64_t grid_cells;        /* last pass */
+    int64_t passes_done;
+    int32_t kernels_per_pass;  /* CUDA kernels launched by one pass */
+    int32_t n_stages;
+    double  r2;                /* radius^2 of the last pass */
+    double  stage_ms[16];      /* summed device time per stage (timing on) */
+    int64_t stage_calls[16];
+    int64_t candidates;        /* photons tested by the gather (last pass, if counted) */
+    int64_t in_radius;         /* photons found in radius (last pass, if counted) */
+} ppm_stats;
+
+typedef struct ppm_ctx ppm_ctx;
+
+/* ---- context ----------------------------------------------------------- */
+int         ppm_version(void);
+const char *ppm_status_string(int status);
+int         ppm_ctx_create(ppm_ctx **out, int device, uint64_t seed);
+int         ppm_ctx_destroy(ppm_ctx *ctx);
+const char *ppm_last_error(const ppm_ctx *ctx);
+void       *ppm_ctx_stream(ppm_ctx *ctx);               /* the cudaStream_t all work runs on */
+int         ppm_ctx_sync(ppm_ctx *ctx);
+
+/* ---- scene and camera input ---------------------------------------------- */
+/* Replaces read_scene (src/scene.rs:20): the scene arrives as data. */
+int  ppm_scene_upload(ppm_ctx *ctx, const ppm_object *objs, int32_t n_objs,
+                      const ppm_material *mats, int32_t n_mats,
+                      const ppm_light *lights, int32_t n_lights);
+/* Replaces read_camera (src/camera.rs:108): derives, then stores. */
+int  ppm_camera_set(ppm_ctx *ctx, const ppm_camera *cam);
+/* Host helpers: camera.rs:150-175 and Surface::new_simple/new_ts (surface.rs:45-66). */
+void ppm_camera_derive(ppm_camera *cam);
+void ppm_material_derive(ppm_material *mat);
+
+/* ---- FP64 parity entry points (host buffers) ------------------------------ */
+/* calc_intersection (src/tracer.rs:306-350) for n rays (n x 6: pos, dir):
+ * t[i] = nearest distance >= NEARLY0, obj[i] = object index or -1; nrm
+ * (optional, n x 3) the normal oriented against the ray. */
+int ppm_intersect(ppm_ctx *ctx, const double *rays, int64_t n,
+                  double *t, int32_t *obj, double *nrm);
+/* FP32 traversal of the same rays (the mixed-precision intersector). */
+int ppm_intersect_f32(ppm_ctx *ctx, const double *rays, int64_t n,
+                      double *t, int32_t *obj);
+
+/* Photon emission + trace_photon for one pass (src/bin/ppmpa.rs:30-31, :86-92;
+ * src/tracer.rs:31-125; src/ray/light.rs:67-91) in FP64.  Results stay on the
+ * device; ppm_photons_download copies them out (order unspecified; emit_idx
+ * and level identify each photon).  pass selects the random stream. */
+int ppm_trace_photons(ppm_ctx *ctx, int64_t nphoton, int32_t use_classic, uint32_t pass,
+                      int64_t *n_stored, double *power, int64_t *n_emitted);
+int ppm_photons_download(ppm_ctx *ctx, double *pos, double *dir, uint8_t *wl,
+                         int32_t *emit_idx, int8_t *level, int64_t cap);
+
+/* build_photonmap (src/photonmap.rs:23-29): sort-by-cell grid over the given
+ * photons (n x 3 positions / directions, wl 0..2), power pw, radius^2 r2. */
+int ppm_photonmap_build(ppm_ctx *ctx, const double *pos, const double *dir,
+                        const uint8_t *wl, int64_t n, double power, double radius2);
+/* Build the map from the photons of the last ppm_trace_photons call. */
+int ppm_photonmap_from_trace(ppm_ctx *ctx, double radius2);
+
+/* kdtree.within(q, r2, squared_euclidean) (src/tracer.rs:180) per query with
+ * its own r2[i] <= the map's radius2.  offsets has nq+1 entries; idx receives
+ * photon indices (input order of ppm_photonmap_build), ascending per query.
+ * idx == NULL: sizes only.  *total = sum of neighbour counts. */
+int ppm_query_within(ppm_ctx *ctx, const double *q, int64_t nq, const double *r2,
+                     int64_t *offsets, int32_t *idx, int64_t cap, int64_t *total);
+
+/* estimate_radiance (src/tracer.rs:179-195): rgb (nq x 3) at positions with
+ * oriented normals, using the map's power and radius2 and filter pfilter. */
+int ppm_estimate(ppm_ctx *ctx, const double *pos, const double *nrm, int64_t nq,
+                 int32_t pfilter, double *rgb);
+
+/* ---- FP32 photon map (gather sweep) --------------------------------------- */
+/* A map of FP32 photons (n x 3 float positions, directions, wl).  Queries are
+ * FP32 positions with FP64 radii^2; membership is decided exactly as the f64
+ * predicate on the f32 values (FP32 test + FP64 recheck in the rounding band). */
+int ppm_photonmap_build_f32(ppm_ctx *ctx, const float *pos, const float *dir,
+                            const uint8_t *wl, int64_t n, double power, double radius2_max);
+int ppm_query_within_f32(ppm_ctx *ctx, const float *q, int64_t nq, const double *r2,
+                         int64_t *offsets, int32_t *idx, int64_t cap, int64_t *total);
+int ppm_estimate_f32(ppm_ctx *ctx, const float *pos, const float *nrm, int64_t nq,
+                     const double *r2, double *rgb);
+
+/* ---- progressive render ---------------------------------------------------- */
+/* Runs cfg->passes passes (emit + trace photons, build the map, eye trace,
+ * gather, PA radius shrink, FP64 running sum) and writes the averaged image
+ * (yreso x xreso x 3 doubles, row-major) -- the output of ppmpa (ppmpa.rs:36-41)
+ * averaged as util/averager.rb:66-69. */
+int ppm_render(ppm_ctx *ctx, const ppm_render_cfg *cfg, double *image_out);
+
+/* Device-resident stepping: begin sets up buffers, resets the running sum and
+ * the radius; step enqueues npasses passes on the context stream (async);
+ * image averages the passes done so far. */
+int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg);
+int ppm_render_step(ppm_ctx *ctx, int32_t npasses);
+int ppm_render_image(ppm_ctx *ctx, double *image_out);
+int ppm_render_pass_image(ppm_ctx *ctx, double *image_out);  /* the last pass alone */
+int ppm_render_stats(ppm_ctx *ctx, ppm_stats *out);
+/* Record per-stage CUDA events inside every pass (adds event nodes). */
+int ppm_set_stage_timing(ppm_ctx *ctx, int32_t on);
+const char *ppm_stage_name(int32_t stage);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PPM_API_H */

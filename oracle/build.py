@@ -1,0 +1,32 @@
+"""Build recipe for the CPU FP64 oracle (test infrastructure only).
+
+Compiles oracle/ppm_oracle.c into oracle/_build/libppm_oracle.so with FMA
+contraction disabled, so that f64 results follow the source's evaluation
+order on both x86-64 and aarch64 hosts.  The reference itself (Rust) cannot
+be compiled here, so there is no oracle/_ref build.
+"""
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT_DIR, "libppm_oracle.so")
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "ppm_oracle.c")
+    hdr = os.path.join(HERE, "ppm_oracle.h")
+    os.makedirs(OUT_DIR, exist_ok=True)
+    if (not force and os.path.exists(LIB)
+            and os.path.getmtime(LIB) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
+        return LIB
+    cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp",
+           "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unused-function",
+           src, "-o", LIB + ".tmp", "-lm"]
+    subprocess.check_call(cmd)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True))

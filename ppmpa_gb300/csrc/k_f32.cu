@@ -1,0 +1,60 @@
+// k_f32.cu -- FP32 mixed-precision path instantiations (FMA contraction on).
+// FP64 remains only in the band recheck of the in-radius test, the flux
+// normalisation and the image accumulation.
+#define PPM_BUILD_F32 1
+#include "ppm_launch.h"
+
+namespace ppm {
+
+void launch_trace_f(const SceneView<float> &sc, const EmitPlan &plan, uint64_t seed, PassState *st, int uc,
+                    PhotonBuf<float> out, unsigned long long cap, int grid, cudaStream_t s) {
+    k_trace_photons<float><<<grid, 256, 0, s>>>(sc, plan, seed, st, uc, out, cap);
+}
+void launch_bbox_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s) {
+    k_bbox<float><<<grid, 256, 0, s>>>(buf, st, n_fixed);
+}
+void launch_hist_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, uint32_t *count, uint2 *keyrank, int grid,
+                   cudaStream_t s) {
+    k_cell_hist<float><<<grid, 256, 0, s>>>(buf, st, n_fixed, count, keyrank);
+}
+void launch_scatter_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, const uint32_t *start,
+                      const uint2 *keyrank, int grid, cudaStream_t s) {
+    k_scatter<float><<<grid, 256, 0, s>>>(buf, st, n_fixed, start, keyrank);
+}
+void launch_eye_f(const SceneView<float> &sc, const DCamera<float> &cam, uint64_t seed, PassState *st, int uc,
+                  HitPoint<float> *hits, unsigned long long hit_cap, double *pass_img, int grid, cudaStream_t s) {
+    k_eye<float><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, hits, hit_cap, pass_img);
+}
+void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
+                     const uint32_t *start, double pw, const double *q_r2, int pfilter, int mode, GatherOutF out,
+                     int grid, cudaStream_t s) {
+    k_gather_f<<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pw, q_r2, pfilter, mode, out);
+}
+void launch_within_f(const float *q, long long nq, const double *q_r2, const PassState *st, const float4 *smap,
+                     const uint32_t *start, const int32_t *sidx, unsigned long long *counts,
+                     const unsigned long long *offsets, int32_t *idx_out, int grid, cudaStream_t s) {
+    k_within<float, float4><<<grid, 256, 0, s>>>(q, nq, q_r2, st, smap, start, sidx, counts, offsets, idx_out);
+}
+void launch_make_queries_f(const float *pos, const float *nrm, long long n, HitPoint<float> *hits, cudaStream_t s) {
+    if (n <= 0) return;
+    k_make_queries<float><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(pos, nrm, n, hits);
+}
+void launch_intersect_f(const SceneView<float> &sc, const double *rays, long long n, double *t, int32_t *obj,
+                        cudaStream_t s) {
+    if (n <= 0) return;
+    k_intersect<float><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(sc, rays, n, t, obj, nullptr);
+}
+
+__global__ void k_pack_photons(const float *pos, const float *dir, const uint8_t *wl, long long n, float4 *raw) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    raw[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2],
+                         __uint_as_float(oct_pack(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2], wl[i])));
+}
+void launch_pack_photons_f(const float *pos, const float *dir, const uint8_t *wl, long long n, float4 *raw,
+                           cudaStream_t s) {
+    if (n <= 0) return;
+    k_pack_photons<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(pos, dir, wl, n, raw);
+}
+
+}  // namespace ppm

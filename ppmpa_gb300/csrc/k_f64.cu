@@ -1,0 +1,48 @@
+// k_f64.cu -- FP64 (plain) path instantiations.  Built with --fmad=false:
+// no multiply-add contraction, so each double expression rounds as written
+// and the photon paths match the FP64 host restatement bit for bit.
+#define PPM_BUILD_F64 1
+#include "ppm_launch.h"
+
+namespace ppm {
+
+void launch_trace_d(const SceneView<double> &sc, const EmitPlan &plan, uint64_t seed, PassState *st, int uc,
+                    PhotonBuf<double> out, unsigned long long cap, int grid, cudaStream_t s) {
+    k_trace_photons<double><<<grid, 256, 0, s>>>(sc, plan, seed, st, uc, out, cap);
+}
+void launch_bbox_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s) {
+    k_bbox<double><<<grid, 256, 0, s>>>(buf, st, n_fixed);
+}
+void launch_hist_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, uint32_t *count, uint2 *keyrank, int grid,
+                   cudaStream_t s) {
+    k_cell_hist<double><<<grid, 256, 0, s>>>(buf, st, n_fixed, count, keyrank);
+}
+void launch_scatter_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, const uint32_t *start,
+                      const uint2 *keyrank, int grid, cudaStream_t s) {
+    k_scatter<double><<<grid, 256, 0, s>>>(buf, st, n_fixed, start, keyrank);
+}
+void launch_eye_d(const SceneView<double> &sc, const DCamera<double> &cam, uint64_t seed, PassState *st, int uc,
+                  HitPoint<double> *hits, unsigned long long hit_cap, double *pass_img, int grid, cudaStream_t s) {
+    k_eye<double><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, hits, hit_cap, pass_img);
+}
+void launch_gather_d(const HitPoint<double> *hits, PassState *st, long long n_fixed, const double4 *spos,
+                     const double4 *sdir, const uint32_t *start, double pw, int pfilter, int mode, GatherOutD out,
+                     int grid, cudaStream_t s) {
+    k_gather_d<<<grid, 256, 0, s>>>(hits, st, n_fixed, spos, sdir, start, pw, pfilter, mode, out);
+}
+void launch_within_d(const double *q, long long nq, const double *q_r2, const PassState *st, const double4 *smap,
+                     const uint32_t *start, unsigned long long *counts, const unsigned long long *offsets,
+                     int32_t *idx_out, int grid, cudaStream_t s) {
+    k_within<double, double4><<<grid, 256, 0, s>>>(q, nq, q_r2, st, smap, start, nullptr, counts, offsets, idx_out);
+}
+void launch_make_queries_d(const double *pos, const double *nrm, long long n, HitPoint<double> *hits, cudaStream_t s) {
+    if (n <= 0) return;
+    k_make_queries<double><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(pos, nrm, n, hits);
+}
+void launch_intersect_d(const SceneView<double> &sc, const double *rays, long long n, double *t, int32_t *obj,
+                        double *nrm, cudaStream_t s) {
+    if (n <= 0) return;
+    k_intersect<double><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(sc, rays, n, t, obj, nrm);
+}
+
+}  // namespace ppm

@@ -1,0 +1,184 @@
+// k_grid.cu -- pass bookkeeping, grid sizing and the cell-count scan.
+//
+// Every per-pass parameter lives in device memory (PassState), so one pass
+// can be captured once as a CUDA graph and replayed: the PA radius
+// recurrence r2_{k+1} = r2_k * ((k+o)+alpha)/((k+o)+1) (util/iterator.rb:33-38)
+// runs on the device in FP64 in k_pass_end.
+#include "ppm_launch.h"
+
+namespace ppm {
+
+__global__ void k_pass_begin(PassState *st) {
+    if (threadIdx.x != 0) return;
+    st->n_stored = 0;
+    st->n_hits = 0;
+    st->candidates = 0;
+    st->in_radius = 0;
+    for (int a = 0; a < 3; a++) {
+        st->bb_lo[a] = ord_enc(1e300);
+        st->bb_hi[a] = ord_enc(-1e300);
+    }
+}
+
+// Grid over the photon bounds with cells of r/k * (1 + 1/128) (k = cells per
+// radius).  The margin keeps |p - q| <= r  =>  |cell(p) - cell(q)| <= ext per
+// axis under FP32 rounding of the cell coordinate (<= 3 ulp of <= 8192 cells).
+__global__ void k_grid_setup(PassState *st, double r2_override) {
+    if (threadIdx.x != 0) return;
+    double r2 = r2_override > 0.0 ? r2_override : st->r2;
+    double r = sqrt(r2);
+    double lo[3], hi[3];
+    bool empty = false;
+    for (int a = 0; a < 3; a++) {
+        lo[a] = ord_dec(st->bb_lo[a]);
+        hi[a] = ord_dec(st->bb_hi[a]);
+        if (!(lo[a] <= hi[a])) empty = true;
+    }
+    if (empty) for (int a = 0; a < 3; a++) { lo[a] = 0.0; hi[a] = 0.0; }
+    double k = st->cell_factor > 0.0 ? st->cell_factor : 1.0;
+    double c = r / k * (1.0 + 1.0 / 128.0);
+    if (!(c > 0.0)) c = 1.0;
+    long long dim[3] = {1, 1, 1};
+    for (int it = 0; it < 400; it++) {
+        bool ok = true;
+        long long tot = 1;
+        for (int a = 0; a < 3; a++) {
+            dim[a] = (long long)floor((hi[a] - lo[a]) / c) + 1;
+            if (dim[a] > 8192) ok = false;
+            tot *= dim[a];
+        }
+        if (ok && tot <= st->cell_cap) break;
+        c *= 1.25;
+    }
+    GridParams g;
+    for (int a = 0; a < 3; a++) {
+        g.org[a] = lo[a];
+        g.orgf[a] = (float)lo[a];
+        g.dim[a] = (int32_t)dim[a];
+    }
+    g.cell = c;
+    g.inv = 1.0 / c;
+    g.invf = (float)(1.0 / c);
+    int ext = (int)ceil(r / c + 3e-3);
+    g.ext = ext < 1 ? 1 : (ext > 8 ? 8 : ext);
+    g.ncell = dim[0] * dim[1] * dim[2];
+    st->grid = g;
+}
+
+// exclusive scan of count[0, ncell) into start[0, ncell], zeroing count
+// (reduce -> scan of tile sums -> downsweep; no inter-block waiting)
+__global__ void __launch_bounds__(256) k_scan_reduce(const uint32_t *count, const PassState *st, uint32_t *block_sums) {
+    const long long n = st->grid.ncell;
+    const long long base = (long long)blockIdx.x * SCAN_TILE;
+    if (base >= n) return;
+    uint32_t s = 0;
+    for (int j = threadIdx.x; j < SCAN_TILE; j += 256) {
+        long long i = base + j;
+        if (i < n) s += count[i];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ uint32_t ws[8];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < 8; w++) t += ws[w];
+        block_sums[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_top(uint32_t *block_sums, const PassState *st) {
+    const long long n = st->grid.ncell;
+    const int nb = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
+    __shared__ uint32_t sh[1024];
+    // each thread owns up to 4 consecutive tile sums
+    uint32_t v[4], t = 0;
+    for (int j = 0; j < 4; j++) {
+        int i = threadIdx.x * 4 + j;
+        v[j] = i < nb ? block_sums[i] : 0u;
+        t += v[j];
+    }
+    sh[threadIdx.x] = t;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        uint32_t add = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0u;
+        __syncthreads();
+        sh[threadIdx.x] += add;
+        __syncthreads();
+    }
+    uint32_t run = sh[threadIdx.x] - t;   // exclusive prefix of this thread's group
+    for (int j = 0; j < 4; j++) {
+        int i = threadIdx.x * 4 + j;
+        if (i < nb) block_sums[i] = run;
+        run += v[j];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_scan_down(uint32_t *count, const PassState *st, const uint32_t *block_sums,
+                                                   uint32_t *start) {
+    const long long n = st->grid.ncell;
+    const long long base = (long long)blockIdx.x * SCAN_TILE;
+    if (base >= n) return;
+    constexpr int PER = SCAN_TILE / 256;   // 16 consecutive cells per thread
+    uint32_t v[PER], t = 0;
+    const long long my = base + (long long)threadIdx.x * PER;
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        long long i = my + j;
+        v[j] = i < n ? count[i] : 0u;
+        t += v[j];
+    }
+    // block exclusive scan of t
+    uint32_t incl = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((threadIdx.x & 31) >= (unsigned)o) incl += u;
+    }
+    __shared__ uint32_t ws[8];
+    if ((threadIdx.x & 31) == 31) ws[threadIdx.x >> 5] = incl;
+    __syncthreads();
+    uint32_t woff = 0;
+    for (int w = 0; w < (int)(threadIdx.x >> 5); w++) woff += ws[w];
+    uint32_t run = block_sums[blockIdx.x] + woff + incl - t;
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        long long i = my + j;
+        if (i < n) {
+            start[i] = run;
+            count[i] = 0u;
+        }
+        run += v[j];
+    }
+    if (my < n && my + PER >= n) start[n] = run;   // the thread holding the last cell
+}
+
+__global__ void k_accum(const double *pass_img, double *sum, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        sum[i] += pass_img[i];
+}
+
+__global__ void k_pass_end(PassState *st) {
+    if (threadIdx.x != 0) return;
+    double i = (double)(st->pass + st->offset);
+    st->r2 = st->r2 * ((i + st->alpha) / (i + 1.0));
+    st->pass += 1;
+}
+
+void launch_pass_begin(PassState *st, cudaStream_t s) { k_pass_begin<<<1, 32, 0, s>>>(st); }
+void launch_grid_setup(PassState *st, double r2_override, cudaStream_t s) { k_grid_setup<<<1, 32, 0, s>>>(st, r2_override); }
+void launch_scan(uint32_t *count, const PassState *st, uint32_t *block_sums, uint32_t *start, long long cell_cap,
+                 cudaStream_t s) {
+    int nb = (int)((cell_cap + SCAN_TILE - 1) / SCAN_TILE);
+    k_scan_reduce<<<nb, 256, 0, s>>>(count, st, block_sums);
+    k_scan_top<<<1, 1024, 0, s>>>(block_sums, st);
+    k_scan_down<<<nb, 256, 0, s>>>(count, st, block_sums, start);
+}
+int kernels_per_scan() { return 3; }
+void launch_accum(const double *pass_img, double *sum, long long n, cudaStream_t s) {
+    k_accum<<<(unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096), 256, 0, s>>>(pass_img, sum, n);
+}
+void launch_pass_end(PassState *st, cudaStream_t s) { k_pass_end<<<1, 32, 0, s>>>(st); }
+
+}  // namespace ppm

@@ -1,0 +1,1068 @@
+// ppm_api.cu -- host runtime behind include/ppm_api.h.
+//
+// A context owns one CUDA stream (plus a side stream that runs the eye pass
+// concurrently with photon tracing), all device buffers and the device-side
+// PassState.  One progressive pass is a fixed sequence of kernels whose
+// parameters live in device memory, so it is captured once as a CUDA graph
+// and replayed for every pass.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/ppm_api.h"
+#include "ppm_launch.h"
+
+using namespace ppm;
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+constexpr int N_STAGES = 5;
+const char *STAGE_NAMES[N_STAGES] = {"photon_trace", "map_build", "eye_trace", "gather", "accumulate"};
+constexpr int TIMING_SLOTS = 256;
+constexpr int HITS_PER_PIXEL = 8;
+constexpr long long CELL_CAP = 1LL << 24;
+
+thread_local std::string g_create_error;
+
+}  // namespace
+
+struct ppm_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t s = nullptr, s2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    std::string err;
+    uint64_t seed = 0;
+
+    // scene
+    std::vector<ppm_object> objs;
+    std::vector<ppm_material> mats;
+    std::vector<ppm_light> lights;
+    DevBuf objs_d, mats_d, lights_d, objs_f, mats_f, lights_f;
+    SceneView<double> sv_d{};
+    SceneView<float> sv_f{};
+    bool have_scene = false;
+    ppm_camera cam{};
+    DCamera<double> cam_d{};
+    DCamera<float> cam_f{};
+    bool have_cam = false;
+
+    // device state and buffers
+    PassState *st = nullptr;
+    DevBuf raw_d, spos, sdir, raw_f, sorted_f, sidx, keyrank, count, start, block_sums;
+    long long photon_cap_d = 0, photon_cap_f = 0;
+    DevBuf hits_d, hits_f;
+    long long hit_cap = 0;
+    DevBuf pass_img, sum_img;
+    long long npx = 0;
+    DevBuf scratch;   // parity entry-point staging
+
+    // parity photon map
+    int map_kind = 0;  // 0 none, 1 f64, 2 f32
+    long long map_n = 0;
+    double map_pw = 0.0, map_r2 = 0.0;
+    int last_trace_uc = 1;
+    double last_trace_pw = 0.0;
+
+    // render
+    ppm_render_cfg cfg{};
+    bool render_ready = false;
+    EmitPlan plan{};
+    double pw = 0.0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    long long passes_done = 0;
+    int kernels_per_pass = 0;
+
+    // timing
+    bool timing = false;
+    cudaEvent_t tev[TIMING_SLOTS][8];
+    bool tev_made = false;
+    int slot_head = 0, slot_pending = 0;
+    double stage_ms[16] = {0};
+    long long stage_calls[16] = {0};
+};
+
+static int set_err(ppm_ctx *c, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return set_err(ctx, e_ == cudaErrorMemoryAllocation ? PPM_ERR_OOM : PPM_ERR_CUDA,     \
+                           "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+static int ensure(ppm_ctx *ctx, DevBuf &b, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (b.bytes >= bytes) return PPM_OK;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    CK(cudaMalloc(&b.p, bytes));
+    b.bytes = bytes;
+    return PPM_OK;
+}
+
+static void release(DevBuf &b) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+}
+
+template <typename T> static T *as(DevBuf &b) { return static_cast<T *>(b.p); }
+
+#define TRY(x)                          \
+    do {                                \
+        int r_ = (x);                   \
+        if (r_ != PPM_OK) return r_;    \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// host-side derivations (same formulas and evaluation order as the reference)
+// ---------------------------------------------------------------------------
+namespace {
+struct HV {
+    double x, y, z;
+};
+HV hv(const double *p) { return {p[0], p[1], p[2]}; }
+HV hadd(HV a, HV b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+HV hsub(HV a, HV b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+HV hsm(double s, HV a) { return {s * a.x, s * a.y, s * a.z}; }
+double hdot(HV a, HV b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+HV hcross(HV a, HV b) { return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
+HV hnorm(HV a) {
+    double n = std::sqrt(hdot(a, a));
+    if (n == 0.0) return a;
+    double r = 1.0 / n;
+    return {a.x * r, a.y * r, a.z * r};
+}
+void hst(double *d, HV v) { d[0] = v.x; d[1] = v.y; d[2] = v.z; }
+}  // namespace
+
+extern "C" void ppm_camera_derive(ppm_camera *c) {
+    // camera.rs:150-175
+    const double SENSOR = 35.0 / 1000.0, ISO = 100.0, FNUM = 4.9, SHUT = 1.0 / 250.0;
+    HV eye = hv(c->eye_pos), tgt = hv(c->target), up = hv(c->upper);
+    HV ez = hnorm(hsub(tgt, eye));
+    HV ex = hnorm(hcross(up, ez));
+    HV ey = hnorm(hcross(ex, ez));
+    double step = (c->focus * SENSOR / c->focal_len) / (double)c->xreso;
+    HV esx = hsm(step, ex), esy = hsm(step, ey);
+    double ea = c->focal_len / c->f_number;
+    HV eex = hsm(ea, ex), eey = hsm(ea, ey);
+    double lx = (double)(c->xreso / 2), ly = (double)(c->yreso / 2);
+    HV orig = hsub(hsub(hsm(c->focus, ez), hsm(lx - 0.5, esx)), hsm(ly - 0.5, esy));
+    c->photon_power = c->blur ? c->iso_sens / ISO * FNUM / c->f_number * c->shut_speed / SHUT : 1.0;
+    hst(c->eye_dir, hnorm(hsub(tgt, eye)));
+    hst(c->origin, orig);
+    hst(c->esx, esx);
+    hst(c->esy, esy);
+    hst(c->eex, eex);
+    hst(c->eey, eey);
+}
+
+extern "C" void ppm_material_derive(ppm_material *m) {
+    // Surface::new_simple / new_ts, surface.rs:52 and :63-64
+    m->density_pow = 1.0 / (std::pow(10.0, 5.0 * (1.0 - std::sqrt(m->roughness))) + 1.0);
+    double r = m->roughness;
+    m->alpha = m->surface == PPM_SURF_TS ? r * r * r * r : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// scene conversion
+// ---------------------------------------------------------------------------
+template <typename T>
+static void conv_objects(const std::vector<ppm_object> &in, std::vector<DObject<T>> &out) {
+    out.resize(in.size());
+    for (size_t i = 0; i < in.size(); i++) {
+        const ppm_object &o = in[i];
+        DObject<T> &d = out[i];
+        d.shape = o.shape;
+        d.mat = o.material;
+        for (int a = 0; a < 3; a++) {
+            d.p[a] = (T)o.position[a];
+            d.n[a] = (T)o.nvec[a];
+            d.d1[a] = (T)o.dir1[a];
+            d.d2[a] = (T)o.dir2[a];
+        }
+        d.dist = (T)o.dist;
+        d.radius = (T)o.radius;
+    }
+}
+
+static uint32_t mat_flags(const ppm_material &m) {
+    auto eq = [](const double *c, double v) { return c[0] == v && c[1] == v && c[2] == v; };
+    uint32_t f = 0;
+    if (eq(m.color_spec, 0.0)) f |= 1u;
+    if (eq(m.color_spec, 1.0)) f |= 2u;
+    if (eq(m.color_diff, 0.0)) f |= 4u;
+    return f;
+}
+
+template <typename T>
+static void conv_materials(const std::vector<ppm_material> &in, std::vector<DMaterial<T>> &out) {
+    out.resize(in.size());
+    for (size_t i = 0; i < in.size(); i++) {
+        const ppm_material &m = in[i];
+        DMaterial<T> &d = out[i];
+        for (int a = 0; a < 3; a++) {
+            d.emit[a] = (T)m.emittance[a];
+            d.ior[a] = (T)m.ior[a];
+            d.cdiff[a] = (T)m.color_diff[a];
+            d.cspec[a] = (T)m.color_spec[a];
+        }
+        d.scatter = (T)m.scatter;
+        d.metal = (T)m.metalness;
+        d.rough = (T)m.roughness;
+        d.dpow = (T)m.density_pow;
+        d.surface = m.surface;
+        d.flags = mat_flags(m);
+    }
+}
+
+template <typename T>
+static void conv_lights(const std::vector<ppm_light> &in, std::vector<DLight<T>> &out) {
+    out.resize(in.size());
+    for (size_t i = 0; i < in.size(); i++) {
+        const ppm_light &l = in[i];
+        DLight<T> &d = out[i];
+        d.kind = l.kind;
+        d.pad = 0;
+        for (int a = 0; a < 3; a++) {
+            d.color[a] = (T)l.color[a];
+            d.pos[a] = (T)l.pos[a];
+            d.nvec[a] = (T)l.nvec[a];
+            d.d1[a] = (T)l.dir1[a];
+            d.d2[a] = (T)l.dir2[a];
+            d.dir[a] = (T)l.dir[a];
+        }
+        d.flux = (T)l.flux;
+    }
+}
+
+template <typename T>
+static void conv_camera(const ppm_camera &c, DCamera<T> &d) {
+    for (int a = 0; a < 3; a++) {
+        d.eye[a] = (T)c.eye_pos[a];
+        d.origin[a] = (T)c.origin[a];
+        d.esx[a] = (T)c.esx[a];
+        d.esy[a] = (T)c.esy[a];
+        d.eex[a] = (T)c.eex[a];
+        d.eey[a] = (T)c.eey[a];
+    }
+    d.xreso = c.xreso;
+    d.yreso = c.yreso;
+    d.jitter_aa = (c.progressive && c.antialias) ? 1 : 0;
+    d.blur = c.blur ? 1 : 0;
+}
+
+template <typename V>
+static int upload_vec(ppm_ctx *ctx, DevBuf &b, const std::vector<V> &v) {
+    TRY(ensure(ctx, b, sizeof(V) * (v.size() ? v.size() : 1)));
+    if (!v.empty()) CK(cudaMemcpyAsync(b.p, v.data(), sizeof(V) * v.size(), cudaMemcpyHostToDevice, ctx->s));
+    return PPM_OK;
+}
+
+// emission plan: ppmpa.rs:30-31 (pw = sum flux / N; n_l = round(flux_l / pw))
+static double make_plan(const std::vector<ppm_light> &lights, long long nphoton, EmitPlan &plan) {
+    double total = 0.0;
+    for (const auto &l : lights) total = total + l.flux;
+    double pw = total / (double)nphoton;
+    plan.n_lights = (int32_t)lights.size();
+    plan.first[0] = 0;
+    for (size_t i = 0; i < lights.size(); i++) plan.first[i + 1] = plan.first[i] + (int64_t)std::llround(lights[i].flux / pw);
+    return pw;
+}
+
+static int upload_state(ppm_ctx *ctx, double r2, int pass, double alpha, int offset, double cell_factor) {
+    PassState h;
+    std::memset(&h, 0, sizeof h);
+    h.r2 = r2;
+    h.alpha = alpha;
+    h.pass = pass;
+    h.offset = offset;
+    h.cell_factor = cell_factor;
+    h.cell_cap = CELL_CAP;
+    CK(cudaMemcpyAsync(ctx->st, &h, sizeof h, cudaMemcpyHostToDevice, ctx->s));
+    return PPM_OK;
+}
+
+static int read_state(ppm_ctx *ctx, PassState &h) {
+    CK(cudaMemcpyAsync(&h, ctx->st, sizeof h, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return PPM_OK;
+}
+
+static int ensure_grid(ppm_ctx *ctx) {
+    if (ctx->count.bytes == 0) {
+        TRY(ensure(ctx, ctx->count, sizeof(uint32_t) * CELL_CAP));
+        CK(cudaMemsetAsync(ctx->count.p, 0, sizeof(uint32_t) * CELL_CAP, ctx->s));
+    }
+    TRY(ensure(ctx, ctx->start, sizeof(uint32_t) * (CELL_CAP + 1)));
+    TRY(ensure(ctx, ctx->block_sums, sizeof(uint32_t) * (CELL_CAP / SCAN_TILE + 1)));
+    return PPM_OK;
+}
+
+static int grid_blocks(ppm_ctx *ctx, int per_sm) { return ctx->sm_count * per_sm; }
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+extern "C" int ppm_version(void) { return PPM_API_VERSION; }
+
+extern "C" const char *ppm_status_string(int s) {
+    switch (s) {
+    case PPM_OK: return "ok";
+    case PPM_ERR_INVALID_ARG: return "invalid argument";
+    case PPM_ERR_OOM: return "out of device memory";
+    case PPM_ERR_CAPACITY: return "capacity exceeded";
+    case PPM_ERR_TIMEOUT: return "timeout";
+    case PPM_ERR_CUDA: return "CUDA error";
+    case PPM_ERR_NOT_READY: return "not ready";
+    case PPM_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+    }
+}
+
+extern "C" int ppm_ctx_create(ppm_ctx **out, int device, uint64_t seed) {
+    if (!out) return PPM_ERR_INVALID_ARG;
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0 || device < 0 || device >= n) {
+        g_create_error = std::string("no CUDA device: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "count 0 or bad index");
+        return PPM_ERR_NO_DEVICE;
+    }
+    ppm_ctx *ctx = new ppm_ctx();
+    ctx->device = device;
+    ctx->seed = seed;
+    if (cudaSetDevice(device) != cudaSuccess) {
+        delete ctx;
+        return PPM_ERR_CUDA;
+    }
+    cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&ctx->s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->s2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMalloc(&ctx->st, sizeof(PassState)) != cudaSuccess) {
+        g_create_error = "stream/event/state allocation failed";
+        ppm_ctx_destroy(ctx);
+        return PPM_ERR_CUDA;
+    }
+    *out = ctx;
+    return PPM_OK;
+}
+
+static void drop_graph(ppm_ctx *ctx) {
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->graph) cudaGraphDestroy(ctx->graph);
+    ctx->graph_exec = nullptr;
+    ctx->graph = nullptr;
+}
+
+extern "C" int ppm_ctx_destroy(ppm_ctx *ctx) {
+    if (!ctx) return PPM_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->s) cudaStreamSynchronize(ctx->s);
+    if (ctx->s2) cudaStreamSynchronize(ctx->s2);
+    drop_graph(ctx);
+    DevBuf *bufs[] = {&ctx->objs_d, &ctx->mats_d, &ctx->lights_d, &ctx->objs_f, &ctx->mats_f, &ctx->lights_f,
+                      &ctx->raw_d, &ctx->spos, &ctx->sdir, &ctx->raw_f, &ctx->sorted_f, &ctx->sidx,
+                      &ctx->keyrank, &ctx->count, &ctx->start, &ctx->block_sums, &ctx->hits_d, &ctx->hits_f,
+                      &ctx->pass_img, &ctx->sum_img, &ctx->scratch};
+    for (DevBuf *b : bufs) release(*b);
+    if (ctx->st) cudaFree(ctx->st);
+    if (ctx->tev_made)
+        for (int i = 0; i < TIMING_SLOTS; i++)
+            for (int j = 0; j < 8; j++) cudaEventDestroy(ctx->tev[i][j]);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->s) cudaStreamDestroy(ctx->s);
+    if (ctx->s2) cudaStreamDestroy(ctx->s2);
+    delete ctx;
+    return PPM_OK;
+}
+
+extern "C" const char *ppm_last_error(const ppm_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+extern "C" void *ppm_ctx_stream(ppm_ctx *ctx) { return ctx ? (void *)ctx->s : nullptr; }
+extern "C" int ppm_ctx_sync(ppm_ctx *ctx) {
+    if (!ctx) return PPM_ERR_INVALID_ARG;
+    CK(cudaStreamSynchronize(ctx->s));
+    CK(cudaStreamSynchronize(ctx->s2));
+    return PPM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// scene and camera
+// ---------------------------------------------------------------------------
+extern "C" int ppm_scene_upload(ppm_ctx *ctx, const ppm_object *objs, int32_t n_objs, const ppm_material *mats,
+                                int32_t n_mats, const ppm_light *lights, int32_t n_lights) {
+    if (!ctx) return PPM_ERR_INVALID_ARG;
+    if (n_objs < 0 || n_mats < 0 || n_lights < 0 || n_lights > 16 || (n_objs && !objs) || (n_mats && !mats) ||
+        (n_lights && !lights))
+        return set_err(ctx, PPM_ERR_INVALID_ARG, "bad scene arrays (n_objs=%d n_mats=%d n_lights=%d, at most 16 lights)",
+                       n_objs, n_mats, n_lights);
+    for (int i = 0; i < n_objs; i++)
+        if (objs[i].material < 0 || objs[i].material >= n_mats || objs[i].shape < 0 || objs[i].shape > 4)
+            return set_err(ctx, PPM_ERR_INVALID_ARG, "object %d: bad material index %d or shape %d", i,
+                           objs[i].material, objs[i].shape);
+    for (int i = 0; i < n_lights; i++)
+        if (lights[i].kind < 0 || lights[i].kind > 2)
+            return set_err(ctx, PPM_ERR_INVALID_ARG, "light %d: bad kind %d", i, lights[i].kind);
+    cudaSetDevice(ctx->device);
+    ctx->objs.assign(objs, objs + n_objs);
+    ctx->mats.assign(mats, mats + n_mats);
+    ctx->lights.assign(lights, lights + n_lights);
+    std::vector<DObject<double>> od;
+    std::vector<DObject<float>> of;
+    std::vector<DMaterial<double>> md;
+    std::vector<DMaterial<float>> mf;
+    std::vector<DLight<double>> ld;
+    std::vector<DLight<float>> lf;
+    conv_objects(ctx->objs, od);
+    conv_objects(ctx->objs, of);
+    conv_materials(ctx->mats, md);
+    conv_materials(ctx->mats, mf);
+    conv_lights(ctx->lights, ld);
+    conv_lights(ctx->lights, lf);
+    TRY(upload_vec(ctx, ctx->objs_d, od));
+    TRY(upload_vec(ctx, ctx->objs_f, of));
+    TRY(upload_vec(ctx, ctx->mats_d, md));
+    TRY(upload_vec(ctx, ctx->mats_f, mf));
+    TRY(upload_vec(ctx, ctx->lights_d, ld));
+    TRY(upload_vec(ctx, ctx->lights_f, lf));
+    CK(cudaStreamSynchronize(ctx->s));
+    ctx->sv_d = SceneView<double>{as<DObject<double>>(ctx->objs_d), as<DMaterial<double>>(ctx->mats_d),
+                                  as<DLight<double>>(ctx->lights_d), n_objs, n_mats, n_lights, 0};
+    ctx->sv_f = SceneView<float>{as<DObject<float>>(ctx->objs_f), as<DMaterial<float>>(ctx->mats_f),
+                                 as<DLight<float>>(ctx->lights_f), n_objs, n_mats, n_lights, 0};
+    ctx->have_scene = true;
+    ctx->render_ready = false;
+    drop_graph(ctx);
+    return PPM_OK;
+}
+
+extern "C" int ppm_camera_set(ppm_ctx *ctx, const ppm_camera *cam) {
+    if (!ctx || !cam) return PPM_ERR_INVALID_ARG;
+    if (cam->xreso <= 0 || cam->yreso <= 0 || (long long)cam->xreso * cam->yreso > (1LL << 28))
+        return set_err(ctx, PPM_ERR_INVALID_ARG, "bad resolution %dx%d", cam->xreso, cam->yreso);
+    ctx->cam = *cam;
+    ppm_camera_derive(&ctx->cam);
+    conv_camera(ctx->cam, ctx->cam_d);
+    conv_camera(ctx->cam, ctx->cam_f);
+    ctx->have_cam = true;
+    ctx->render_ready = false;
+    drop_graph(ctx);
+    return PPM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 parity entry points
+// ---------------------------------------------------------------------------
+extern "C" int ppm_intersect(ppm_ctx *ctx, const double *rays, int64_t n, double *t, int32_t *obj, double *nrm) {
+    if (!ctx || n < 0 || (n && (!rays || !t || !obj))) return PPM_ERR_INVALID_ARG;
+    if (!ctx->have_scene) return set_err(ctx, PPM_ERR_NOT_READY, "no scene uploaded");
+    if (n == 0) return PPM_OK;
+    cudaSetDevice(ctx->device);
+    size_t rb = sizeof(double) * 6 * n, tb = sizeof(double) * n, ob = sizeof(int32_t) * n, nb = sizeof(double) * 3 * n;
+    TRY(ensure(ctx, ctx->scratch, rb + tb + ob + nb + 64));
+    char *base = as<char>(ctx->scratch);
+    double *d_rays = (double *)base, *d_t = (double *)(base + rb);
+    double *d_n = (double *)(base + rb + tb);
+    int32_t *d_o = (int32_t *)(base + rb + tb + nb);
+    CK(cudaMemcpyAsync(d_rays, rays, rb, cudaMemcpyHostToDevice, ctx->s));
+    launch_intersect_d(ctx->sv_d, d_rays, n, d_t, d_o, nrm ? d_n : nullptr, ctx->s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(t, d_t, tb, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaMemcpyAsync(obj, d_o, ob, cudaMemcpyDeviceToHost, ctx->s));
+    if (nrm) CK(cudaMemcpyAsync(nrm, d_n, nb, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return PPM_OK;
+}
+
+extern "C" int ppm_intersect_f32(ppm_ctx *ctx, const double *rays, int64_t n, double *t, int32_t *obj) {
+    if (!ctx || n < 0 || (n && (!rays || !t || !obj))) return PPM_ERR_INVALID_ARG;
+    if (!ctx->have_scene) return set_err(ctx, PPM_ERR_NOT_READY, "no scene uploaded");
+    if (n == 0) return PPM_OK;
+    cudaSetDevice(ctx->device);
+    size_t rb = sizeof(double) * 6 * n, tb = sizeof(double) * n, ob = sizeof(int32_t) * n;
+    TRY(ensure(ctx, ctx->scratch, rb + tb + ob + 64));
+    char *base = as<char>(ctx->scratch);
+    double *d_rays = (double *)base, *d_t = (double *)(base + rb);
+    int32_t *d_o = (int32_t *)(base + rb + tb);
+    CK(cudaMemcpyAsync(d_rays, rays, rb, cudaMemcpyHostToDevice, ctx->s));
+    launch_intersect_f(ctx->sv_f, d_rays, n, d_t, d_o, ctx->s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(t, d_t, tb, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaMemcpyAsync(obj, d_o, ob, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return PPM_OK;
+}
+
+static int ensure_photons_d(ppm_ctx *ctx, long long cap) {
+    TRY(ensure(ctx, ctx->raw_d, sizeof(PhotonD) * cap));
+    TRY(ensure(ctx, ctx->spos, sizeof(double4) * cap));
+    TRY(ensure(ctx, ctx->sdir, sizeof(double4) * cap));
+    TRY(ensure(ctx, ctx->keyrank, sizeof(uint2) * cap));
+    ctx->photon_cap_d = std::max(ctx->photon_cap_d, cap);
+    return ensure_grid(ctx);
+}
+
+static int ensure_photons_f(ppm_ctx *ctx, long long cap, bool with_idx) {
+    TRY(ensure(ctx, ctx->raw_f, sizeof(float4) * cap));
+    TRY(ensure(ctx, ctx->sorted_f, sizeof(float4) * cap));
+    TRY(ensure(ctx, ctx->keyrank, sizeof(uint2) * cap));
+    if (with_idx) TRY(ensure(ctx, ctx->sidx, sizeof(int32_t) * cap));
+    ctx->photon_cap_f = std::max(ctx->photon_cap_f, cap);
+    return ensure_grid(ctx);
+}
+
+extern "C" int ppm_trace_photons(ppm_ctx *ctx, int64_t nphoton, int32_t use_classic, uint32_t pass, int64_t *n_stored,
+                                 double *power, int64_t *n_emitted) {
+    if (!ctx || nphoton <= 0) return PPM_ERR_INVALID_ARG;
+    if (!ctx->have_scene || ctx->lights.empty()) return set_err(ctx, PPM_ERR_NOT_READY, "no scene with lights");
+    cudaSetDevice(ctx->device);
+    EmitPlan plan;
+    double pw = make_plan(ctx->lights, nphoton, plan);
+    long long nem = plan.first[plan.n_lights];
+    if (nem > 0x7fffffffLL) return set_err(ctx, PPM_ERR_INVALID_ARG, "too many photons");
+    long long cap = std::max(1LL, nem * MAX_TRACE);
+    TRY(ensure_photons_d(ctx, cap));
+    TRY(upload_state(ctx, 0.0, (int)pass, 0.0, 1, 1.0));
+    PhotonBuf<double> pb{as<PhotonD>(ctx->raw_d), as<double4>(ctx->spos), as<double4>(ctx->sdir)};
+    launch_trace_d(ctx->sv_d, plan, ctx->seed, ctx->st, use_classic ? 1 : 0, pb, (unsigned long long)cap,
+                   grid_blocks(ctx, 8), ctx->s);
+    CK(cudaGetLastError());
+    PassState h;
+    TRY(read_state(ctx, h));
+    if (h.overflow & 1u) return set_err(ctx, PPM_ERR_CAPACITY, "photon buffer overflow");
+    ctx->map_n = (long long)h.n_stored;
+    ctx->last_trace_pw = pw;
+    ctx->last_trace_uc = use_classic;
+    if (n_stored) *n_stored = (int64_t)h.n_stored;
+    if (power) *power = pw;
+    if (n_emitted) *n_emitted = nem;
+    ctx->map_kind = 0;
+    return PPM_OK;
+}
+
+extern "C" int ppm_photons_download(ppm_ctx *ctx, double *pos, double *dir, uint8_t *wl, int32_t *emit_idx,
+                                    int8_t *level, int64_t cap) {
+    if (!ctx) return PPM_ERR_INVALID_ARG;
+    long long n = ctx->map_n;
+    if (cap < n) return set_err(ctx, PPM_ERR_CAPACITY, "need room for %lld photons", n);
+    std::vector<PhotonD> h((size_t)n);
+    if (n) {
+        CK(cudaMemcpyAsync(h.data(), ctx->raw_d.p, sizeof(PhotonD) * n, cudaMemcpyDeviceToHost, ctx->s));
+        CK(cudaStreamSynchronize(ctx->s));
+    }
+    for (long long i = 0; i < n; i++) {
+        for (int a = 0; a < 3; a++) {
+            if (pos) pos[3 * i + a] = h[i].pos[a];
+            if (dir) dir[3 * i + a] = h[i].dir[a];
+        }
+        if (wl) wl[i] = h[i].wl;
+        if (emit_idx) emit_idx[i] = h[i].emit;
+        if (level) level[i] = h[i].level;
+    }
+    return PPM_OK;
+}
+
+// build the sorted FP64 map from raw_d[0, n)
+static int build_map_d(ppm_ctx *ctx, long long n, double r2, double pw) {
+    PhotonBuf<double> pb{as<PhotonD>(ctx->raw_d), as<double4>(ctx->spos), as<double4>(ctx->sdir)};
+    TRY(upload_state(ctx, r2, 0, 0.0, 1, 1.0));
+    launch_pass_begin(ctx->st, ctx->s);
+    int g = grid_blocks(ctx, 4);
+    launch_bbox_d(pb, ctx->st, n, g, ctx->s);
+    launch_grid_setup(ctx->st, r2, ctx->s);
+    launch_hist_d(pb, ctx->st, n, as<uint32_t>(ctx->count), as<uint2>(ctx->keyrank), g, ctx->s);
+    launch_scan(as<uint32_t>(ctx->count), ctx->st, as<uint32_t>(ctx->block_sums), as<uint32_t>(ctx->start), CELL_CAP,
+                ctx->s);
+    launch_scatter_d(pb, ctx->st, n, as<uint32_t>(ctx->start), as<uint2>(ctx->keyrank), g, ctx->s);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->s));
+    ctx->map_kind = 1;
+    ctx->map_n = n;
+    ctx->map_pw = pw;
+    ctx->map_r2 = r2;
+    return PPM_OK;
+}
+
+extern "C" int ppm_photonmap_build(ppm_ctx *ctx, const double *pos, const double *dir, const uint8_t *wl, int64_t n,
+                                   double power, double radius2) {
+    if (!ctx || n < 0 || (n && (!pos || !dir || !wl)) || !(radius2 > 0.0)) return PPM_ERR_INVALID_ARG;
+    if (n > 0x7fffffffLL) return set_err(ctx, PPM_ERR_INVALID_ARG, "at most 2^31-1 photons");
+    cudaSetDevice(ctx->device);
+    drop_graph(ctx);
+    ctx->render_ready = false;
+    TRY(ensure_photons_d(ctx, std::max<long long>(n, 1)));
+    std::vector<PhotonD> h((size_t)n);
+    for (long long i = 0; i < n; i++) {
+        for (int a = 0; a < 3; a++) { h[i].pos[a] = pos[3 * i + a]; h[i].dir[a] = dir[3 * i + a]; }
+        if (wl[i] > 2) return set_err(ctx, PPM_ERR_INVALID_ARG, "photon %lld: wavelength %d > 2", i, (int)wl[i]);
+        h[i].wl = wl[i];
+        h[i].emit = (int32_t)i;
+        h[i].level = 0;
+        h[i].pad = 0;
+    }
+    if (n) CK(cudaMemcpyAsync(ctx->raw_d.p, h.data(), sizeof(PhotonD) * n, cudaMemcpyHostToDevice, ctx->s));
+    return build_map_d(ctx, n, radius2, power);
+}
+
+extern "C" int ppm_photonmap_from_trace(ppm_ctx *ctx, double radius2) {
+    if (!ctx || !(radius2 > 0.0)) return PPM_ERR_INVALID_ARG;
+    if (ctx->raw_d.p == nullptr) return set_err(ctx, PPM_ERR_NOT_READY, "no traced photons");
+    cudaSetDevice(ctx->device);
+    return build_map_d(ctx, ctx->map_n, radius2, ctx->last_trace_pw);
+}
+
+static int check_r2(ppm_ctx *ctx, const double *r2, int64_t nq) {
+    for (int64_t i = 0; i < nq; i++)
+        if (!(r2[i] >= 0.0) || r2[i] > ctx->map_r2 * (1.0 + 1e-12))
+            return set_err(ctx, PPM_ERR_INVALID_ARG, "query %lld: r2 %.17g outside [0, map radius2 %.17g]", (long long)i,
+                           r2[i], ctx->map_r2);
+    return PPM_OK;
+}
+
+// shared count -> offsets -> fill flow for both map precisions
+template <typename Launch>
+static int within_flow(ppm_ctx *ctx, int64_t nq, int64_t *offsets, int32_t *idx, int64_t cap, int64_t *total,
+                       char *d_base, Launch launch) {
+    unsigned long long *d_counts = (unsigned long long *)d_base;
+    launch(d_counts, (const unsigned long long *)nullptr, (int32_t *)nullptr);
+    CK(cudaGetLastError());
+    std::vector<unsigned long long> cnt((size_t)nq);
+    if (nq) CK(cudaMemcpyAsync(cnt.data(), d_counts, sizeof(unsigned long long) * nq, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    std::vector<unsigned long long> off((size_t)nq + 1);
+    unsigned long long run = 0;
+    for (int64_t i = 0; i < nq; i++) { off[i] = run; run += cnt[i]; }
+    off[nq] = run;
+    if (total) *total = (int64_t)run;
+    if (offsets)
+        for (int64_t i = 0; i <= nq; i++) offsets[i] = (int64_t)off[i];
+    if (!idx) return PPM_OK;
+    if ((int64_t)run > cap) return set_err(ctx, PPM_ERR_CAPACITY, "idx needs %llu entries, cap %lld", run, (long long)cap);
+    DevBuf out;
+    size_t ob = sizeof(int32_t) * (run ? run : 1), fb = sizeof(unsigned long long) * (nq + 1);
+    if (cudaMalloc(&out.p, ob + fb) != cudaSuccess) return set_err(ctx, PPM_ERR_OOM, "no memory for %llu indices", run);
+    int32_t *d_idx = (int32_t *)out.p;
+    unsigned long long *d_off = (unsigned long long *)((char *)out.p + ob);
+    cudaMemcpyAsync(d_off, off.data(), fb, cudaMemcpyHostToDevice, ctx->s);
+    launch((unsigned long long *)nullptr, (const unsigned long long *)d_off, d_idx);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(idx, d_idx, sizeof(int32_t) * run, cudaMemcpyDeviceToHost, ctx->s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->s);
+    cudaFree(out.p);
+    if (e != cudaSuccess) return set_err(ctx, PPM_ERR_CUDA, "within fill: %s", cudaGetErrorString(e));
+    for (int64_t i = 0; i < nq; i++) std::sort(idx + off[i], idx + off[i + 1]);
+    return PPM_OK;
+}
+
+extern "C" int ppm_query_within(ppm_ctx *ctx, const double *q, int64_t nq, const double *r2, int64_t *offsets,
+                                int32_t *idx, int64_t cap, int64_t *total) {
+    if (!ctx || nq < 0 || (nq && (!q || !r2))) return PPM_ERR_INVALID_ARG;
+    if (ctx->map_kind != 1) return set_err(ctx, PPM_ERR_NOT_READY, "no FP64 photon map built");
+    TRY(check_r2(ctx, r2, nq));
+    cudaSetDevice(ctx->device);
+    size_t qb = sizeof(double) * 3 * nq, rb = sizeof(double) * nq, cb = sizeof(unsigned long long) * (nq + 1);
+    TRY(ensure(ctx, ctx->scratch, qb + rb + cb + 64));
+    char *base = as<char>(ctx->scratch);
+    double *d_q = (double *)base, *d_r2 = (double *)(base + qb);
+    if (nq) {
+        CK(cudaMemcpyAsync(d_q, q, qb, cudaMemcpyHostToDevice, ctx->s));
+        CK(cudaMemcpyAsync(d_r2, r2, rb, cudaMemcpyHostToDevice, ctx->s));
+    }
+    int g = grid_blocks(ctx, 8);
+    return within_flow(ctx, nq, offsets, idx, cap, total, base + qb + rb,
+                       [&](unsigned long long *counts, const unsigned long long *off, int32_t *out) {
+                           launch_within_d(d_q, nq, d_r2, ctx->st, as<double4>(ctx->spos), as<uint32_t>(ctx->start),
+                                           counts, off, out, g, ctx->s);
+                       });
+}
+
+extern "C" int ppm_estimate(ppm_ctx *ctx, const double *pos, const double *nrm, int64_t nq, int32_t pfilter,
+                            double *rgb) {
+    if (!ctx || nq < 0 || (nq && (!pos || !nrm || !rgb)) || pfilter < 0 || pfilter > 2) return PPM_ERR_INVALID_ARG;
+    if (ctx->map_kind != 1) return set_err(ctx, PPM_ERR_NOT_READY, "no FP64 photon map built");
+    if (nq == 0) return PPM_OK;
+    cudaSetDevice(ctx->device);
+    size_t pb = sizeof(double) * 3 * nq, hb = sizeof(HitPoint<double>) * nq, ob = sizeof(double) * 3 * nq;
+    TRY(ensure(ctx, ctx->scratch, 2 * pb + hb + ob + 256));
+    char *base = as<char>(ctx->scratch);
+    double *d_p = (double *)base, *d_n = (double *)(base + pb);
+    HitPoint<double> *d_h = (HitPoint<double> *)(base + 2 * pb);
+    double *d_o = (double *)(base + 2 * pb + hb);
+    CK(cudaMemcpyAsync(d_p, pos, pb, cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(d_n, nrm, pb, cudaMemcpyHostToDevice, ctx->s));
+    launch_make_queries_d(d_p, d_n, nq, d_h, ctx->s);
+    GatherOutD go{nullptr, d_o, nullptr};
+    launch_gather_d(d_h, ctx->st, nq, as<double4>(ctx->spos), as<double4>(ctx->sdir), as<uint32_t>(ctx->start),
+                    ctx->map_pw, pfilter, 1, go, grid_blocks(ctx, 8), ctx->s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(rgb, d_o, ob, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return PPM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 photon map (gather sweep)
+// ---------------------------------------------------------------------------
+extern "C" int ppm_photonmap_build_f32(ppm_ctx *ctx, const float *pos, const float *dir, const uint8_t *wl, int64_t n,
+                                       double power, double radius2_max) {
+    if (!ctx || n < 0 || (n && (!pos || !dir || !wl)) || !(radius2_max > 0.0)) return PPM_ERR_INVALID_ARG;
+    if (n > 0x7fffffffLL) return set_err(ctx, PPM_ERR_INVALID_ARG, "at most 2^31-1 photons");
+    for (int64_t i = 0; i < n; i++)
+        if (wl[i] > 2) return set_err(ctx, PPM_ERR_INVALID_ARG, "photon %lld: wavelength %d > 2", (long long)i, (int)wl[i]);
+    cudaSetDevice(ctx->device);
+    drop_graph(ctx);
+    ctx->render_ready = false;
+    TRY(ensure_photons_f(ctx, std::max<long long>(n, 1), true));
+    // stage host arrays (pos, dir: 12 B each, wl: 1 B) and pack on the device
+    size_t vb = sizeof(float) * 3 * n;
+    TRY(ensure(ctx, ctx->scratch, 2 * vb + n + 64));
+    char *base = as<char>(ctx->scratch);
+    float *d_pos = (float *)base, *d_dir = (float *)(base + vb);
+    uint8_t *d_wl = (uint8_t *)(base + 2 * vb);
+    if (n) {
+        CK(cudaMemcpyAsync(d_pos, pos, vb, cudaMemcpyHostToDevice, ctx->s));
+        CK(cudaMemcpyAsync(d_dir, dir, vb, cudaMemcpyHostToDevice, ctx->s));
+        CK(cudaMemcpyAsync(d_wl, wl, n, cudaMemcpyHostToDevice, ctx->s));
+    }
+    launch_pack_photons_f(d_pos, d_dir, d_wl, n, as<float4>(ctx->raw_f), ctx->s);
+    PhotonBuf<float> pb{as<float4>(ctx->raw_f), as<float4>(ctx->sorted_f), as<int32_t>(ctx->sidx)};
+    TRY(upload_state(ctx, radius2_max, 0, 0.0, 1, 2.0));
+    launch_pass_begin(ctx->st, ctx->s);
+    int g = grid_blocks(ctx, 4);
+    launch_bbox_f(pb, ctx->st, n, g, ctx->s);
+    launch_grid_setup(ctx->st, radius2_max, ctx->s);
+    launch_hist_f(pb, ctx->st, n, as<uint32_t>(ctx->count), as<uint2>(ctx->keyrank), g, ctx->s);
+    launch_scan(as<uint32_t>(ctx->count), ctx->st, as<uint32_t>(ctx->block_sums), as<uint32_t>(ctx->start), CELL_CAP,
+                ctx->s);
+    launch_scatter_f(pb, ctx->st, n, as<uint32_t>(ctx->start), as<uint2>(ctx->keyrank), g, ctx->s);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->s));
+    ctx->map_kind = 2;
+    ctx->map_n = n;
+    ctx->map_pw = power;
+    ctx->map_r2 = radius2_max;
+    return PPM_OK;
+}
+
+extern "C" int ppm_query_within_f32(ppm_ctx *ctx, const float *q, int64_t nq, const double *r2, int64_t *offsets,
+                                    int32_t *idx, int64_t cap, int64_t *total) {
+    if (!ctx || nq < 0 || (nq && (!q || !r2))) return PPM_ERR_INVALID_ARG;
+    if (ctx->map_kind != 2) return set_err(ctx, PPM_ERR_NOT_READY, "no FP32 photon map built");
+    TRY(check_r2(ctx, r2, nq));
+    cudaSetDevice(ctx->device);
+    size_t qb = sizeof(float) * 3 * nq, rb = sizeof(double) * nq, cb = sizeof(unsigned long long) * (nq + 1);
+    qb = (qb + 15) & ~(size_t)15;
+    TRY(ensure(ctx, ctx->scratch, qb + rb + cb + 64));
+    char *base = as<char>(ctx->scratch);
+    float *d_q = (float *)base;
+    double *d_r2 = (double *)(base + qb);
+    if (nq) {
+        CK(cudaMemcpyAsync(d_q, q, sizeof(float) * 3 * nq, cudaMemcpyHostToDevice, ctx->s));
+        CK(cudaMemcpyAsync(d_r2, r2, rb, cudaMemcpyHostToDevice, ctx->s));
+    }
+    int g = grid_blocks(ctx, 8);
+    return within_flow(ctx, nq, offsets, idx, cap, total, base + qb + rb,
+                       [&](unsigned long long *counts, const unsigned long long *off, int32_t *out) {
+                           launch_within_f(d_q, nq, d_r2, ctx->st, as<float4>(ctx->sorted_f), as<uint32_t>(ctx->start),
+                                           as<int32_t>(ctx->sidx), counts, off, out, g, ctx->s);
+                       });
+}
+
+extern "C" int ppm_estimate_f32(ppm_ctx *ctx, const float *pos, const float *nrm, int64_t nq, const double *r2,
+                                double *rgb) {
+    if (!ctx || nq < 0 || (nq && (!pos || !nrm || !r2 || !rgb))) return PPM_ERR_INVALID_ARG;
+    if (ctx->map_kind != 2) return set_err(ctx, PPM_ERR_NOT_READY, "no FP32 photon map built");
+    TRY(check_r2(ctx, r2, nq));
+    if (nq == 0) return PPM_OK;
+    cudaSetDevice(ctx->device);
+    size_t pb = (sizeof(float) * 3 * nq + 15) & ~(size_t)15, hb = sizeof(HitPoint<float>) * nq;
+    size_t rb = sizeof(double) * nq, ob = sizeof(double) * 3 * nq;
+    TRY(ensure(ctx, ctx->scratch, 2 * pb + hb + rb + ob + 256));
+    char *base = as<char>(ctx->scratch);
+    float *d_p = (float *)base, *d_n = (float *)(base + pb);
+    HitPoint<float> *d_h = (HitPoint<float> *)(base + 2 * pb);
+    double *d_r2 = (double *)(base + 2 * pb + hb);
+    double *d_o = (double *)(base + 2 * pb + hb + rb);
+    CK(cudaMemcpyAsync(d_p, pos, sizeof(float) * 3 * nq, cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(d_n, nrm, sizeof(float) * 3 * nq, cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(d_r2, r2, rb, cudaMemcpyHostToDevice, ctx->s));
+    launch_make_queries_f(d_p, d_n, nq, d_h, ctx->s);
+    GatherOutF go{nullptr, d_o, nullptr};
+    launch_gather_f(d_h, ctx->st, nq, as<float4>(ctx->sorted_f), as<uint32_t>(ctx->start), ctx->map_pw, d_r2, PF_NONE,
+                    1, go, grid_blocks(ctx, 8), ctx->s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(rgb, d_o, ob, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return PPM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// progressive render
+// ---------------------------------------------------------------------------
+extern "C" const char *ppm_stage_name(int32_t stage) {
+    return stage >= 0 && stage < N_STAGES ? STAGE_NAMES[stage] : "";
+}
+
+extern "C" int ppm_set_stage_timing(ppm_ctx *ctx, int32_t on) {
+    if (!ctx) return PPM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (on && !ctx->tev_made) {
+        for (int i = 0; i < TIMING_SLOTS; i++)
+            for (int j = 0; j < 8; j++) CK(cudaEventCreate(&ctx->tev[i][j]));
+        ctx->tev_made = true;
+    }
+    ctx->timing = on != 0;
+    return PPM_OK;
+}
+
+// event slot layout: 0 pass start, 1 after trace+bbox, 2 after map build,
+// 3 after gather, 4 after accumulate/end; 5/6 eye start/end on the side stream
+static int drain_timing(ppm_ctx *ctx) {
+    if (ctx->slot_pending == 0) return PPM_OK;
+    CK(cudaStreamSynchronize(ctx->s));
+    CK(cudaStreamSynchronize(ctx->s2));
+    for (int k = 0; k < ctx->slot_pending; k++) {
+        int slot = (ctx->slot_head - ctx->slot_pending + k + TIMING_SLOTS) % TIMING_SLOTS;
+        cudaEvent_t *e = ctx->tev[slot];
+        float ms;
+        const int pairs[N_STAGES][2] = {{0, 1}, {1, 2}, {5, 6}, {2, 3}, {3, 4}};
+        for (int st = 0; st < N_STAGES; st++) {
+            CK(cudaEventElapsedTime(&ms, e[pairs[st][0]], e[pairs[st][1]]));
+            ctx->stage_ms[st] += ms;
+            ctx->stage_calls[st] += 1;
+        }
+    }
+    ctx->slot_pending = 0;
+    return PPM_OK;
+}
+
+static int enqueue_pass(ppm_ctx *ctx, bool capture) {
+    const bool mixed = ctx->cfg.precision == PPM_PRECISION_MIXED;
+    const int uc = ctx->cfg.use_classic ? 1 : 0;
+    cudaStream_t s = ctx->s, s2 = ctx->s2;
+    cudaEvent_t *ev = nullptr;
+    if (ctx->timing && !capture) {
+        if (ctx->slot_pending == TIMING_SLOTS) TRY(drain_timing(ctx));
+        ev = ctx->tev[ctx->slot_head];
+        ctx->slot_head = (ctx->slot_head + 1) % TIMING_SLOTS;
+        ctx->slot_pending++;
+    }
+    int kernels = 0;
+    const int g8 = grid_blocks(ctx, 8), g4 = grid_blocks(ctx, 4);
+    if (ev) CK(cudaEventRecord(ev[0], s));
+    launch_pass_begin(ctx->st, s); kernels++;
+    // the eye pass does not depend on the photon map: run it on the side stream
+    CK(cudaEventRecord(ctx->ev_fork, s));
+    CK(cudaStreamWaitEvent(s2, ctx->ev_fork, 0));
+    if (ev) CK(cudaEventRecord(ev[5], s2));
+    long long eye_grid = std::min<long long>((ctx->npx + 127) / 128, (long long)ctx->sm_count * 16);
+    if (mixed)
+        launch_eye_f(ctx->sv_f, ctx->cam_f, ctx->cfg.seed, ctx->st, uc, as<HitPoint<float>>(ctx->hits_f),
+                     (unsigned long long)ctx->hit_cap, as<double>(ctx->pass_img), (int)eye_grid, s2);
+    else
+        launch_eye_d(ctx->sv_d, ctx->cam_d, ctx->cfg.seed, ctx->st, uc, as<HitPoint<double>>(ctx->hits_d),
+                     (unsigned long long)ctx->hit_cap, as<double>(ctx->pass_img), (int)eye_grid, s2);
+    kernels++;
+    if (ev) CK(cudaEventRecord(ev[6], s2));
+    CK(cudaEventRecord(ctx->ev_join, s2));
+    // photons
+    if (mixed) {
+        PhotonBuf<float> pb{as<float4>(ctx->raw_f), as<float4>(ctx->sorted_f), nullptr};
+        launch_trace_f(ctx->sv_f, ctx->plan, ctx->cfg.seed, ctx->st, uc, pb, (unsigned long long)ctx->photon_cap_f, g8, s);
+        launch_bbox_f(pb, ctx->st, -1, g4, s);
+        if (ev) CK(cudaEventRecord(ev[1], s));
+        launch_grid_setup(ctx->st, -1.0, s);
+        launch_hist_f(pb, ctx->st, -1, as<uint32_t>(ctx->count), as<uint2>(ctx->keyrank), g8, s);
+        launch_scan(as<uint32_t>(ctx->count), ctx->st, as<uint32_t>(ctx->block_sums), as<uint32_t>(ctx->start), CELL_CAP, s);
+        launch_scatter_f(pb, ctx->st, -1, as<uint32_t>(ctx->start), as<uint2>(ctx->keyrank), g8, s);
+    } else {
+        PhotonBuf<double> pb{as<PhotonD>(ctx->raw_d), as<double4>(ctx->spos), as<double4>(ctx->sdir)};
+        launch_trace_d(ctx->sv_d, ctx->plan, ctx->cfg.seed, ctx->st, uc, pb, (unsigned long long)ctx->photon_cap_d, g8, s);
+        launch_bbox_d(pb, ctx->st, -1, g4, s);
+        if (ev) CK(cudaEventRecord(ev[1], s));
+        launch_grid_setup(ctx->st, -1.0, s);
+        launch_hist_d(pb, ctx->st, -1, as<uint32_t>(ctx->count), as<uint2>(ctx->keyrank), g8, s);
+        launch_scan(as<uint32_t>(ctx->count), ctx->st, as<uint32_t>(ctx->block_sums), as<uint32_t>(ctx->start), CELL_CAP, s);
+        launch_scatter_d(pb, ctx->st, -1, as<uint32_t>(ctx->start), as<uint2>(ctx->keyrank), g8, s);
+    }
+    kernels += 5 + kernels_per_scan();
+    if (ev) CK(cudaEventRecord(ev[2], s));
+    CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+    if (mixed) {
+        GatherOutF go{as<double>(ctx->pass_img), nullptr, nullptr};
+        launch_gather_f(as<HitPoint<float>>(ctx->hits_f), ctx->st, -1, as<float4>(ctx->sorted_f), as<uint32_t>(ctx->start),
+                        ctx->pw, nullptr, ctx->cam.pfilter, 0, go, g8, s);
+    } else {
+        GatherOutD go{as<double>(ctx->pass_img), nullptr, nullptr};
+        launch_gather_d(as<HitPoint<double>>(ctx->hits_d), ctx->st, -1, as<double4>(ctx->spos), as<double4>(ctx->sdir),
+                        as<uint32_t>(ctx->start), ctx->pw, ctx->cam.pfilter, 0, go, g8, s);
+    }
+    kernels++;
+    if (ev) CK(cudaEventRecord(ev[3], s));
+    launch_accum(as<double>(ctx->pass_img), as<double>(ctx->sum_img), 3 * ctx->npx, s);
+    launch_pass_end(ctx->st, s);
+    kernels += 2;
+    if (ev) CK(cudaEventRecord(ev[4], s));
+    CK(cudaGetLastError());
+    ctx->kernels_per_pass = kernels;
+    return PPM_OK;
+}
+
+static double schedule_r2(const ppm_render_cfg &c, int upto) {
+    double r = c.radius0 * c.radius0;
+    for (int k = 0; k < upto; k++) {
+        double i = (double)(k + c.schedule_offset);
+        r = r * ((i + c.alpha) / (i + 1.0));
+    }
+    return r;
+}
+
+extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
+    if (!ctx || !cfg) return PPM_ERR_INVALID_ARG;
+    if (!ctx->have_scene || !ctx->have_cam || ctx->lights.empty())
+        return set_err(ctx, PPM_ERR_NOT_READY, "scene (with lights) and camera must be set first");
+    if (cfg->nphoton <= 0 || cfg->passes < 0 || !(cfg->radius0 > 0.0) || cfg->precision < 0 || cfg->precision > 1 ||
+        cfg->cell_factor < 0 || cfg->cell_factor > 2 || cfg->first_pass < 0)
+        return set_err(ctx, PPM_ERR_INVALID_ARG, "bad render configuration");
+    cudaSetDevice(ctx->device);
+    drop_graph(ctx);
+    ctx->cfg = *cfg;
+    ctx->pw = make_plan(ctx->lights, cfg->nphoton, ctx->plan);
+    long long nem = ctx->plan.first[ctx->plan.n_lights];
+    if (nem > 0x7fffffffLL / MAX_TRACE) return set_err(ctx, PPM_ERR_INVALID_ARG, "too many photons per pass");
+    long long cap = std::max(1LL, nem * MAX_TRACE);
+    ctx->npx = (long long)ctx->cam.xreso * ctx->cam.yreso;
+    ctx->hit_cap = ctx->npx * HITS_PER_PIXEL;
+    if (cfg->precision == PPM_PRECISION_MIXED) {
+        TRY(ensure_photons_f(ctx, cap, false));
+        TRY(ensure(ctx, ctx->hits_f, sizeof(HitPoint<float>) * ctx->hit_cap));
+    } else {
+        TRY(ensure_photons_d(ctx, cap));
+        TRY(ensure(ctx, ctx->hits_d, sizeof(HitPoint<double>) * ctx->hit_cap));
+    }
+    TRY(ensure(ctx, ctx->pass_img, sizeof(double) * 3 * ctx->npx));
+    TRY(ensure(ctx, ctx->sum_img, sizeof(double) * 3 * ctx->npx));
+    CK(cudaMemsetAsync(ctx->sum_img.p, 0, sizeof(double) * 3 * ctx->npx, ctx->s));
+    CK(cudaMemsetAsync(ctx->pass_img.p, 0, sizeof(double) * 3 * ctx->npx, ctx->s));
+    int cf = cfg->cell_factor ? cfg->cell_factor : 1;
+    TRY(upload_state(ctx, schedule_r2(*cfg, cfg->first_pass), cfg->first_pass, cfg->alpha, cfg->schedule_offset, (double)cf));
+    CK(cudaStreamSynchronize(ctx->s));
+    ctx->passes_done = 0;
+    ctx->map_kind = 0;
+    for (int i = 0; i < 16; i++) { ctx->stage_ms[i] = 0.0; ctx->stage_calls[i] = 0; }
+    ctx->slot_pending = 0;
+    if (cfg->use_graph) {
+        CK(cudaStreamBeginCapture(ctx->s, cudaStreamCaptureModeThreadLocal));
+        int r = enqueue_pass(ctx, true);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(ctx->s, &g);
+        if (r != PPM_OK) { if (g) cudaGraphDestroy(g); return r; }
+        if (e != cudaSuccess) return set_err(ctx, PPM_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+        ctx->graph = g;
+        CK(cudaGraphInstantiate(&ctx->graph_exec, g, 0));
+    }
+    ctx->render_ready = true;
+    return PPM_OK;
+}
+
+extern "C" int ppm_render_step(ppm_ctx *ctx, int32_t npasses) {
+    if (!ctx || npasses < 0) return PPM_ERR_INVALID_ARG;
+    if (!ctx->render_ready) return set_err(ctx, PPM_ERR_NOT_READY, "ppm_render_begin first");
+    cudaSetDevice(ctx->device);
+    for (int i = 0; i < npasses; i++) {
+        if (ctx->graph_exec && !ctx->timing) {
+            CK(cudaGraphLaunch(ctx->graph_exec, ctx->s));
+        } else {
+            TRY(enqueue_pass(ctx, false));
+        }
+        ctx->passes_done++;
+    }
+    return PPM_OK;
+}
+
+static int check_overflow(ppm_ctx *ctx, PassState &h) {
+    TRY(read_state(ctx, h));
+    if (h.overflow & 1u) return set_err(ctx, PPM_ERR_CAPACITY, "photon buffer overflow");
+    if (h.overflow & 2u) return set_err(ctx, PPM_ERR_CAPACITY, "hit-point buffer overflow (%d per pixel)", HITS_PER_PIXEL);
+    if (h.overflow & 4u) return set_err(ctx, PPM_ERR_CAPACITY, "eye stack overflow");
+    return PPM_OK;
+}
+
+extern "C" int ppm_render_image(ppm_ctx *ctx, double *image_out) {
+    if (!ctx || !image_out) return PPM_ERR_INVALID_ARG;
+    if (!ctx->render_ready) return set_err(ctx, PPM_ERR_NOT_READY, "ppm_render_begin first");
+    cudaSetDevice(ctx->device);
+    PassState h;
+    TRY(check_overflow(ctx, h));
+    CK(cudaMemcpyAsync(image_out, ctx->sum_img.p, sizeof(double) * 3 * ctx->npx, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    if (ctx->passes_done > 0) {
+        double d = (double)ctx->passes_done;
+        for (long long i = 0; i < 3 * ctx->npx; i++) image_out[i] = image_out[i] / d;
+    }
+    return PPM_OK;
+}
+
+extern "C" int ppm_render_pass_image(ppm_ctx *ctx, double *image_out) {
+    if (!ctx || !image_out) return PPM_ERR_INVALID_ARG;
+    if (!ctx->render_ready) return set_err(ctx, PPM_ERR_NOT_READY, "ppm_render_begin first");
+    cudaSetDevice(ctx->device);
+    PassState h;
+    TRY(check_overflow(ctx, h));
+    CK(cudaMemcpyAsync(image_out, ctx->pass_img.p, sizeof(double) * 3 * ctx->npx, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return PPM_OK;
+}
+
+extern "C" int ppm_render_stats(ppm_ctx *ctx, ppm_stats *out) {
+    if (!ctx || !out) return PPM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    std::memset(out, 0, sizeof *out);
+    PassState h;
+    TRY(read_state(ctx, h));
+    TRY(drain_timing(ctx));
+    out->photons_emitted = ctx->render_ready ? ctx->plan.first[ctx->plan.n_lights] : 0;
+    out->photons_stored = (int64_t)h.n_stored;
+    out->hit_points = (int64_t)h.n_hits;
+    out->grid_cells = h.grid.ncell;
+    out->passes_done = ctx->passes_done;
+    out->kernels_per_pass = ctx->kernels_per_pass;
+    out->n_stages = N_STAGES;
+    out->r2 = h.r2;
+    for (int i = 0; i < 16; i++) { out->stage_ms[i] = ctx->stage_ms[i]; out->stage_calls[i] = ctx->stage_calls[i]; }
+    out->candidates = (int64_t)h.candidates;
+    out->in_radius = (int64_t)h.in_radius;
+    return PPM_OK;
+}
+
+extern "C" int ppm_render(ppm_ctx *ctx, const ppm_render_cfg *cfg, double *image_out) {
+    if (!ctx || !cfg || !image_out) return PPM_ERR_INVALID_ARG;
+    TRY(ppm_render_begin(ctx, cfg));
+    TRY(ppm_render_step(ctx, cfg->passes));
+    return ppm_render_image(ctx, image_out);
+}

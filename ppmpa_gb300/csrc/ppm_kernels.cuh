@@ -1,0 +1,775 @@
+// ppm_kernels.cuh -- the pass kernels, templated on the arithmetic type.
+//
+//   trace   : emission + bounce loop, one thread per photon path with path
+//             regeneration; stored photons appended with warp-aggregated
+//             atomics (tracer.rs:31-125, ppmpa.rs:86-92)
+//   bbox    : bounds of the stored photons (grid extent)
+//   hist    : cell key + rank per photon (counting-sort histogram)
+//   scatter : photons moved into cell order (the photon map,
+//             photonmap.rs:23-29 -- a sort-by-cell grid replaces the kd-tree)
+//   eye     : camera rays + eye tree (tracer.rs:129-177) depth first with a
+//             per-thread stack; throughput-weighted hit points appended
+//   gather  : one warp per hit point scans the cell rows around it and sums
+//             photon_to_radiance over the exact in-radius set (tracer.rs:179-195)
+//   accum   : FP64 running sum of pass images (util/averager.rb:66-69)
+#pragma once
+#include "ppm_trace.cuh"
+
+namespace ppm {
+
+// ---------------------------------------------------------------------------
+// shared device state
+// ---------------------------------------------------------------------------
+struct GridParams {
+    double org[3];
+    double cell, inv;
+    float orgf[3];
+    float invf;
+    int32_t dim[3];
+    int32_t ext;
+    int64_t ncell;
+};
+
+struct PassState {
+    double r2;                 // radius^2 used by the current pass
+    double alpha;
+    int32_t pass;              // random-stream pass index
+    int32_t offset;            // PA schedule offset
+    unsigned long long n_stored;
+    unsigned long long n_hits;
+    unsigned int overflow;     // bit0 photons, bit1 hit points, bit2 eye stack
+    unsigned int pad;
+    unsigned long long bb_lo[3], bb_hi[3];   // orderable encodings of f64 bounds
+    GridParams grid;
+    unsigned long long candidates, in_radius;
+    double cell_factor;
+    int64_t cell_cap;
+};
+
+// monotone f64 <-> u64 encoding for atomicMin/atomicMax on bounds
+__device__ __forceinline__ unsigned long long ord_enc(double d) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
+}
+__device__ __forceinline__ double ord_dec(unsigned long long e) {
+    unsigned long long b = (e >> 63) ? (e & 0x7fffffffffffffffULL) : ~e;
+    return __longlong_as_double((long long)b);
+}
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// warp-aggregated append: returns this lane's slot (called by the lanes that append)
+__device__ __forceinline__ unsigned long long agg_append(unsigned long long *ctr) {
+    unsigned active = __activemask();
+    int leader = __ffs(active) - 1;
+    unsigned rank = __popc(active & ((1u << lane_id()) - 1u));
+    unsigned long long base = 0;
+    if ((int)lane_id() == leader) base = atomicAdd(ctr, (unsigned long long)__popc(active));
+    base = __shfl_sync(active, base, leader);
+    return base + rank;
+}
+
+// octahedral unit-vector encoding, 15 bits per axis + 2-bit wavelength
+// (Meyer et al., "On floating-point normal vectors", EGSR 2010)
+__device__ __forceinline__ uint32_t oct_pack(float x, float y, float z, int wl) {
+    float s = fabsf(x) + fabsf(y) + fabsf(z);
+    float inv = s > 0.0f ? 1.0f / s : 0.0f;
+    float px = x * inv, py = y * inv;
+    if (z < 0.0f) {
+        float ox = (1.0f - fabsf(py)) * (px >= 0.0f ? 1.0f : -1.0f);
+        float oy = (1.0f - fabsf(px)) * (py >= 0.0f ? 1.0f : -1.0f);
+        px = ox; py = oy;
+    }
+    uint32_t qx = (uint32_t)__float2int_rn((px * 0.5f + 0.5f) * 32767.0f);
+    uint32_t qy = (uint32_t)__float2int_rn((py * 0.5f + 0.5f) * 32767.0f);
+    qx = min(qx, 32767u); qy = min(qy, 32767u);
+    return qx | (qy << 15) | ((uint32_t)wl << 30);
+}
+__device__ __forceinline__ V3<float> oct_unpack(uint32_t m) {
+    float px = (float)(m & 32767u) * (2.0f / 32767.0f) - 1.0f;
+    float py = (float)((m >> 15) & 32767u) * (2.0f / 32767.0f) - 1.0f;
+    float pz = 1.0f - fabsf(px) - fabsf(py);
+    if (pz < 0.0f) {
+        float ox = (1.0f - fabsf(py)) * (px >= 0.0f ? 1.0f : -1.0f);
+        float oy = (1.0f - fabsf(px)) * (py >= 0.0f ? 1.0f : -1.0f);
+        px = ox; py = oy;
+    }
+    float inv = rsqrtf(px * px + py * py + pz * pz);
+    return mk3(px * inv, py * inv, pz * inv);
+}
+
+// unsorted photon record of the FP64 path (also the parity download format)
+struct PhotonD {
+    double pos[3];
+    double dir[3];
+    int32_t emit;
+    int8_t level;
+    uint8_t wl;
+    int16_t pad;
+};
+
+template <typename T> struct PhotonBuf;
+template <> struct PhotonBuf<double> {
+    PhotonD *raw;          // unsorted
+    double4 *spos;         // sorted: x, y, z, meta (orig index | wl << 40)
+    double4 *sdir;         // sorted: dx, dy, dz, 0
+    __device__ __forceinline__ void write(unsigned long long i, const PhotonPath<double> &ph, V3<double> p) const {
+        PhotonD r;
+        r.pos[0] = p.x; r.pos[1] = p.y; r.pos[2] = p.z;
+        r.dir[0] = ph.dir.x; r.dir[1] = ph.dir.y; r.dir[2] = ph.dir.z;
+        r.emit = (int32_t)ph.item; r.level = (int8_t)ph.level; r.wl = (uint8_t)ph.wl; r.pad = 0;
+        raw[i] = r;
+    }
+    __device__ __forceinline__ V3<double> raw_pos(unsigned long long i) const { return ld3(raw[i].pos); }
+};
+template <> struct PhotonBuf<float> {
+    float4 *raw;           // unsorted: x, y, z, oct(dir) | wl
+    float4 *sorted;        // sorted copy
+    int32_t *sidx;         // optional: original index per sorted slot
+    __device__ __forceinline__ void write(unsigned long long i, const PhotonPath<float> &ph, V3<float> p) const {
+        raw[i] = make_float4(p.x, p.y, p.z, __uint_as_float(oct_pack(ph.dir.x, ph.dir.y, ph.dir.z, ph.wl)));
+    }
+    __device__ __forceinline__ V3<float> raw_pos(unsigned long long i) const {
+        float4 r = raw[i];
+        return mk3(r.x, r.y, r.z);
+    }
+};
+
+template <typename T>
+struct HitPoint {
+    T pos[3];
+    T nrm[3];
+    T w[3];
+    int32_t pixel;
+};
+
+// ---------------------------------------------------------------------------
+// photon emission + tracing
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_trace_photons(SceneView<T> sc, EmitPlan plan, uint64_t seed, PassState *st,
+                                                       int uc, PhotonBuf<T> out, unsigned long long cap) {
+    const uint32_t pass = (uint32_t)st->pass;
+    const int64_t n_emit = plan.first[plan.n_lights];
+    int64_t next = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    PhotonPath<T> ph;
+    bool alive = false;
+    while (alive || next < n_emit) {
+        if (!alive) {
+            int li = 0;
+            while (li < plan.n_lights - 1 && next >= plan.first[li + 1]) li++;
+            ph.item = (uint32_t)next;
+            Rng rg;
+            rg.init(seed, ph.item, pass, TAG_EMIT);
+            generate_photon(sc.lights[li], rg, ph);
+            next += stride;
+            alive = true;
+        }
+        bool store;
+        V3<T> spos;
+        const int lvl = ph.level;
+        PhotonPath<T> cur = ph;
+        alive = photon_event(sc, seed, pass, uc != 0, ph, store, spos);
+        if (store) {
+            unsigned long long slot = agg_append(&st->n_stored);
+            if (slot < cap) {
+                cur.level = lvl;
+                out.write(slot, cur, spos);
+            } else {
+                atomicOr(&st->overflow, 1u);
+            }
+        }
+    }
+}
+
+// bounds of n photons (block reduction, then one atomic per block and axis)
+template <typename T>
+__global__ void __launch_bounds__(256) k_bbox(PhotonBuf<T> buf, PassState *st, long long n_fixed) {
+    unsigned long long n = n_fixed >= 0 ? (unsigned long long)n_fixed : st->n_stored;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        V3<T> p = buf.raw_pos(i);
+        double v[3] = {(double)p.x, (double)p.y, (double)p.z};
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            if (v[a] == v[a]) { lo[a] = fmin(lo[a], v[a]); hi[a] = fmax(hi[a], v[a]); }
+        }
+    }
+    __shared__ double slo[3][8], shi[3][8];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[a] = fmin(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = fmax(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+        if (lane_id() == 0) { slo[a][threadIdx.x >> 5] = lo[a]; shi[a][threadIdx.x >> 5] = hi[a]; }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        int a = threadIdx.x;
+        double l = slo[a][0], h = shi[a][0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) { l = fmin(l, slo[a][w]); h = fmax(h, shi[a][w]); }
+        if (l <= h) {
+            atomicMin(&st->bb_lo[a], ord_enc(l));
+            atomicMax(&st->bb_hi[a], ord_enc(h));
+        }
+    }
+}
+
+// cell coordinate, clamped to the grid
+template <typename T> struct CellMath;
+template <> struct CellMath<double> {
+    __device__ static __forceinline__ int coord(const GridParams &g, double p, int a) {
+        double f = floor((p - g.org[a]) * g.inv);
+        f = fmin(fmax(f, 0.0), (double)(g.dim[a] - 1));
+        return (int)f;
+    }
+};
+template <> struct CellMath<float> {
+    __device__ static __forceinline__ int coord(const GridParams &g, float p, int a) {
+        float f = floorf((p - g.orgf[a]) * g.invf);
+        f = fminf(fmaxf(f, 0.0f), (float)(g.dim[a] - 1));
+        return (int)f;
+    }
+};
+
+template <typename T>
+__device__ __forceinline__ uint32_t cell_of(const GridParams &g, V3<T> p) {
+    int cx = CellMath<T>::coord(g, p.x, 0), cy = CellMath<T>::coord(g, p.y, 1), cz = CellMath<T>::coord(g, p.z, 2);
+    return (uint32_t)((cz * g.dim[1] + cy) * g.dim[0] + cx);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_cell_hist(PhotonBuf<T> buf, PassState *st, long long n_fixed,
+                                                   uint32_t *count, uint2 *keyrank) {
+    unsigned long long n = n_fixed >= 0 ? (unsigned long long)n_fixed : st->n_stored;
+    const GridParams g = st->grid;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        uint32_t c = cell_of(g, buf.raw_pos(i));
+        uint32_t r = atomicAdd(&count[c], 1u);
+        keyrank[i] = make_uint2(c, r);
+    }
+}
+
+template <typename T> __global__ void k_scatter(PhotonBuf<T> buf, PassState *st, long long n_fixed,
+                                                const uint32_t *start, const uint2 *keyrank);
+
+#if defined(PPM_BUILD_F64)
+template <>
+__global__ void __launch_bounds__(256) k_scatter<double>(PhotonBuf<double> buf, PassState *st, long long n_fixed,
+                                                         const uint32_t *start, const uint2 *keyrank) {
+    unsigned long long n = n_fixed >= 0 ? (unsigned long long)n_fixed : st->n_stored;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        uint2 kr = keyrank[i];
+        uint32_t dst = start[kr.x] + kr.y;
+        const PhotonD r = buf.raw[i];
+        unsigned long long meta = (unsigned long long)i | ((unsigned long long)r.wl << 40);
+        buf.spos[dst] = make_double4(r.pos[0], r.pos[1], r.pos[2], __longlong_as_double((long long)meta));
+        buf.sdir[dst] = make_double4(r.dir[0], r.dir[1], r.dir[2], 0.0);
+    }
+}
+
+#endif
+
+#if defined(PPM_BUILD_F32)
+template <>
+__global__ void __launch_bounds__(256) k_scatter<float>(PhotonBuf<float> buf, PassState *st, long long n_fixed,
+                                                        const uint32_t *start, const uint2 *keyrank) {
+    unsigned long long n = n_fixed >= 0 ? (unsigned long long)n_fixed : st->n_stored;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        uint2 kr = keyrank[i];
+        uint32_t dst = start[kr.x] + kr.y;
+        buf.sorted[dst] = buf.raw[i];
+        if (buf.sidx) buf.sidx[dst] = (int32_t)i;
+    }
+}
+
+#endif
+
+// ---------------------------------------------------------------------------
+// eye pass: camera rays (camera.rs:58-75) and the eye tree (tracer.rs:129-177)
+// ---------------------------------------------------------------------------
+template <typename T>
+struct EyeEntry {
+    V3<T> pos, dir, w;
+    int16_t medium;
+    int16_t level;
+    uint32_t node;
+};
+
+constexpr int EYE_STACK = 12;
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_eye(SceneView<T> sc, DCamera<T> cam, uint64_t seed, PassState *st, int uc,
+                                             HitPoint<T> *hits, unsigned long long hit_cap, double *pass_img) {
+    const uint32_t pass = (uint32_t)st->pass;
+    const int64_t npx = (int64_t)cam.xreso * cam.yreso;
+    const T air[3] = {T(1), T(1), T(1)};
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < npx; p += (int64_t)gridDim.x * blockDim.x) {
+        const T y = (T)(p / cam.xreso), x = (T)(p % cam.xreso);
+        Rng rg;
+        rg.init(seed, (uint32_t)p, pass, TAG_CAMERA);
+        V3<T> blur = mk3(T(0), T(0), T(0));
+        if (cam.blur) {
+            T r1 = gen_range<T>(rg, T(-0.5), T(0.5));
+            T r2 = gen_range<T>(rg, T(-0.5), T(0.5));
+            blur = r1 * ld3(cam.eex) + r2 * ld3(cam.eey);
+        }
+        T r3 = T(0), r4 = T(0);
+        if (cam.jitter_aa) {
+            r3 = gen_range<T>(rg, T(-0.5), T(0.5));
+            r4 = gen_range<T>(rg, T(-0.5), T(0.5));
+        }
+        EyeEntry<T> stack[EYE_STACK];
+        int sp = 0;
+        stack[0].pos = ld3(cam.eye) + blur;
+        V3<T> ed = ((ld3(cam.origin) + (x + r3) * ld3(cam.esx)) + (y + r4) * ld3(cam.esy)) - blur;
+        stack[0].dir = ed;
+        normalize(ed, stack[0].dir);
+        stack[0].w = mk3(T(1), T(1), T(1));
+        stack[0].medium = -1;
+        stack[0].level = 0;
+        stack[0].node = 1u;
+        sp = 1;
+        V3<T> acc = mk3(T(0), T(0), T(0));
+        while (sp > 0) {
+            EyeEntry<T> e = stack[--sp];
+            Isect<T> is;
+            if (!intersect(sc, e.pos, e.dir, is)) continue;
+            const int mid = sc.objs[is.obj].mat;
+            const DMaterial<T> &mate = sc.mats[mid];
+            acc = acc + hmul(e.w, ld3(mate.emit)) * Cst<T>::sr_half();
+            Coef<T> cf;
+            V3<T> rdir = is.n, td = is.n;
+            T cos1;
+            bool has_t = false, diffuse_only = mate.surface == SF_SIMPLE && mate.scatter == T(1);
+            if (diffuse_only) {
+                // Simple surface with diffuseness 1: no reflected child, the
+                // refracted child has weight 0 and c_di does not depend on cos
+                cf = bsdf_coef(mate, T(0));
+                cos1 = T(0);
+            } else {
+                T cos2;
+                V3<T> rdir0 = specular_reflection(is.n, e.dir, cos1);
+                Rng rv;
+                rv.init(seed, (uint32_t)p, pass, TAG_EYE | e.node);
+                rdir = reflection_glossy(rv, is.n, rdir0, sf_power_glossy(mate));
+                T eta = relative_ior_average(ior_of(sc, e.medium, air), mate.ior);
+                V3<T> hvec = is.n;
+                if (!normalize(rdir - e.dir, hvec)) hvec = is.n;
+                has_t = specular_refraction(hvec, e.dir, eta, td, cos2);
+                T cos = cos1 < cos2 ? cos1 : cos2;
+                cf = bsdf_coef(mate, cos);
+            }
+            V3<T> W = hmul(e.w, cf.di);
+            if (any_nz(W)) {
+                if (uc) {
+                    V3<T> di = mk3(T(0), T(0), T(0));
+                    for (int l = 0; l < sc.n_lights; l++) di = di + radiance_from_light(sc, is.pos, is.n, sc.lights[l]);
+                    acc = acc + hmul(W, di);
+                }
+                unsigned long long slot = agg_append(&st->n_hits);
+                if (slot < hit_cap) {
+                    HitPoint<T> h;
+                    h.pos[0] = is.pos.x; h.pos[1] = is.pos.y; h.pos[2] = is.pos.z;
+                    h.nrm[0] = is.n.x; h.nrm[1] = is.n.y; h.nrm[2] = is.n.z;
+                    h.w[0] = W.x; h.w[1] = W.y; h.w[2] = W.z;
+                    h.pixel = (int32_t)p;
+                    hits[slot] = h;
+                } else {
+                    atomicOr(&st->overflow, 2u);
+                }
+            }
+            if (diffuse_only || e.level + 1 >= MAX_TRACE) continue;
+            V3<T> wt = hmul(e.w, cf.ti);
+            if (has_t && sf_refract(mate, cos1) && any_nz(wt)) {
+                if (sp < EYE_STACK) {
+                    EyeEntry<T> c;
+                    c.pos = is.pos; c.dir = td; c.w = wt;
+                    c.medium = (int16_t)(is.in ? mid : -1);
+                    c.level = (int16_t)(e.level + 1); c.node = 2u * e.node + 1u;
+                    stack[sp++] = c;
+                } else {
+                    atomicOr(&st->overflow, 4u);
+                }
+            }
+            V3<T> ws = hmul(e.w, cf.si);
+            if (sf_reflect(mate, cos1) && any_nz(ws)) {
+                if (sp < EYE_STACK) {
+                    EyeEntry<T> c;
+                    c.pos = is.pos; c.dir = rdir; c.w = ws;
+                    c.medium = e.medium;
+                    c.level = (int16_t)(e.level + 1); c.node = 2u * e.node;
+                    stack[sp++] = c;
+                } else {
+                    atomicOr(&st->overflow, 4u);
+                }
+            }
+        }
+        pass_img[3 * p] = (double)acc.x;
+        pass_img[3 * p + 1] = (double)acc.y;
+        pass_img[3 * p + 2] = (double)acc.z;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// candidate enumeration: the (2e+1)^2 x-rows of cells around a query are
+// concatenated; lanes stride over the concatenation.  Rows are processed in
+// chunks of 32 (one row per lane), a lane finds its row by binary search
+// over the rows' inclusive prefix sums held across the warp.
+// ---------------------------------------------------------------------------
+struct RowChunk {
+    uint32_t begin;   // this lane's row begin (photon index)
+    uint32_t incl;    // inclusive prefix of row lengths (this lane's row)
+    uint32_t total;
+};
+
+template <typename T>
+__device__ __forceinline__ void query_cells(const GridParams &g, V3<T> q, int ext, int c[3], int lo[3], int hi[3]) {
+    c[0] = CellMath<T>::coord(g, q.x, 0);
+    c[1] = CellMath<T>::coord(g, q.y, 1);
+    c[2] = CellMath<T>::coord(g, q.z, 2);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        lo[a] = max(c[a] - ext, 0);
+        hi[a] = min(c[a] + ext, g.dim[a] - 1);
+    }
+}
+
+__device__ __forceinline__ RowChunk make_chunk(const GridParams &g, const uint32_t *start, const int lo[3], const int hi[3],
+                                               int row0) {
+    const int ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+    const int nrows = ny * nz;
+    int row = row0 + (int)lane_id();
+    uint32_t b = 0, len = 0;
+    if (row < nrows) {
+        int yy = lo[1] + row % ny, zz = lo[2] + row / ny;
+        int base = (zz * g.dim[1] + yy) * g.dim[0];
+        b = start[base + lo[0]];
+        len = start[base + hi[0] + 1] - b;
+    }
+    uint32_t incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int)lane_id() >= o) incl += v;
+    }
+    RowChunk rc;
+    rc.begin = b;
+    rc.incl = incl;
+    rc.total = __shfl_sync(0xffffffffu, incl, 31);
+    return rc;
+}
+
+// photon index of virtual position v (< rc.total) of the chunk.  All lanes
+// must call this (it shuffles with the full mask).
+__device__ __forceinline__ uint32_t chunk_index(const RowChunk &rc, uint32_t v) {
+    int lo = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+        uint32_t val = __shfl_sync(0xffffffffu, rc.incl, lo + step - 1);
+        if (val <= v) lo += step;
+    }
+    uint32_t b = __shfl_sync(0xffffffffu, rc.begin, lo);
+    uint32_t prev = __shfl_sync(0xffffffffu, rc.incl, (lo + 31) & 31);
+    if (lo == 0) prev = 0u;
+    return b + (v - prev);
+}
+
+__device__ __forceinline__ double filter_wt(int pfilter, double d, double r2) {
+    if (pfilter == PF_CONE) {   // tracer.rs:201-204
+        double d2 = sqrt(d / r2) / 1.1;
+        return d2 > 1.0 ? 0.0 : (1.0 - d2) / (1.0 - 2.0 / (3.0 * 1.1));
+    }
+    if (pfilter == PF_GAUSS) {  // tracer.rs:213-216
+        double e_r = 1.0 - pm_exp(-1.953 * d / (r2 * 2.0));
+        double eb = 1.0 - 0.14184788965323;
+        return e_r > eb ? 0.0 : 0.918 * (1.0 - e_r / eb) + 0.5;
+    }
+    return 1.0;
+}
+
+// squared_euclidean(query, point) as the kdtree crate sums it
+__device__ __forceinline__ double sq_euclid(double qx, double qy, double qz, double px, double py, double pz) {
+    double dx = qx - px, dy = qy - py, dz = qz - pz;
+    double s = 0.0;
+    s = __dadd_rn(s, __dmul_rn(dx, dx));
+    s = __dadd_rn(s, __dmul_rn(dy, dy));
+    s = __dadd_rn(s, __dmul_rn(dz, dz));
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 gather over the sorted double map.  mode 0: render (atomicAdd
+// W * estimate into pass_img); mode 1: per-query estimate into out_rgb.
+// ---------------------------------------------------------------------------
+struct GatherOutD {
+    double *pass_img;
+    double *out_rgb;
+    unsigned long long *count;  // optional candidate / in-radius counters
+};
+
+#if defined(PPM_BUILD_F64)
+__global__ void __launch_bounds__(256) k_gather_d(const HitPoint<double> *hits, PassState *st, long long n_fixed,
+                                                  const double4 *spos, const double4 *sdir, const uint32_t *start,
+                                                  double pw, int pfilter, int mode, GatherOutD out) {
+    const unsigned long long nq = n_fixed >= 0 ? (unsigned long long)n_fixed : st->n_hits;
+    const GridParams g = st->grid;
+    const double r2 = st->r2;
+    const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    for (unsigned long long qi = warp; qi < nq; qi += nwarps) {
+        const HitPoint<double> h = hits[qi];
+        V3<double> q = ld3(h.pos), n = ld3(h.nrm);
+        int c[3], lo[3], hi[3];
+        query_cells(g, q, g.ext, c, lo, hi);
+        const int nrows = (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+        for (int row0 = 0; row0 < nrows; row0 += 32) {
+            RowChunk rc = make_chunk(g, start, lo, hi, row0);
+            for (uint32_t base = 0; base < rc.total; base += 32) {
+                uint32_t v = base + lane_id();
+                uint32_t idx = chunk_index(rc, min(v, rc.total - 1));
+                if (v < rc.total) {
+                    double4 pp = spos[idx];
+                    double d = sq_euclid(q.x, q.y, q.z, pp.x, pp.y, pp.z);
+                    if (d <= r2) {
+                        double4 pd = sdir[idx];
+                        double wt = filter_wt(pfilter, d, r2);
+                        double pwt = wt * pw;
+                        double cos0 = dot(n, mk3(pd.x, pd.y, pd.z));
+                        double pw2 = cos0 < 0.0 ? pwt * -cos0 : 0.0;
+                        int wl = (int)(((unsigned long long)__double_as_longlong(pp.w)) >> 40);
+                        if (wl == 0) s0 += pw2; else if (wl == 1) s1 += pw2; else s2 += pw2;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+            s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        }
+        if (lane_id() == 0) {
+            double k = ONE_PI_D / r2;
+            if (mode == 0) {
+                double *px = out.pass_img + 3 * (long long)h.pixel;
+                atomicAdd(px, h.w[0] * (s0 * k));
+                atomicAdd(px + 1, h.w[1] * (s1 * k));
+                atomicAdd(px + 2, h.w[2] * (s2 * k));
+            } else {
+                out.out_rgb[3 * qi] = s0 * k;
+                out.out_rgb[3 * qi + 1] = s1 * k;
+                out.out_rgb[3 * qi + 2] = s2 * k;
+            }
+        }
+    }
+}
+
+#endif  // PPM_BUILD_F64
+
+// ---------------------------------------------------------------------------
+// FP32 gather over the sorted float4 map with Kahan-compensated per-lane
+// flux sums.  Membership: FP32 distance test; candidates inside the rounding
+// band [r2_lo, r2_hi] are re-decided by the FP64 predicate on the same
+// (f32-valued) coordinates, so the in-radius set equals the f64 one.
+// ---------------------------------------------------------------------------
+struct Kahan {
+    float s, c;
+    __device__ __forceinline__ void add(float v) {
+        float y = v - c;
+        float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+
+// compensated pairwise combination (two-sum) across the warp
+__device__ __forceinline__ float warp_sum_comp(Kahan k) {
+    float s = k.s, c = -k.c;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        float so = __shfl_xor_sync(0xffffffffu, s, o);
+        float co = __shfl_xor_sync(0xffffffffu, c, o);
+        float t = s + so;
+        float bp = t - s;
+        float err = (s - (t - bp)) + (so - bp);
+        s = t;
+        c = c + co + err;
+    }
+    return s + c;
+}
+
+__device__ __forceinline__ bool in_radius_f32(float qx, float qy, float qz, float4 pp, float r2_lo, float r2_hi,
+                                              double r2, float &d2f) {
+    float dx = qx - pp.x, dy = qy - pp.y, dz = qz - pp.z;
+    d2f = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+    if (d2f < r2_lo) return true;
+    if (d2f > r2_hi) return false;
+    return sq_euclid((double)qx, (double)qy, (double)qz, (double)pp.x, (double)pp.y, (double)pp.z) <= r2;
+}
+
+__device__ __forceinline__ float filter_wt_f(int pfilter, float d, float r2) {
+    if (pfilter == PF_CONE) {
+        float d2 = sqrtf(d / r2) * (1.0f / 1.1f);
+        return d2 > 1.0f ? 0.0f : (1.0f - d2) * (float)(1.0 / (1.0 - 2.0 / (3.0 * 1.1)));
+    }
+    if (pfilter == PF_GAUSS) {
+        float e_r = 1.0f - __expf(-1.953f * d / (r2 * 2.0f));
+        const float eb = (float)(1.0 - 0.14184788965323);
+        return e_r > eb ? 0.0f : 0.918f * (1.0f - e_r / eb) + 0.5f;
+    }
+    return 1.0f;
+}
+
+struct GatherOutF {
+    double *pass_img;
+    double *out_rgb;
+    unsigned long long *count;
+};
+
+#if defined(PPM_BUILD_F32)
+__global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed,
+                                                  const float4 *smap, const uint32_t *start, double pw,
+                                                  const double *q_r2, int pfilter, int mode, GatherOutF out) {
+    const unsigned long long nq = n_fixed >= 0 ? (unsigned long long)n_fixed : st->n_hits;
+    const GridParams g = st->grid;
+    const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    for (unsigned long long qi = warp; qi < nq; qi += nwarps) {
+        const HitPoint<float> h = hits[qi];
+        const double r2 = q_r2 ? q_r2[qi] : st->r2;
+        const float r2_lo = __double2float_rd(r2 * (1.0 - 1e-6));
+        const float r2_hi = __double2float_ru(r2 * (1.0 + 1e-6));
+        int ext = g.ext;
+        if (q_r2) ext = min(g.ext, max(1, (int)ceil(sqrt(r2) * g.inv + 3e-3)));
+        V3<float> q = ld3(h.pos), n = ld3(h.nrm);
+        int c[3], lo[3], hi[3];
+        query_cells(g, q, ext, c, lo, hi);
+        const int nrows = (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+        Kahan k0 = {0.f, 0.f}, k1 = {0.f, 0.f}, k2 = {0.f, 0.f};
+        for (int row0 = 0; row0 < nrows; row0 += 32) {
+            RowChunk rc = make_chunk(g, start, lo, hi, row0);
+            for (uint32_t base = 0; base < rc.total; base += 32) {
+                uint32_t v = base + lane_id();
+                uint32_t idx = chunk_index(rc, min(v, rc.total - 1));
+                if (v < rc.total) {
+                    float4 pp = smap[idx];
+                    float d2f;
+                    if (in_radius_f32(q.x, q.y, q.z, pp, r2_lo, r2_hi, r2, d2f)) {
+                        uint32_t m = __float_as_uint(pp.w);
+                        V3<float> pd = oct_unpack(m);
+                        float cos0 = dot(n, pd);
+                        float val = cos0 < 0.0f ? -cos0 : 0.0f;
+                        if (pfilter != PF_NONE) val *= filter_wt_f(pfilter, d2f, (float)r2);
+                        int wl = (int)(m >> 30);
+                        k0.add(wl == 0 ? val : 0.0f);
+                        k1.add(wl == 1 ? val : 0.0f);
+                        k2.add(wl == 2 ? val : 0.0f);
+                    }
+                }
+            }
+        }
+        float s0 = warp_sum_comp(k0), s1 = warp_sum_comp(k1), s2 = warp_sum_comp(k2);
+        if (lane_id() == 0) {
+            double kk = pw * (ONE_PI_D / r2);
+            if (mode == 0) {
+                double *px = out.pass_img + 3 * (long long)h.pixel;
+                atomicAdd(px, (double)h.w[0] * ((double)s0 * kk));
+                atomicAdd(px + 1, (double)h.w[1] * ((double)s1 * kk));
+                atomicAdd(px + 2, (double)h.w[2] * ((double)s2 * kk));
+            } else {
+                out.out_rgb[3 * qi] = (double)s0 * kk;
+                out.out_rgb[3 * qi + 1] = (double)s1 * kk;
+                out.out_rgb[3 * qi + 2] = (double)s2 * kk;
+            }
+        }
+    }
+}
+
+#endif  // PPM_BUILD_F32
+
+// ---------------------------------------------------------------------------
+// in-radius sets (parity entry points): count pass, then fill pass
+// ---------------------------------------------------------------------------
+template <typename T, typename MapT>
+__global__ void __launch_bounds__(256) k_within(const T *q, long long nq, const double *q_r2, const PassState *st,
+                                                const MapT *smap, const uint32_t *start, const int32_t *sidx,
+                                                unsigned long long *counts, const unsigned long long *offsets,
+                                                int32_t *idx_out) {
+    const GridParams g = st->grid;
+    const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    for (unsigned long long qi = warp; qi < (unsigned long long)nq; qi += nwarps) {
+        V3<T> qq = ld3(q + 3 * qi);
+        const double r2 = q_r2[qi];
+        const float r2_lo = __double2float_rd(r2 * (1.0 - 1e-6));
+        const float r2_hi = __double2float_ru(r2 * (1.0 + 1e-6));
+        int ext = min(g.ext, max(1, (int)ceil(sqrt(r2) * g.inv + 3e-3)));
+        int c[3], lo[3], hi[3];
+        query_cells(g, qq, ext, c, lo, hi);
+        const int nrows = (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+        unsigned long long found = 0;
+        unsigned long long wbase = offsets ? offsets[qi] : 0;
+        for (int row0 = 0; row0 < nrows; row0 += 32) {
+            RowChunk rc = make_chunk(g, start, lo, hi, row0);
+            for (uint32_t base = 0; base < rc.total; base += 32) {
+                uint32_t v = base + lane_id();
+                uint32_t idx = chunk_index(rc, min(v, rc.total - 1));
+                bool hit = false;
+                int32_t orig = 0;
+                if (v < rc.total) {
+                    if constexpr (sizeof(T) == 8) {
+                        double4 pp = smap[idx];
+                        hit = sq_euclid(qq.x, qq.y, qq.z, pp.x, pp.y, pp.z) <= r2;
+                        orig = (int32_t)(((unsigned long long)__double_as_longlong(pp.w)) & 0xffffffffffULL);
+                    } else {
+                        float d2f;
+                        hit = in_radius_f32(qq.x, qq.y, qq.z, smap[idx], r2_lo, r2_hi, r2, d2f);
+                        orig = sidx[idx];
+                    }
+                }
+                unsigned m = __ballot_sync(0xffffffffu, hit);
+                if (idx_out && hit) idx_out[wbase + found + __popc(m & ((1u << lane_id()) - 1u))] = orig;
+                found += __popc(m);
+            }
+        }
+        if (lane_id() == 0 && counts) counts[qi] = found;
+    }
+}
+
+// queries from host arrays for the estimate entry points
+template <typename T>
+__global__ void k_make_queries(const T *pos, const T *nrm, long long n, HitPoint<T> *hits) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    HitPoint<T> h;
+    for (int a = 0; a < 3; a++) { h.pos[a] = pos[3 * i + a]; h.nrm[a] = nrm[3 * i + a]; h.w[a] = T(1); }
+    h.pixel = (int32_t)i;
+    hits[i] = h;
+}
+
+// first-hit parity kernel: calc_intersection for a batch of rays
+template <typename T>
+__global__ void k_intersect(SceneView<T> sc, const double *rays, long long n, double *t, int32_t *obj, double *nrm) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double *r = rays + 6 * i;
+    V3<T> rp = mk3((T)r[0], (T)r[1], (T)r[2]), rd = mk3((T)r[3], (T)r[4], (T)r[5]);
+    Isect<T> is;
+    if (intersect(sc, rp, rd, is)) {
+        t[i] = (double)is.t; obj[i] = is.obj;
+        if (nrm) { nrm[3 * i] = (double)is.n.x; nrm[3 * i + 1] = (double)is.n.y; nrm[3 * i + 2] = (double)is.n.z; }
+    } else {
+        t[i] = 0.0; obj[i] = -1;
+        if (nrm) { nrm[3 * i] = 0.0; nrm[3 * i + 1] = 0.0; nrm[3 * i + 2] = 0.0; }
+    }
+}
+
+}  // namespace ppm

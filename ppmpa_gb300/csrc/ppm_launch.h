@@ -1,0 +1,62 @@
+// ppm_launch.h -- host-side launch wrappers shared between the translation
+// units (k_f64.cu: FP64 path, compiled without FMA contraction; k_f32.cu:
+// FP32 mixed path; k_grid.cu: integer grid / scan / pass bookkeeping).
+#pragma once
+#include <cuda_runtime.h>
+#include "ppm_kernels.cuh"
+
+namespace ppm {
+
+// ---- FP64 path -------------------------------------------------------------
+void launch_trace_d(const SceneView<double> &sc, const EmitPlan &plan, uint64_t seed, PassState *st, int uc,
+                    PhotonBuf<double> out, unsigned long long cap, int grid, cudaStream_t s);
+void launch_bbox_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s);
+void launch_hist_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, uint32_t *count, uint2 *keyrank, int grid,
+                   cudaStream_t s);
+void launch_scatter_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, const uint32_t *start,
+                      const uint2 *keyrank, int grid, cudaStream_t s);
+void launch_eye_d(const SceneView<double> &sc, const DCamera<double> &cam, uint64_t seed, PassState *st, int uc,
+                  HitPoint<double> *hits, unsigned long long hit_cap, double *pass_img, int grid, cudaStream_t s);
+void launch_gather_d(const HitPoint<double> *hits, PassState *st, long long n_fixed, const double4 *spos,
+                     const double4 *sdir, const uint32_t *start, double pw, int pfilter, int mode, GatherOutD out,
+                     int grid, cudaStream_t s);
+void launch_within_d(const double *q, long long nq, const double *q_r2, const PassState *st, const double4 *smap,
+                     const uint32_t *start, unsigned long long *counts, const unsigned long long *offsets,
+                     int32_t *idx_out, int grid, cudaStream_t s);
+void launch_make_queries_d(const double *pos, const double *nrm, long long n, HitPoint<double> *hits, cudaStream_t s);
+void launch_intersect_d(const SceneView<double> &sc, const double *rays, long long n, double *t, int32_t *obj,
+                        double *nrm, cudaStream_t s);
+
+// ---- FP32 mixed path ---------------------------------------------------------
+void launch_trace_f(const SceneView<float> &sc, const EmitPlan &plan, uint64_t seed, PassState *st, int uc,
+                    PhotonBuf<float> out, unsigned long long cap, int grid, cudaStream_t s);
+void launch_bbox_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s);
+void launch_hist_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, uint32_t *count, uint2 *keyrank, int grid,
+                   cudaStream_t s);
+void launch_scatter_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, const uint32_t *start,
+                      const uint2 *keyrank, int grid, cudaStream_t s);
+void launch_eye_f(const SceneView<float> &sc, const DCamera<float> &cam, uint64_t seed, PassState *st, int uc,
+                  HitPoint<float> *hits, unsigned long long hit_cap, double *pass_img, int grid, cudaStream_t s);
+void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
+                     const uint32_t *start, double pw, const double *q_r2, int pfilter, int mode, GatherOutF out,
+                     int grid, cudaStream_t s);
+void launch_within_f(const float *q, long long nq, const double *q_r2, const PassState *st, const float4 *smap,
+                     const uint32_t *start, const int32_t *sidx, unsigned long long *counts,
+                     const unsigned long long *offsets, int32_t *idx_out, int grid, cudaStream_t s);
+void launch_make_queries_f(const float *pos, const float *nrm, long long n, HitPoint<float> *hits, cudaStream_t s);
+void launch_intersect_f(const SceneView<float> &sc, const double *rays, long long n, double *t, int32_t *obj,
+                        cudaStream_t s);
+void launch_pack_photons_f(const float *pos, const float *dir, const uint8_t *wl, long long n, float4 *raw,
+                           cudaStream_t s);
+
+// ---- grid / scan / pass bookkeeping ------------------------------------------------
+constexpr int SCAN_TILE = 4096;
+void launch_pass_begin(PassState *st, cudaStream_t s);
+void launch_grid_setup(PassState *st, double r2_override, cudaStream_t s);
+void launch_scan(uint32_t *count, const PassState *st, uint32_t *block_sums, uint32_t *start, long long cell_cap,
+                 cudaStream_t s);
+void launch_accum(const double *pass_img, double *sum, long long n, cudaStream_t s);
+void launch_pass_end(PassState *st, cudaStream_t s);
+int kernels_per_scan();
+
+}  // namespace ppm

@@ -1,0 +1,101 @@
+"""CPU checks of the C ABI library and the host-side logic (no GPU needed):
+the library loads and exports every entry point include/ppm_api.h declares;
+the host derivations (camera, material) agree bit for bit between the
+Python builders, the library and the oracle; error paths return statuses."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from oracle import binding as B
+from ppmpa_gb300 import _lib, scene as S
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "ppm_api.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"\b(ppm_[a-z0-9_]+)\s*\(", text)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    lib = C.CDLL(built_lib)
+    names = declared_functions()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # the Python binding types every declared entry point
+    assert set(names) == set(_lib.SIGNATURES), set(names) ^ set(_lib.SIGNATURES)
+
+
+def test_struct_layouts_match_oracle_and_abi():
+    L = B.lib()
+    assert C.sizeof(S.Object) == L.orc_sizeof(0) == 120
+    assert C.sizeof(S.Material) == L.orc_sizeof(1) == 168
+    assert C.sizeof(S.Light) == L.orc_sizeof(2) == 160
+    assert C.sizeof(S.Camera) == L.orc_sizeof(3) == 336
+
+
+def _camera_fields(c):
+    return [tuple(getattr(c, f)) for f in ("eye_dir", "origin", "esx", "esy", "eex", "eey")] + [c.photon_power]
+
+
+@pytest.mark.parametrize("mk", [S.reference_camera, lambda: S.box_camera(512), lambda: S.make_camera(
+    320, 200, blur=True, eye_position=(0.3, 1.7, -3.1), target_position=(0.1, 0.9, 2.0), focus=5.5, f_number=2.8)])
+def test_camera_derivation_agrees(built_lib, mk):
+    lib = _lib.load(built_lib)
+    py = mk()
+    via_lib = S.Camera.from_buffer_copy(py)
+    lib.ppm_camera_derive(C.byref(via_lib))
+    via_orc = S.Camera.from_buffer_copy(py)
+    B.lib().orc_camera_derive(C.byref(via_orc))
+    assert _camera_fields(py) == _camera_fields(via_lib) == _camera_fields(via_orc)
+
+
+def test_material_derivation_agrees(built_lib):
+    lib = _lib.load(built_lib)
+    sc = S.reference_scene()
+    mats, n = sc.c_materials()
+    for i in range(n):
+        a = S.Material.from_buffer_copy(mats[i])
+        b = S.Material.from_buffer_copy(mats[i])
+        lib.ppm_material_derive(C.byref(a))
+        B.lib().orc_material_derive(C.byref(b))
+        assert a.density_pow == b.density_pow == mats[i].density_pow
+        assert a.alpha == b.alpha == mats[i].alpha
+    # Surface::new_simple with roughness 0: 1 / (10^5 + 1)
+    assert S.new_simple((1, 1, 1), (0, 0, 0), 1, 0, 0).density_pow == 1.0 / (10.0 ** 5.0 + 1.0)
+
+
+def test_reference_scene_shape():
+    sc = S.reference_scene()
+    assert len(sc.objects) == 17 and len(sc.materials) == 14 and len(sc.lights) == 1
+    assert sc.lights[0].color == (1.0 / 3.0,) * 3
+    box = S.box_scene("c2")
+    assert len(box.objects) == 7 and box.materials[-1].surface == S.SURF_TS
+
+
+def test_status_strings_and_no_device_path(built_lib):
+    lib = _lib.load(built_lib)
+    assert lib.ppm_version() == 1
+    assert lib.ppm_status_string(0) == b"ok"
+    assert lib.ppm_status_string(3) == b"capacity exceeded"
+    assert lib.ppm_ctx_destroy(None) == 0
+    # invalid arguments are rejected before any device work
+    assert lib.ppm_ctx_create(None, 0, 1) == 1
+    assert lib.ppm_scene_upload(None, None, 0, None, 0, None, 0) == 1
+    assert lib.ppm_render_step(None, 1) == 1
+
+
+def test_ctx_create_without_gpu_reports_no_device(built_lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = _lib.load(built_lib)
+    h = C.c_void_p()
+    st = lib.ppm_ctx_create(C.byref(h), 0, 1)
+    assert st == 7 and not h.value
+    assert lib.ppm_last_error(None).startswith(b"no CUDA device")
