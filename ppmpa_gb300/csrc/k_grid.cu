@@ -34,21 +34,25 @@ __global__ void k_grid_setup(PassState *st, double r2_override) {
         hi[a] = ord_dec(st->bb_hi[a]);
         if (!(lo[a] <= hi[a])) empty = true;
     }
+    for (int a = 0; a < 3; a++)
+        if (!(hi[a] - lo[a] >= 0.0 && hi[a] - lo[a] < 1e30)) empty = true;
     if (empty) for (int a = 0; a < 3; a++) { lo[a] = 0.0; hi[a] = 0.0; }
     double k = st->cell_factor > 0.0 ? st->cell_factor : 1.0;
     double c = r / k * (1.0 + 1.0 / 128.0);
-    if (!(c > 0.0)) c = 1.0;
+    if (!(c > 0.0 && c < 1e30)) c = 1.0;
     long long dim[3] = {1, 1, 1};
     for (int it = 0; it < 400; it++) {
         bool ok = true;
         long long tot = 1;
         for (int a = 0; a < 3; a++) {
-            dim[a] = (long long)floor((hi[a] - lo[a]) / c) + 1;
-            if (dim[a] > 8192) ok = false;
+            double f = floor((hi[a] - lo[a]) / c);
+            if (!(f >= 0.0 && f < 8192.0)) { ok = false; dim[a] = 8193; }
+            else dim[a] = (long long)f + 1;
             tot *= dim[a];
         }
         if (ok && tot <= st->cell_cap) break;
         c *= 1.25;
+        if (it == 399) { dim[0] = dim[1] = dim[2] = 1; c = 1e30; }
     }
     GridParams g;
     for (int a = 0; a < 3; a++) {
@@ -59,7 +63,8 @@ __global__ void k_grid_setup(PassState *st, double r2_override) {
     g.cell = c;
     g.inv = 1.0 / c;
     g.invf = (float)(1.0 / c);
-    int ext = (int)ceil(r / c + 3e-3);
+    double ef = ceil(r / c + 3e-3);
+    int ext = ef >= 1.0 && ef <= 8.0 ? (int)ef : (ef > 8.0 ? 8 : 1);
     g.ext = ext < 1 ? 1 : (ext > 8 ? 8 : ext);
     g.ncell = dim[0] * dim[1] * dim[2];
     st->grid = g;

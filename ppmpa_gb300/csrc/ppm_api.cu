@@ -292,9 +292,12 @@ static double make_plan(const std::vector<ppm_light> &lights, long long nphoton,
     return pw;
 }
 
-static int upload_state(ppm_ctx *ctx, double r2, int pass, double alpha, int offset, double cell_factor) {
+static int upload_state(ppm_ctx *ctx, double r2, int pass, double alpha, int offset, double cell_factor,
+                        long long photon_cap, long long hit_cap) {
     PassState h;
     std::memset(&h, 0, sizeof h);
+    h.photon_cap = (unsigned long long)photon_cap;
+    h.hit_cap = (unsigned long long)hit_cap;
     h.r2 = r2;
     h.alpha = alpha;
     h.pass = pass;
@@ -547,7 +550,7 @@ extern "C" int ppm_trace_photons(ppm_ctx *ctx, int64_t nphoton, int32_t use_clas
     if (nem > 0x7fffffffLL) return set_err(ctx, PPM_ERR_INVALID_ARG, "too many photons");
     long long cap = std::max(1LL, nem * MAX_TRACE);
     TRY(ensure_photons_d(ctx, cap));
-    TRY(upload_state(ctx, 0.0, (int)pass, 0.0, 1, 1.0));
+    TRY(upload_state(ctx, 0.0, (int)pass, 0.0, 1, 1.0, cap, 0));
     PhotonBuf<double> pb{as<PhotonD>(ctx->raw_d), as<double4>(ctx->spos), as<double4>(ctx->sdir)};
     launch_trace_d(ctx->sv_d, plan, ctx->seed, ctx->st, use_classic ? 1 : 0, pb, (unsigned long long)cap,
                    grid_blocks(ctx, 8), ctx->s);
@@ -590,7 +593,7 @@ extern "C" int ppm_photons_download(ppm_ctx *ctx, double *pos, double *dir, uint
 // build the sorted FP64 map from raw_d[0, n)
 static int build_map_d(ppm_ctx *ctx, long long n, double r2, double pw) {
     PhotonBuf<double> pb{as<PhotonD>(ctx->raw_d), as<double4>(ctx->spos), as<double4>(ctx->sdir)};
-    TRY(upload_state(ctx, r2, 0, 0.0, 1, 1.0));
+    TRY(upload_state(ctx, r2, 0, 0.0, 1, 1.0, n, 0));
     launch_pass_begin(ctx->st, ctx->s);
     int g = grid_blocks(ctx, 4);
     launch_bbox_d(pb, ctx->st, n, g, ctx->s);
@@ -664,7 +667,8 @@ static int within_flow(ppm_ctx *ctx, int64_t nq, int64_t *offsets, int32_t *idx,
     if (!idx) return PPM_OK;
     if ((int64_t)run > cap) return set_err(ctx, PPM_ERR_CAPACITY, "idx needs %llu entries, cap %lld", run, (long long)cap);
     DevBuf out;
-    size_t ob = sizeof(int32_t) * (run ? run : 1), fb = sizeof(unsigned long long) * (nq + 1);
+    // index section rounded up to 16 bytes so the u64 offsets after it stay aligned
+    size_t ob = (sizeof(int32_t) * (run ? run : 1) + 15) & ~(size_t)15, fb = sizeof(unsigned long long) * (nq + 1);
     if (cudaMalloc(&out.p, ob + fb) != cudaSuccess) return set_err(ctx, PPM_ERR_OOM, "no memory for %llu indices", run);
     int32_t *d_idx = (int32_t *)out.p;
     unsigned long long *d_off = (unsigned long long *)((char *)out.p + ob);
@@ -751,7 +755,7 @@ extern "C" int ppm_photonmap_build_f32(ppm_ctx *ctx, const float *pos, const flo
     }
     launch_pack_photons_f(d_pos, d_dir, d_wl, n, as<float4>(ctx->raw_f), ctx->s);
     PhotonBuf<float> pb{as<float4>(ctx->raw_f), as<float4>(ctx->sorted_f), as<int32_t>(ctx->sidx)};
-    TRY(upload_state(ctx, radius2_max, 0, 0.0, 1, 2.0));
+    TRY(upload_state(ctx, radius2_max, 0, 0.0, 1, 2.0, n, 0));
     launch_pass_begin(ctx->st, ctx->s);
     int g = grid_blocks(ctx, 4);
     launch_bbox_f(pb, ctx->st, n, g, ctx->s);
@@ -970,7 +974,8 @@ extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
     CK(cudaMemsetAsync(ctx->sum_img.p, 0, sizeof(double) * 3 * ctx->npx, ctx->s));
     CK(cudaMemsetAsync(ctx->pass_img.p, 0, sizeof(double) * 3 * ctx->npx, ctx->s));
     int cf = cfg->cell_factor ? cfg->cell_factor : 1;
-    TRY(upload_state(ctx, schedule_r2(*cfg, cfg->first_pass), cfg->first_pass, cfg->alpha, cfg->schedule_offset, (double)cf));
+    TRY(upload_state(ctx, schedule_r2(*cfg, cfg->first_pass), cfg->first_pass, cfg->alpha, cfg->schedule_offset, (double)cf,
+                     cap, ctx->hit_cap));
     CK(cudaStreamSynchronize(ctx->s));
     ctx->passes_done = 0;
     ctx->map_kind = 0;

@@ -44,7 +44,24 @@ struct PassState {
     unsigned long long candidates, in_radius;
     double cell_factor;
     int64_t cell_cap;
+    unsigned long long photon_cap;   // buffers hold at most this many photons
+    unsigned long long hit_cap;      // and this many hit points
 };
+
+// number of valid photons / hit points (the counters keep counting past the
+// capacity on overflow; readers never go beyond the buffers)
+// (a host-supplied count n_fixed >= 0 describes a buffer the host sized; only
+// device-counted values are clamped)
+__device__ __forceinline__ unsigned long long n_photons(const PassState *st, long long n_fixed) {
+    if (n_fixed >= 0) return (unsigned long long)n_fixed;
+    unsigned long long n = st->n_stored;
+    return n < st->photon_cap ? n : st->photon_cap;
+}
+__device__ __forceinline__ unsigned long long n_hitpoints(const PassState *st, long long n_fixed) {
+    if (n_fixed >= 0) return (unsigned long long)n_fixed;
+    unsigned long long n = st->n_hits;
+    return n < st->hit_cap ? n : st->hit_cap;
+}
 
 // monotone f64 <-> u64 encoding for atomicMin/atomicMax on bounds
 __device__ __forceinline__ unsigned long long ord_enc(double d) {
@@ -186,7 +203,7 @@ __global__ void __launch_bounds__(256) k_trace_photons(SceneView<T> sc, EmitPlan
 // bounds of n photons (block reduction, then one atomic per block and axis)
 template <typename T>
 __global__ void __launch_bounds__(256) k_bbox(PhotonBuf<T> buf, PassState *st, long long n_fixed) {
-    unsigned long long n = n_fixed >= 0 ? (unsigned long long)n_fixed : st->n_stored;
+    unsigned long long n = n_photons(st, n_fixed);
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
@@ -194,7 +211,7 @@ __global__ void __launch_bounds__(256) k_bbox(PhotonBuf<T> buf, PassState *st, l
         double v[3] = {(double)p.x, (double)p.y, (double)p.z};
 #pragma unroll
         for (int a = 0; a < 3; a++) {
-            if (v[a] == v[a]) { lo[a] = fmin(lo[a], v[a]); hi[a] = fmax(hi[a], v[a]); }
+            if (isfinite(v[a]) && fabs(v[a]) < 1e30) { lo[a] = fmin(lo[a], v[a]); hi[a] = fmax(hi[a], v[a]); }
         }
     }
     __shared__ double slo[3][8], shi[3][8];
@@ -244,7 +261,7 @@ __device__ __forceinline__ uint32_t cell_of(const GridParams &g, V3<T> p) {
 template <typename T>
 __global__ void __launch_bounds__(256) k_cell_hist(PhotonBuf<T> buf, PassState *st, long long n_fixed,
                                                    uint32_t *count, uint2 *keyrank) {
-    unsigned long long n = n_fixed >= 0 ? (unsigned long long)n_fixed : st->n_stored;
+    unsigned long long n = n_photons(st, n_fixed);
     const GridParams g = st->grid;
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
@@ -261,7 +278,7 @@ template <typename T> __global__ void k_scatter(PhotonBuf<T> buf, PassState *st,
 template <>
 __global__ void __launch_bounds__(256) k_scatter<double>(PhotonBuf<double> buf, PassState *st, long long n_fixed,
                                                          const uint32_t *start, const uint2 *keyrank) {
-    unsigned long long n = n_fixed >= 0 ? (unsigned long long)n_fixed : st->n_stored;
+    unsigned long long n = n_photons(st, n_fixed);
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
         uint2 kr = keyrank[i];
@@ -279,7 +296,7 @@ __global__ void __launch_bounds__(256) k_scatter<double>(PhotonBuf<double> buf, 
 template <>
 __global__ void __launch_bounds__(256) k_scatter<float>(PhotonBuf<float> buf, PassState *st, long long n_fixed,
                                                         const uint32_t *start, const uint2 *keyrank) {
-    unsigned long long n = n_fixed >= 0 ? (unsigned long long)n_fixed : st->n_stored;
+    unsigned long long n = n_photons(st, n_fixed);
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
         uint2 kr = keyrank[i];
@@ -518,7 +535,7 @@ struct GatherOutD {
 __global__ void __launch_bounds__(256) k_gather_d(const HitPoint<double> *hits, PassState *st, long long n_fixed,
                                                   const double4 *spos, const double4 *sdir, const uint32_t *start,
                                                   double pw, int pfilter, int mode, GatherOutD out) {
-    const unsigned long long nq = n_fixed >= 0 ? (unsigned long long)n_fixed : st->n_hits;
+    const unsigned long long nq = n_hitpoints(st, n_fixed);
     const GridParams g = st->grid;
     const double r2 = st->r2;
     const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -638,7 +655,7 @@ struct GatherOutF {
 __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed,
                                                   const float4 *smap, const uint32_t *start, double pw,
                                                   const double *q_r2, int pfilter, int mode, GatherOutF out) {
-    const unsigned long long nq = n_fixed >= 0 ? (unsigned long long)n_fixed : st->n_hits;
+    const unsigned long long nq = n_hitpoints(st, n_fixed);
     const GridParams g = st->grid;
     const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
