@@ -1,0 +1,380 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the PPM-PA hot path on GB300.
+
+A step is one progressive pass of the glass-box workload (512x512, 1M
+photons per pass, glass sphere IOR 1.5 + mirror sphere, point light, r0 =
+0.05, alpha = 0.7): emit + trace the photons, build the photon map, trace
+the eye rays, gather, shrink the radius, accumulate the FP64 image.  The
+pass runs as one replayed CUDA graph in the mixed-precision mode (FP32
+trace/gather with Kahan flux sums, FP64 radius/average/normalisation).
+
+Prints one JSON line (rank 0): metric Mphotons/s (emitted photons per
+second), plus the plain FP64 path's throughput, image RMSE of both paths
+against an FP64 high-pass image, the end-to-end throughput through the
+public C ABI with host buffers, the roofline of the dominant kernel, the CPU
+baseline and the SM clocks sampled during the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # BASELINE config 2: glass box, 512^2, 1M photons/pass, 64 passes
+    "glass_box_512": dict(scene="c2", reso=512, nphoton=1_000_000, passes=64, r0=0.05, alpha=0.7),
+    # BASELINE config 1: diffuse-sphere box, 256^2, 200k photons/pass, 10 passes
+    "box_256": dict(scene="c1", reso=256, nphoton=200_000, passes=10, r0=0.05, alpha=0.7),
+}
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="glass_box_512", choices=list(WORKLOADS))
+    p.add_argument("--oracle-passes", type=int, default=1024,
+                   help="passes of the FP64 high-pass image the RMSE is measured against")
+    p.add_argument("--no-rmse", action="store_true")
+    p.add_argument("--seed", type=int, default=1)
+    p.add_argument("--profile", type=int, default=0,
+                   help="only run this many mixed passes (one warm-up) and exit: the profiler's command")
+    p.add_argument("--precision", default="mixed", choices=["mixed", "plain"])
+    p.add_argument("--cell-factor", type=int, default=0, help="grid cells per radius (0: library default)")
+    return p.parse_args()
+
+
+def run_profile(args, w):
+    from ppmpa_gb300 import MIXED, PLAIN, Context, RenderConfig
+    sc, cam = scene_of(w)
+    with Context(0, seed=args.seed) as ctx:
+        ctx.upload_scene(sc)
+        ctx.set_camera(cam)
+        prec = MIXED if args.precision == "mixed" else PLAIN
+        ctx.render_begin(RenderConfig(nphoton=w["nphoton"], passes=args.profile + 1, radius0=w["r0"],
+                                      alpha=w["alpha"], precision=prec, use_graph=True, seed=args.seed,
+                                      cell_factor=args.cell_factor))
+        ctx.render_step(args.profile + 1)
+        img = ctx.render_image()
+        st = ctx.stats()
+        # one more eager pass with the gather counters on
+        ctx.set_stage_timing(2)
+        ctx.render_step(1)
+        ctx.sync()
+        cnt = ctx.stats()
+        ctx.set_stage_timing(0)
+        st["stage_ms"] = cnt["stage_ms"]
+        st.update({k: cnt[k] for k in ("candidates", "in_radius", "gather_slots")})
+    print(json.dumps({"profile_passes": args.profile + 1, "kernels_per_pass": st["kernels_per_pass"],
+                      "photons_stored": st["photons_stored"], "hit_points": st["hit_points"],
+                      "grid_cells": st["grid_cells"], "candidates": st["candidates"], "in_radius": st["in_radius"],
+                      "gather_slots": st["gather_slots"], "stage_ms_last": st["stage_ms"], "mean": float(img.mean())}))
+
+
+def scene_of(w):
+    from ppmpa_gb300 import scene as S
+    return S.box_scene(w["scene"]), S.box_camera(w["reso"])
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU: the FP64 restatement of the reference's CPU path
+# ---------------------------------------------------------------------------
+def cpu_pass_rate(w, seed, passes=1):
+    """Oracle passes (trace + eye/gather) on all host threads; returns (Mphotons/s, threads, seconds)."""
+    from oracle.binding import Oracle, radius_schedule
+    sc, cam = scene_of(w)
+    orc = Oracle(sc, cam, threads=0)
+    r2 = radius_schedule(w["r0"], w["alpha"], 1, passes)
+    img = np.zeros((cam.yreso, cam.xreso, 3))
+    t0 = time.perf_counter()
+    for k in range(passes):
+        ph = orc.trace_photons(w["nphoton"], True, seed, k)
+        img += orc.eye_pass(ph, r2[k], True, seed, k)
+    dt = time.perf_counter() - t0
+    return w["nphoton"] * passes / dt / 1e6, orc.L.orc_get_threads(), dt
+
+
+def run_reference(args, w):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    for k in range(args.warmup):
+        cpu_pass_rate(w, args.seed + 1000 + k)
+    total = 0.0
+    threads = 1
+    for k in range(args.steps):
+        _, threads, dt = cpu_pass_rate(w, args.seed + k)
+        total += dt
+    value = w["nphoton"] * args.steps / total / 1e6
+    out = {
+        "impl": "reference", "metric": "Mphotons/s per pass (emitted photons traced, full PA pass)", "value": value,
+        "unit": "Mphotons/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene, seeded photon streams)",
+        "config": {"workload": args.workload, **w},
+        "cpu_baseline": {"value": value, "unit": "Mphotons/s", "cores": threads, "kind": "port",
+                         "sample": f"one full pass per step ({w['nphoton']} photons, {w['reso']}x{w['reso']} eye "
+                                   f"rays), FP64 restatement of the reference CPU path, {threads} threads"},
+        "e2e": {"value": value, "unit": "Mphotons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+def algorithmic_bytes(stage, st, npx):
+    """Compulsory DRAM bytes of one launch of each stage (mixed-precision layout)."""
+    nq, nph, ncell = st["hit_points"], st["photons_stored"], st["grid_cells"]
+    if stage == "gather":
+        # hit point (40 B) read once, 3 FP64 adds into the pass image, each photon
+        # record (16 B) and the cell starts read once
+        return nq * (40 + 48) + nph * 16 + (ncell + 1) * 4
+    if stage == "photon_trace":
+        return nph * 16 + nph * 16          # records written once, bounds pass reads them once
+    if stage == "map_build":
+        return nph * (16 + 8) + ncell * 4 * 3 + nph * (8 + 16 + 16)
+    if stage == "eye_trace":
+        return nq * 40 + npx * 24
+    if stage == "accumulate":
+        return npx * 24 * 3
+    return 0
+
+
+def run_gpu(args, w):
+    import torch
+    from ppmpa_gb300 import MIXED, PLAIN, Context, RenderConfig
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    sc, cam = scene_of(w)
+    ctx = Context(local, seed=args.seed)
+    ctx.upload_scene(sc)
+    ctx.set_camera(cam)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def cfg(precision, passes, first=0, graph=True, seed=None):
+        return RenderConfig(nphoton=w["nphoton"], passes=passes, use_classic=True, radius0=w["r0"],
+                            alpha=w["alpha"], schedule_offset=1, precision=precision, use_graph=graph,
+                            seed=args.seed if seed is None else seed, first_pass=first, cell_factor=args.cell_factor)
+
+    def timed_passes(precision, steps, warmup, first):
+        ctx.render_begin(cfg(precision, steps + warmup, first=first))
+        ctx.render_step(warmup)
+        ctx.sync()
+        torch.cuda.synchronize()
+        barrier()
+        evs = []
+        for _ in range(steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ctx.render_step(1)
+            b.record(stream)
+            with torch.cuda.stream(stream):
+                flush.zero_()          # evict L2 between timed passes (not timed)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        ctx.sync()
+        barrier()
+        ms = sum(a.elapsed_time(b) for a, b in evs)
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([ms], device=f"cuda:{local}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    base_pass = rank * 1_000_000
+    clocks = Clocks(local)
+    clocks.start()
+    ms = timed_passes(MIXED, args.steps, max(3, args.warmup), base_pass)
+    clk = clocks.stop()
+    st = ctx.stats()
+    value = world * args.steps * w["nphoton"] / (ms / 1e3) / 1e6
+    kernels_per_pass = st["kernels_per_pass"]
+
+    # per-stage device time (eager passes with CUDA events between stages)
+    ctx.render_begin(cfg(MIXED, args.steps, first=base_pass + 500_000, graph=False))
+    ctx.set_stage_timing(True)
+    ctx.render_step(args.steps)
+    ctx.sync()
+    st_t = ctx.stats()
+    ctx.set_stage_timing(False)
+    npx = w["reso"] * w["reso"]
+    stage_avg = {k: st_t["stage_ms"][k] / max(1, st_t["stage_calls"][k]) for k in st_t["stage_ms"]}
+    dominant = max(stage_avg, key=stage_avg.get)
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak, peak_src = json.load(open(peaks_path))["hbm_gbs"], "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    ab = algorithmic_bytes(dominant, st_t, npx)
+    achieved = ab / (stage_avg[dominant] / 1e3) / 1e9
+    traffic = None
+    prof_sum = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof_sum):
+        traffic = json.load(open(prof_sum)).get(dominant)
+
+    # plain FP64 path on the same workload
+    steps_plain = max(3, min(args.steps, 10))
+    ms_plain = timed_passes(PLAIN, steps_plain, 2, base_pass + 800_000)
+    value_plain = world * steps_plain * w["nphoton"] / (ms_plain / 1e3) / 1e6
+
+    out_rmse = None
+    if not args.no_rmse and rank == 0:
+        P = w["passes"]
+        ctx.render_begin(cfg(MIXED, P))
+        ctx.render_step(P)
+        img_mixed = ctx.render_image()
+        ctx.render_begin(cfg(PLAIN, P))
+        ctx.render_step(P)
+        img_plain = ctx.render_image()
+        t0 = time.perf_counter()
+        ctx.render_begin(cfg(PLAIN, args.oracle_passes, seed=args.seed + 7919))
+        ctx.render_step(args.oracle_passes)
+        img_ref = ctx.render_image()
+        t_oracle = time.perf_counter() - t0
+        rm = float(np.sqrt(np.mean((img_mixed - img_ref) ** 2)))
+        rp = float(np.sqrt(np.mean((img_plain - img_ref) ** 2)))
+        out_rmse = {"mixed": rm, "plain": rp, "mixed_over_plain": rm / rp, "passes": P,
+                    "oracle": f"FP64 plain GPU path, {args.oracle_passes} passes, independent seed",
+                    "oracle_seconds": round(t_oracle, 2), "mean_radiance": float(img_ref.mean())}
+
+    # end to end through the public C ABI: scene + camera upload, a full
+    # progressive render, image download (host buffers), per step
+    e2e_steps = 3
+    ctx.sync()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        ctx.upload_scene(sc)
+        ctx.set_camera(cam)
+        img = ctx.render(cfg(MIXED, w["passes"], first=base_pass + 900_000 + k * w["passes"]))
+    t_e2e = time.perf_counter() - t0
+    e2e_value = world * e2e_steps * w["passes"] * w["nphoton"] / t_e2e / 1e6
+    import ctypes
+    from ppmpa_gb300 import scene as S
+    h2d = (ctypes.sizeof(S.Object) * len(sc.objects) + ctypes.sizeof(S.Material) * len(sc.materials) +
+           ctypes.sizeof(S.Light) * len(sc.lights) + ctypes.sizeof(S.Camera))
+    d2h = img.nbytes
+
+    cpu = None
+    if rank == 0:
+        rate, threads, dt = cpu_pass_rate(w, args.seed, 1)
+        cpu = {"value": rate, "unit": "Mphotons/s", "cores": threads, "kind": "port",
+               "sample": f"one full pass ({w['nphoton']} photons, {w['reso']}x{w['reso']}), FP64 restatement "
+                         f"of the reference CPU path, {threads} threads, {dt:.2f} s"}
+
+    ctx.close()
+    if rank != 0:
+        return
+    out = {
+        "metric": "Mphotons/s per pass (emitted photons traced through a full PA pass), mixed precision",
+        "value": value, "unit": "Mphotons/s", "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 trace/gather, f64 radius/average", "data": "synthetic (seeded scene, seeded photon streams)",
+        "config": {"workload": args.workload, **w, "precision": "mixed", "cuda_graph": True,
+                   "l2": "flushed between timed passes (2x L2 write)", "parallelism": f"passes x{world}"},
+        "plain_fp64": {"value": value_plain, "unit": "Mphotons/s", "ms_per_step": ms_plain / steps_plain,
+                       "mixed_over_plain": value / value_plain},
+        "rmse": out_rmse,
+        "e2e": {"value": e2e_value, "unit": "Mphotons/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "step": f"ppm_scene_upload + ppm_camera_set + ppm_render({w['passes']} passes) + image download"},
+        "gpu_launches": kernels_per_pass * args.steps,
+        "kernels_per_pass": kernels_per_pass,
+        "stages_ms_per_pass": {k: round(v, 4) for k, v in stage_avg.items()},
+        "roofline": {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                     "algorithmic_bytes": ab},
+        "pass_stats": {"photons_stored": st["photons_stored"], "hit_points": st["hit_points"],
+                       "grid_cells": st["grid_cells"]},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+    }
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    w = WORKLOADS[args.workload]
+    if args.profile:
+        run_profile(args, w)
+    elif args.impl == "reference":
+        run_reference(args, w)
+    else:
+        run_gpu(args, w)
+
+
+if __name__ == "__main__":
+    main()

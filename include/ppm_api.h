@@ -135,8 +135,9 @@ typedef struct ppm_stats {
     double  r2;                /* radius^2 of the last pass */
     double  stage_ms[16];      /* summed device time per stage (timing on) */
     int64_t stage_calls[16];
-    int64_t candidates;        /* photons tested by the gather (last pass, if counted) */
-    int64_t in_radius;         /* photons found in radius (last pass, if counted) */
+    int64_t candidates;        /* photons tested by the gather (last pass, stage timing level 2) */
+    int64_t in_radius;         /* photons found in radius (last pass, stage timing level 2) */
+    int64_t gather_slots;      /* lane slots the gather issued (last pass, stage timing level 2) */
 } ppm_stats;
 
 typedef struct ppm_ctx ppm_ctx;
@@ -225,7 +226,8 @@ int ppm_render_step(ppm_ctx *ctx, int32_t npasses);
 int ppm_render_image(ppm_ctx *ctx, double *image_out);
 int ppm_render_pass_image(ppm_ctx *ctx, double *image_out);  /* the last pass alone */
 int ppm_render_stats(ppm_ctx *ctx, ppm_stats *out);
-/* Record per-stage CUDA events inside every pass (adds event nodes). */
+/* on = 1: record per-stage CUDA events inside every pass (passes then run
+ * eagerly, not as a graph); on = 2: also count gather candidates and hits. */
 int ppm_set_stage_timing(ppm_ctx *ctx, int32_t on);
 const char *ppm_stage_name(int32_t stage);
 

@@ -41,13 +41,14 @@ class RenderConfig:
     cell_factor: int = 0
     seed: int = 1
     first_pass: int = 0
+    flags: int = 0
 
     def to_c(self) -> S.RenderCfg:
         c = S.RenderCfg()
         c.nphoton, c.passes, c.use_classic = int(self.nphoton), int(self.passes), int(bool(self.use_classic))
         c.radius0, c.alpha, c.schedule_offset = float(self.radius0), float(self.alpha), int(self.schedule_offset)
         c.precision, c.use_graph, c.cell_factor = int(self.precision), int(bool(self.use_graph)), int(self.cell_factor)
-        c.seed, c.first_pass, c.flags = int(self.seed), int(self.first_pass), 0
+        c.seed, c.first_pass, c.flags = int(self.seed), int(self.first_pass), int(self.flags)
         return c
 
 
@@ -225,8 +226,9 @@ class Context:
         self._check(self.lib.ppm_render_pass_image(self.h, _ptr(img, C.c_double)))
         return img
 
-    def set_stage_timing(self, on: bool):
-        self._check(self.lib.ppm_set_stage_timing(self.h, int(bool(on))))
+    def set_stage_timing(self, on):
+        """0 off, 1 per-stage CUDA events, 2 events + gather candidate counters."""
+        self._check(self.lib.ppm_set_stage_timing(self.h, int(on)))
 
     def stats(self) -> dict:
         s = S.Stats()
@@ -234,5 +236,6 @@ class Context:
         names = [self.lib.ppm_stage_name(i).decode() for i in range(s.n_stages)]
         return dict(photons_emitted=s.photons_emitted, photons_stored=s.photons_stored, hit_points=s.hit_points,
                     grid_cells=s.grid_cells, passes_done=s.passes_done, kernels_per_pass=s.kernels_per_pass,
-                    r2=s.r2, stage_ms={n: s.stage_ms[i] for i, n in enumerate(names)},
+                    r2=s.r2, candidates=s.candidates, in_radius=s.in_radius, gather_slots=s.gather_slots,
+                    stage_ms={n: s.stage_ms[i] for i, n in enumerate(names)},
                     stage_calls={n: s.stage_calls[i] for i, n in enumerate(names)})

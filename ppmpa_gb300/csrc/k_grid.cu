@@ -14,6 +14,8 @@ __global__ void k_pass_begin(PassState *st) {
     st->n_hits = 0;
     st->candidates = 0;
     st->in_radius = 0;
+    st->slots = 0;
+    st->rows = 0;
     for (int a = 0; a < 3; a++) {
         st->bb_lo[a] = ord_enc(1e300);
         st->bb_hi[a] = ord_enc(-1e300);

@@ -85,6 +85,7 @@ struct ppm_ctx {
 
     // timing
     bool timing = false;
+    bool count_gather = false;
     cudaEvent_t tev[TIMING_SLOTS][8];
     bool tev_made = false;
     int slot_head = 0, slot_pending = 0;
@@ -841,11 +842,13 @@ extern "C" int ppm_set_stage_timing(ppm_ctx *ctx, int32_t on) {
         ctx->tev_made = true;
     }
     ctx->timing = on != 0;
+    ctx->count_gather = on >= 2;   // level 2 also counts gather candidates / hits
     return PPM_OK;
 }
 
 // event slot layout: 0 pass start, 1 after trace+bbox, 2 after map build,
-// 3 after gather, 4 after accumulate/end; 5/6 eye start/end on the side stream
+// 7 after joining the eye stream, 3 after gather, 4 after accumulate/end;
+// 5/6 eye start/end on the side stream
 static int drain_timing(ppm_ctx *ctx) {
     if (ctx->slot_pending == 0) return PPM_OK;
     CK(cudaStreamSynchronize(ctx->s));
@@ -854,7 +857,7 @@ static int drain_timing(ppm_ctx *ctx) {
         int slot = (ctx->slot_head - ctx->slot_pending + k + TIMING_SLOTS) % TIMING_SLOTS;
         cudaEvent_t *e = ctx->tev[slot];
         float ms;
-        const int pairs[N_STAGES][2] = {{0, 1}, {1, 2}, {5, 6}, {2, 3}, {3, 4}};
+        const int pairs[N_STAGES][2] = {{0, 1}, {1, 2}, {5, 6}, {7, 3}, {3, 4}};
         for (int st = 0; st < N_STAGES; st++) {
             CK(cudaEventElapsedTime(&ms, e[pairs[st][0]], e[pairs[st][1]]));
             ctx->stage_ms[st] += ms;
@@ -917,8 +920,9 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
     kernels += 5 + kernels_per_scan();
     if (ev) CK(cudaEventRecord(ev[2], s));
     CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+    if (ev) CK(cudaEventRecord(ev[7], s));
     if (mixed) {
-        GatherOutF go{as<double>(ctx->pass_img), nullptr, nullptr};
+        GatherOutF go{as<double>(ctx->pass_img), nullptr, ctx->count_gather ? &ctx->st->candidates : nullptr};
         launch_gather_f(as<HitPoint<float>>(ctx->hits_f), ctx->st, -1, as<float4>(ctx->sorted_f), as<uint32_t>(ctx->start),
                         ctx->pw, nullptr, ctx->cam.pfilter, 0, go, g8, s);
     } else {
@@ -1062,6 +1066,7 @@ extern "C" int ppm_render_stats(ppm_ctx *ctx, ppm_stats *out) {
     for (int i = 0; i < 16; i++) { out->stage_ms[i] = ctx->stage_ms[i]; out->stage_calls[i] = ctx->stage_calls[i]; }
     out->candidates = (int64_t)h.candidates;
     out->in_radius = (int64_t)h.in_radius;
+    out->gather_slots = (int64_t)h.slots;
     return PPM_OK;
 }
 

@@ -105,7 +105,15 @@ struct Rng {
         return v;
     }
     __device__ __forceinline__ double u64d() { return (double)(next64() >> 12) * 0x1p-52; }
-    __device__ __forceinline__ float u32f() { return (float)(uint32_t)(next64() >> 40) * 0x1p-24f; }
+    // FP32 draws use every 32-bit word of a block (4 draws per Philox call);
+    // an Rng instance serves one precision only
+    __device__ __forceinline__ float u32f() {
+        int w = k & 3;
+        if (w == 0) philox4x32_10(item, pass, tag, (uint32_t)(k >> 2), k0, k1, buf);
+        uint32_t v = w == 0 ? buf[0] : (w == 1 ? buf[1] : (w == 2 ? buf[2] : buf[3]));
+        k++;
+        return (float)(v >> 8) * 0x1p-24f;
+    }
 };
 
 template <typename T> struct RngT;
@@ -258,11 +266,28 @@ template <typename T> __device__ __forceinline__ T pow5(T x) { T x2 = x * x; T x
 // Device scene tables (converted from the ABI structs to precision T)
 // ---------------------------------------------------------------------------
 template <typename T>
-struct DObject {
+struct alignas(16) DObject {
     int32_t shape, mat;
     T p[3], n[3], d1[3], d2[3];
     T dist, radius;
 };
+static_assert(sizeof(DObject<float>) == 64, "FP32 object = four 16-byte vectors");
+static_assert(sizeof(DObject<double>) == 128, "FP64 object = eight 16-byte vectors");
+
+// object fetch with 16-byte vector loads (the table is read by every lane
+// for every ray, uniformly: each load is one broadcast transaction)
+template <typename T>
+__device__ __forceinline__ DObject<T> load_object(const DObject<T> *objs, int i) {
+    constexpr int NV = sizeof(DObject<T>) / 16;
+    union {
+        uint4 v[NV];
+        DObject<T> o;
+    } u;
+    const uint4 *src = reinterpret_cast<const uint4 *>(objs + i);
+#pragma unroll
+    for (int k = 0; k < NV; k++) u.v[k] = __ldg(src + k);
+    return u.o;
+}
 
 template <typename T>
 struct DMaterial {

@@ -41,7 +41,8 @@ struct PassState {
     unsigned int pad;
     unsigned long long bb_lo[3], bb_hi[3];   // orderable encodings of f64 bounds
     GridParams grid;
-    unsigned long long candidates, in_radius;
+    unsigned long long candidates, in_radius;   // gather counters (valid candidates, hits)
+    unsigned long long slots, rows;             // lane slots issued, non-empty rows visited
     double cell_factor;
     int64_t cell_cap;
     unsigned long long photon_cap;   // buffers hold at most this many photons
@@ -435,17 +436,12 @@ __global__ void __launch_bounds__(128) k_eye(SceneView<T> sc, DCamera<T> cam, ui
 }
 
 // ---------------------------------------------------------------------------
-// candidate enumeration: the (2e+1)^2 x-rows of cells around a query are
-// concatenated; lanes stride over the concatenation.  Rows are processed in
-// chunks of 32 (one row per lane), a lane finds its row by binary search
-// over the rows' inclusive prefix sums held across the warp.
+// candidate enumeration: the (2e+1)^2 x-rows of cells around a query (each
+// row spans 2e+1 cells, contiguous in the sorted map).  Lane j holds row j
+// (rows in chunks of 32); the warp walks the non-empty rows in order and its
+// lanes stride through each row, so a candidate costs an increment, not a
+// search.
 // ---------------------------------------------------------------------------
-struct RowChunk {
-    uint32_t begin;   // this lane's row begin (photon index)
-    uint32_t incl;    // inclusive prefix of row lengths (this lane's row)
-    uint32_t total;
-};
-
 template <typename T>
 __device__ __forceinline__ void query_cells(const GridParams &g, V3<T> q, int ext, int c[3], int lo[3], int hi[3]) {
     c[0] = CellMath<T>::coord(g, q.x, 0);
@@ -458,44 +454,99 @@ __device__ __forceinline__ void query_cells(const GridParams &g, V3<T> q, int ex
     }
 }
 
-__device__ __forceinline__ RowChunk make_chunk(const GridParams &g, const uint32_t *start, const int lo[3], const int hi[3],
-                                               int row0) {
+struct RowSet {
+    uint32_t begin, len;   // this lane's row (culled x-range)
+    unsigned nonempty;     // ballot of rows with len > 0
+};
+
+// Row culling: the row (yy, zz) can hold a photon within r of q only where
+// the sphere reaches its y/z slab; its x-range shrinks to the sphere's chord
+// there.  The slab bounds are widened and the chord lengthened by margins
+// that exceed the rounding of the cell coordinates (<= 3 ulp of <= 8192
+// cells), so the culled set still contains every photon within r; the exact
+// predicate then decides membership.
+template <typename T> struct RowCull;
+template <> struct RowCull<float> {
+    __device__ static __forceinline__ bool range(const GridParams &g, V3<float> q, float r2, int yy, int zz,
+                                                 int lo_x, int hi_x, int &x0, int &x1) {
+        const float c = (float)g.cell, m = 4e-3f * c;
+        const float ylo = g.orgf[1] + (float)yy * c, zlo = g.orgf[2] + (float)zz * c;
+        const float dy = fmaxf(0.0f, fmaxf(ylo - q.y, q.y - (ylo + c)) - m);
+        const float dz = fmaxf(0.0f, fmaxf(zlo - q.z, q.z - (zlo + c)) - m);
+        const float rem = r2 * 1.00002f - dy * dy - dz * dz;
+        if (rem < 0.0f) return false;
+        const float rx = sqrtf(rem) * 1.00001f;
+        const float fx0 = floorf((q.x - rx - g.orgf[0]) * g.invf - 4e-3f);
+        const float fx1 = floorf((q.x + rx - g.orgf[0]) * g.invf + 4e-3f);
+        x0 = max(lo_x, (int)fmaxf(fx0, -1.0f));
+        x1 = min(hi_x, (int)fminf(fx1, (float)g.dim[0]));
+        return x0 <= x1;
+    }
+};
+template <> struct RowCull<double> {
+    __device__ static __forceinline__ bool range(const GridParams &g, V3<double> q, double r2, int yy, int zz,
+                                                 int lo_x, int hi_x, int &x0, int &x1) {
+        const double c = g.cell, m = 1e-6 * c;
+        const double ylo = g.org[1] + (double)yy * c, zlo = g.org[2] + (double)zz * c;
+        const double dy = fmax(0.0, fmax(ylo - q.y, q.y - (ylo + c)) - m);
+        const double dz = fmax(0.0, fmax(zlo - q.z, q.z - (zlo + c)) - m);
+        const double rem = r2 * (1.0 + 1e-12) - dy * dy - dz * dz;
+        if (rem < 0.0) return false;
+        const double rx = sqrt(rem) * (1.0 + 1e-12);
+        const double fx0 = floor((q.x - rx - g.org[0]) * g.inv - 1e-6);
+        const double fx1 = floor((q.x + rx - g.org[0]) * g.inv + 1e-6);
+        x0 = max(lo_x, (int)fmax(fx0, -1.0));
+        x1 = min(hi_x, (int)fmin(fx1, (double)g.dim[0]));
+        return x0 <= x1;
+    }
+};
+
+template <typename T>
+__device__ __forceinline__ RowSet make_rows(const GridParams &g, const uint32_t *start, V3<T> q, T r2, const int lo[3],
+                                            const int hi[3], int row0) {
     const int ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
     const int nrows = ny * nz;
     int row = row0 + (int)lane_id();
-    uint32_t b = 0, len = 0;
+    RowSet rs;
+    rs.begin = 0;
+    rs.len = 0;
+    int x0, x1;
     if (row < nrows) {
-        int yy = lo[1] + row % ny, zz = lo[2] + row / ny;
-        int base = (zz * g.dim[1] + yy) * g.dim[0];
-        b = start[base + lo[0]];
-        len = start[base + hi[0] + 1] - b;
+        int zi = row / ny;
+        int yy = lo[1] + (row - zi * ny), zz = lo[2] + zi;
+        if (RowCull<T>::range(g, q, r2, yy, zz, lo[0], hi[0], x0, x1)) {
+            int base = (zz * g.dim[1] + yy) * g.dim[0];
+            rs.begin = start[base + x0];
+            rs.len = start[base + x1 + 1] - rs.begin;
+        }
     }
-    uint32_t incl = len;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-        if ((int)lane_id() >= o) incl += v;
-    }
-    RowChunk rc;
-    rc.begin = b;
-    rc.incl = incl;
-    rc.total = __shfl_sync(0xffffffffu, incl, 31);
-    return rc;
+    rs.nonempty = __ballot_sync(0xffffffffu, rs.len > 0);
+    return rs;
 }
 
-// photon index of virtual position v (< rc.total) of the chunk.  All lanes
-// must call this (it shuffles with the full mask).
-__device__ __forceinline__ uint32_t chunk_index(const RowChunk &rc, uint32_t v) {
-    int lo = 0;
-#pragma unroll
-    for (int step = 16; step > 0; step >>= 1) {
-        uint32_t val = __shfl_sync(0xffffffffu, rc.incl, lo + step - 1);
-        if (val <= v) lo += step;
+// calls f(photon_index, valid) for every candidate of the query, lanes in
+// parallel; all lanes of the warp must enter (warp-uniform query)
+template <typename T, typename F>
+__device__ __forceinline__ void for_each_candidate(const GridParams &g, const uint32_t *start, V3<T> q, T r2,
+                                                   const int lo[3], const int hi[3], F &&f) {
+    const int nrows = (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+    for (int row0 = 0; row0 < nrows; row0 += 32) {
+        RowSet rs = make_rows(g, start, q, r2, lo, hi, row0);
+        unsigned m = rs.nonempty;
+        while (m) {
+            int r = __ffs(m) - 1;
+            m &= m - 1;
+            uint32_t b = __shfl_sync(0xffffffffu, rs.begin, r);
+            uint32_t n = __shfl_sync(0xffffffffu, rs.len, r);
+            // warp-uniform trip count: every lane runs every iteration (lanes
+            // past the row end with valid = false), so warp-collective code
+            // inside f is reached by the whole warp at the same point
+            for (uint32_t base = 0; base < n; base += 32) {
+                uint32_t o = base + lane_id();
+                f(o < n ? b + o : 0u, o < n);
+            }
+        }
     }
-    uint32_t b = __shfl_sync(0xffffffffu, rc.begin, lo);
-    uint32_t prev = __shfl_sync(0xffffffffu, rc.incl, (lo + 31) & 31);
-    if (lo == 0) prev = 0u;
-    return b + (v - prev);
 }
 
 __device__ __forceinline__ double filter_wt(int pfilter, double d, double r2) {
@@ -545,28 +596,21 @@ __global__ void __launch_bounds__(256) k_gather_d(const HitPoint<double> *hits, 
         V3<double> q = ld3(h.pos), n = ld3(h.nrm);
         int c[3], lo[3], hi[3];
         query_cells(g, q, g.ext, c, lo, hi);
-        const int nrows = (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
         double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-        for (int row0 = 0; row0 < nrows; row0 += 32) {
-            RowChunk rc = make_chunk(g, start, lo, hi, row0);
-            for (uint32_t base = 0; base < rc.total; base += 32) {
-                uint32_t v = base + lane_id();
-                uint32_t idx = chunk_index(rc, min(v, rc.total - 1));
-                if (v < rc.total) {
-                    double4 pp = spos[idx];
-                    double d = sq_euclid(q.x, q.y, q.z, pp.x, pp.y, pp.z);
-                    if (d <= r2) {
-                        double4 pd = sdir[idx];
-                        double wt = filter_wt(pfilter, d, r2);
-                        double pwt = wt * pw;
-                        double cos0 = dot(n, mk3(pd.x, pd.y, pd.z));
-                        double pw2 = cos0 < 0.0 ? pwt * -cos0 : 0.0;
-                        int wl = (int)(((unsigned long long)__double_as_longlong(pp.w)) >> 40);
-                        if (wl == 0) s0 += pw2; else if (wl == 1) s1 += pw2; else s2 += pw2;
-                    }
-                }
+        for_each_candidate(g, start, q, r2, lo, hi, [&](uint32_t idx, bool valid) {
+            if (!valid) return;
+            double4 pp = spos[idx];
+            double d = sq_euclid(q.x, q.y, q.z, pp.x, pp.y, pp.z);
+            if (d <= r2) {
+                double4 pd = sdir[idx];
+                double wt = filter_wt(pfilter, d, r2);
+                double pwt = wt * pw;
+                double cos0 = dot(n, mk3(pd.x, pd.y, pd.z));
+                double pw2 = cos0 < 0.0 ? pwt * -cos0 : 0.0;
+                int wl = (int)(((unsigned long long)__double_as_longlong(pp.w)) >> 40);
+                if (wl == 0) s0 += pw2; else if (wl == 1) s1 += pw2; else s2 += pw2;
             }
-        }
+        });
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             s0 += __shfl_xor_sync(0xffffffffu, s0, o);
@@ -657,6 +701,7 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
                                                   const double *q_r2, int pfilter, int mode, GatherOutF out) {
     const unsigned long long nq = n_hitpoints(st, n_fixed);
     const GridParams g = st->grid;
+    const unsigned lane = lane_id();
     const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
     for (unsigned long long qi = warp; qi < nq; qi += nwarps) {
@@ -664,37 +709,49 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
         const double r2 = q_r2 ? q_r2[qi] : st->r2;
         const float r2_lo = __double2float_rd(r2 * (1.0 - 1e-6));
         const float r2_hi = __double2float_ru(r2 * (1.0 + 1e-6));
+        const float r2f = (float)r2;
         int ext = g.ext;
         if (q_r2) ext = min(g.ext, max(1, (int)ceil(sqrt(r2) * g.inv + 3e-3)));
         V3<float> q = ld3(h.pos), n = ld3(h.nrm);
         int c[3], lo[3], hi[3];
         query_cells(g, q, ext, c, lo, hi);
-        const int nrows = (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
         Kahan k0 = {0.f, 0.f}, k1 = {0.f, 0.f}, k2 = {0.f, 0.f};
-        for (int row0 = 0; row0 < nrows; row0 += 32) {
-            RowChunk rc = make_chunk(g, start, lo, hi, row0);
-            for (uint32_t base = 0; base < rc.total; base += 32) {
-                uint32_t v = base + lane_id();
-                uint32_t idx = chunk_index(rc, min(v, rc.total - 1));
-                if (v < rc.total) {
-                    float4 pp = smap[idx];
-                    float d2f;
-                    if (in_radius_f32(q.x, q.y, q.z, pp, r2_lo, r2_hi, r2, d2f)) {
-                        uint32_t m = __float_as_uint(pp.w);
-                        V3<float> pd = oct_unpack(m);
-                        float cos0 = dot(n, pd);
-                        float val = cos0 < 0.0f ? -cos0 : 0.0f;
-                        if (pfilter != PF_NONE) val *= filter_wt_f(pfilter, d2f, (float)r2);
-                        int wl = (int)(m >> 30);
-                        k0.add(wl == 0 ? val : 0.0f);
-                        k1.add(wl == 1 ? val : 0.0f);
-                        k2.add(wl == 2 ? val : 0.0f);
-                    }
-                }
+        unsigned long long c_slots = 0, c_valid = 0, c_hits = 0;
+        for_each_candidate(g, start, q, r2f, lo, hi, [&](uint32_t idx, bool valid) {
+            if (out.count) {
+                c_slots += 1;
+                c_valid += valid;
+            }
+            if (!valid) return;
+            float4 pp = smap[idx];
+            float d2f;
+            if (in_radius_f32(q.x, q.y, q.z, pp, r2_lo, r2_hi, r2, d2f)) {
+                uint32_t m = __float_as_uint(pp.w);
+                V3<float> pd = oct_unpack(m);
+                float cos0 = dot(n, pd);
+                float val = cos0 < 0.0f ? -cos0 : 0.0f;
+                if (pfilter != PF_NONE) val *= filter_wt_f(pfilter, d2f, r2f);
+                int wl = (int)(m >> 30);
+                k0.add(wl == 0 ? val : 0.0f);
+                k1.add(wl == 1 ? val : 0.0f);
+                k2.add(wl == 2 ? val : 0.0f);
+                if (out.count) c_hits += 1;
+            }
+        });
+        float s0 = warp_sum_comp(k0), s1 = warp_sum_comp(k1), s2 = warp_sum_comp(k2);
+        if (out.count) {
+            for (int o = 16; o > 0; o >>= 1) {
+                c_slots += __shfl_xor_sync(0xffffffffu, c_slots, o);
+                c_valid += __shfl_xor_sync(0xffffffffu, c_valid, o);
+                c_hits += __shfl_xor_sync(0xffffffffu, c_hits, o);
+            }
+            if (lane == 0) {
+                atomicAdd(out.count + 0, c_valid);
+                atomicAdd(out.count + 1, c_hits);
+                atomicAdd(out.count + 2, c_slots);
             }
         }
-        float s0 = warp_sum_comp(k0), s1 = warp_sum_comp(k1), s2 = warp_sum_comp(k2);
-        if (lane_id() == 0) {
+        if (lane == 0) {
             double kk = pw * (ONE_PI_D / r2);
             if (mode == 0) {
                 double *px = out.pass_img + 3 * (long long)h.pixel;
@@ -731,32 +788,26 @@ __global__ void __launch_bounds__(256) k_within(const T *q, long long nq, const 
         int ext = min(g.ext, max(1, (int)ceil(sqrt(r2) * g.inv + 3e-3)));
         int c[3], lo[3], hi[3];
         query_cells(g, qq, ext, c, lo, hi);
-        const int nrows = (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
         unsigned long long found = 0;
         unsigned long long wbase = offsets ? offsets[qi] : 0;
-        for (int row0 = 0; row0 < nrows; row0 += 32) {
-            RowChunk rc = make_chunk(g, start, lo, hi, row0);
-            for (uint32_t base = 0; base < rc.total; base += 32) {
-                uint32_t v = base + lane_id();
-                uint32_t idx = chunk_index(rc, min(v, rc.total - 1));
-                bool hit = false;
-                int32_t orig = 0;
-                if (v < rc.total) {
-                    if constexpr (sizeof(T) == 8) {
-                        double4 pp = smap[idx];
-                        hit = sq_euclid(qq.x, qq.y, qq.z, pp.x, pp.y, pp.z) <= r2;
-                        orig = (int32_t)(((unsigned long long)__double_as_longlong(pp.w)) & 0xffffffffffULL);
-                    } else {
-                        float d2f;
-                        hit = in_radius_f32(qq.x, qq.y, qq.z, smap[idx], r2_lo, r2_hi, r2, d2f);
-                        orig = sidx[idx];
-                    }
+        for_each_candidate(g, start, qq, (T)r2, lo, hi, [&](uint32_t idx, bool valid) {
+            bool hit = false;
+            int32_t orig = 0;
+            if (valid) {
+                if constexpr (sizeof(T) == 8) {
+                    double4 pp = smap[idx];
+                    hit = sq_euclid(qq.x, qq.y, qq.z, pp.x, pp.y, pp.z) <= r2;
+                    orig = (int32_t)(((unsigned long long)__double_as_longlong(pp.w)) & 0xffffffffffULL);
+                } else {
+                    float d2f;
+                    hit = in_radius_f32(qq.x, qq.y, qq.z, smap[idx], r2_lo, r2_hi, r2, d2f);
+                    orig = sidx[idx];
                 }
-                unsigned m = __ballot_sync(0xffffffffu, hit);
-                if (idx_out && hit) idx_out[wbase + found + __popc(m & ((1u << lane_id()) - 1u))] = orig;
-                found += __popc(m);
             }
-        }
+            unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (idx_out && hit) idx_out[wbase + found + __popc(m & ((1u << lane_id()) - 1u))] = orig;
+            found += __popc(m);
+        });
         if (lane_id() == 0 && counts) counts[qi] = found;
     }
 }

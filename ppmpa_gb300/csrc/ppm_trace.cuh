@@ -18,17 +18,34 @@ template <typename T> struct Cst {
 // ---------------------------------------------------------------------------
 // Shapes: src/ray/geometry.rs:132-202
 // ---------------------------------------------------------------------------
+template <typename T> struct Div;
+template <> struct Div<double> {   // FP64: true division, as the reference
+    double inv;
+    __device__ __forceinline__ explicit Div(double d) : inv(d) {}
+    __device__ __forceinline__ double of(double x) const { return x / inv; }
+};
+template <> struct Div<float> {    // FP32: one reciprocal, three multiplies
+    float inv;
+    __device__ __forceinline__ explicit Div(float d) : inv(1.0f / d) {}
+    __device__ __forceinline__ float of(float x) const { return x * inv; }
+};
+
+// Moller-Trumbore as method_moller (geometry.rs:149-165), with early exits:
+// every value that decides the result is computed exactly as the reference
+// computes it, so the FP64 outcome is unchanged.
 template <typename T>
 __device__ __forceinline__ bool method_moller(T l, V3<T> p0, V3<T> d1, V3<T> d2, V3<T> p, V3<T> d, T &t) {
     V3<T> re2 = cross(d, d2);
     T det_a = dot(re2, d1);
+    if (det_a == T(0)) return false;
+    Div<T> dv(det_a);
     V3<T> pp = p - p0;
+    T u = dv.of(dot(re2, pp));
+    if (u < T(0) || u > T(1)) return false;
     V3<T> te1 = cross(pp, d1);
-    T u = dot(re2, pp) / det_a;
-    T v = dot(te1, d) / det_a;
-    T tt = dot(te1, d2) / det_a;
-    if (det_a == T(0) || u < T(0) || u > T(1) || v < T(0) || v > T(1) || u + v > l) return false;
-    t = tt;
+    T v = dv.of(dot(te1, d));
+    if (v < T(0) || v > T(1) || u + v > l) return false;
+    t = dv.of(dot(te1, d2));
     return true;
 }
 
@@ -79,12 +96,13 @@ __device__ __forceinline__ bool intersect(const SceneView<T> &sc, V3<T> rp, V3<T
     int bi = -1;
     for (int i = 0; i < sc.n_objs; i++) {
         T ta, tb;
-        int k = shape_distance(sc.objs[i], rp, rd, ta, tb);
+        const DObject<T> o = load_object(sc.objs, i);
+        int k = shape_distance(o, rp, rd, ta, tb);
         if (k >= 1 && ta >= Cst<T>::nearly0() && (bi < 0 || ta < best)) { best = ta; bi = i; }
         if (k == 2 && tb >= Cst<T>::nearly0() && (bi < 0 || tb < best)) { best = tb; bi = i; }
     }
     if (bi < 0) return false;
-    const DObject<T> &o = sc.objs[bi];
+    const DObject<T> o = load_object(sc.objs, bi);
     V3<T> p = rp + rd * best;
     V3<T> n;
     if (o.shape == SH_SPHERE) {

@@ -68,7 +68,8 @@ class Stats(C.Structure):
     _fields_ = [("photons_emitted", C.c_int64), ("photons_stored", C.c_int64), ("hit_points", C.c_int64),
                 ("grid_cells", C.c_int64), ("passes_done", C.c_int64), ("kernels_per_pass", C.c_int32),
                 ("n_stages", C.c_int32), ("r2", C.c_double), ("stage_ms", C.c_double * 16),
-                ("stage_calls", C.c_int64 * 16), ("candidates", C.c_int64), ("in_radius", C.c_int64)]
+                ("stage_calls", C.c_int64 * 16), ("candidates", C.c_int64), ("in_radius", C.c_int64),
+                ("gather_slots", C.c_int64)]
 
 
 # ---------------------------------------------------------------------------

@@ -253,3 +253,21 @@ def test_error_paths(ctx):
     with pytest.raises(PPMError) as e:
         ctx.upload_scene(bad)
     assert e.value.status == 1
+
+
+
+def test_cell_factors_give_the_same_image(ctx):
+    # the grid granularity changes which candidates are tested, never the
+    # in-radius sets; images agree up to FP32 summation order
+    sc, cam, orc = _setup(ctx, "box_c2")
+    imgs = []
+    for prec in (MIXED, PLAIN):
+        for cf in (1, 2):
+            cfg = RenderConfig(nphoton=30000, passes=1, radius0=0.08, precision=prec, use_graph=False, seed=21,
+                               cell_factor=cf)
+            ctx.render_begin(cfg)
+            ctx.render_step(1)
+            imgs.append(ctx.render_pass_image())
+    assert np.allclose(imgs[1], imgs[0], rtol=2e-5, atol=1e-7 * imgs[0].max())
+    assert np.allclose(imgs[3], imgs[2], rtol=1e-12, atol=1e-14 * imgs[2].max())
+    assert imgs[0].max() > 0
