@@ -6,9 +6,14 @@
 
 namespace ppm {
 
-void launch_trace_f(const SceneView<float> &sc, const EmitPlan &plan, uint64_t seed, PassState *st, int uc,
-                    PhotonBuf<float> out, unsigned long long cap, int grid, cudaStream_t s) {
-    k_trace_photons<float><<<grid, 256, 0, s>>>(sc, plan, seed, st, uc, out, cap);
+void launch_emit_f(const SceneView<float> &sc, const EmitPlan &plan, uint64_t seed, const PassState *st,
+                   RayQueue<float> q, int grid, cudaStream_t s) {
+    k_emit<float><<<grid, 256, 0, s>>>(sc, plan, seed, st, q);
+}
+void launch_bounce_f(const SceneView<float> &sc, uint64_t seed, PassState *st, int uc, int level, long long n_level0,
+                     RayQueue<float> in, RayQueue<float> out, unsigned long long qcap, PhotonBuf<float> photons,
+                     int grid, cudaStream_t s) {
+    k_bounce<float><<<grid, 256, 0, s>>>(sc, seed, st, uc, level, n_level0, in, out, qcap, photons);
 }
 void launch_bbox_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s) {
     k_bbox<float><<<grid, 256, 0, s>>>(buf, st, n_fixed);
@@ -21,14 +26,20 @@ void launch_scatter_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, co
                       const uint2 *keyrank, int grid, cudaStream_t s) {
     k_scatter<float><<<grid, 256, 0, s>>>(buf, st, n_fixed, start, keyrank);
 }
-void launch_eye_f(const SceneView<float> &sc, const DCamera<float> &cam, uint64_t seed, PassState *st, int uc,
-                  HitPoint<float> *hits, unsigned long long hit_cap, double *pass_img, int grid, cudaStream_t s) {
-    k_eye<float><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, hits, hit_cap, pass_img);
+void launch_eye_level_f(const SceneView<float> &sc, const DCamera<float> &cam, uint64_t seed, PassState *st, int uc,
+                        int level, EyeQueue<float> in, EyeQueue<float> out, unsigned long long qcap,
+                        HitPoint<float> *hits, EyeOut<float> pix, int grid, cudaStream_t s) {
+    k_eye_level<float><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
 }
 void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
                      const uint32_t *start, double pw, const double *q_r2, int pfilter, int mode, GatherOutF out,
                      int grid, cudaStream_t s) {
-    k_gather_f<<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pw, q_r2, pfilter, mode, out);
+    if (q_r2)
+        k_gather_f<false, true><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pw, q_r2, pfilter, mode, out);
+    else if (out.count)
+        k_gather_f<true, false><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pw, q_r2, pfilter, mode, out);
+    else
+        k_gather_f<false, false><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pw, q_r2, pfilter, mode, out);
 }
 void launch_within_f(const float *q, long long nq, const double *q_r2, const PassState *st, const float4 *smap,
                      const uint32_t *start, const int32_t *sidx, unsigned long long *counts,

@@ -6,9 +6,14 @@
 
 namespace ppm {
 
-void launch_trace_d(const SceneView<double> &sc, const EmitPlan &plan, uint64_t seed, PassState *st, int uc,
-                    PhotonBuf<double> out, unsigned long long cap, int grid, cudaStream_t s) {
-    k_trace_photons<double><<<grid, 256, 0, s>>>(sc, plan, seed, st, uc, out, cap);
+void launch_emit_d(const SceneView<double> &sc, const EmitPlan &plan, uint64_t seed, const PassState *st,
+                   RayQueue<double> q, int grid, cudaStream_t s) {
+    k_emit<double><<<grid, 256, 0, s>>>(sc, plan, seed, st, q);
+}
+void launch_bounce_d(const SceneView<double> &sc, uint64_t seed, PassState *st, int uc, int level, long long n_level0,
+                     RayQueue<double> in, RayQueue<double> out, unsigned long long qcap, PhotonBuf<double> photons,
+                     int grid, cudaStream_t s) {
+    k_bounce<double><<<grid, 256, 0, s>>>(sc, seed, st, uc, level, n_level0, in, out, qcap, photons);
 }
 void launch_bbox_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s) {
     k_bbox<double><<<grid, 256, 0, s>>>(buf, st, n_fixed);
@@ -21,9 +26,10 @@ void launch_scatter_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, c
                       const uint2 *keyrank, int grid, cudaStream_t s) {
     k_scatter<double><<<grid, 256, 0, s>>>(buf, st, n_fixed, start, keyrank);
 }
-void launch_eye_d(const SceneView<double> &sc, const DCamera<double> &cam, uint64_t seed, PassState *st, int uc,
-                  HitPoint<double> *hits, unsigned long long hit_cap, double *pass_img, int grid, cudaStream_t s) {
-    k_eye<double><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, hits, hit_cap, pass_img);
+void launch_eye_level_d(const SceneView<double> &sc, const DCamera<double> &cam, uint64_t seed, PassState *st, int uc,
+                        int level, EyeQueue<double> in, EyeQueue<double> out, unsigned long long qcap,
+                        HitPoint<double> *hits, EyeOut<double> pix, int grid, cudaStream_t s) {
+    k_eye_level<double><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
 }
 void launch_gather_d(const HitPoint<double> *hits, PassState *st, long long n_fixed, const double4 *spos,
                      const double4 *sdir, const uint32_t *start, double pw, int pfilter, int mode, GatherOutD out,

@@ -16,6 +16,10 @@ __global__ void k_pass_begin(PassState *st) {
     st->in_radius = 0;
     st->slots = 0;
     st->rows = 0;
+    for (int l = 0; l < MAX_TRACE + 2; l++) {
+        st->qn[l] = 0;
+        st->eq[l] = 0;
+    }
     for (int a = 0; a < 3; a++) {
         st->bb_lo[a] = ord_enc(1e300);
         st->bb_hi[a] = ord_enc(-1e300);
@@ -52,7 +56,7 @@ __global__ void k_grid_setup(PassState *st, double r2_override) {
             else dim[a] = (long long)f + 1;
             tot *= dim[a];
         }
-        if (ok && tot <= st->cell_cap) break;
+        if (ok && 3 * tot <= st->cell_cap) break;
         c *= 1.25;
         if (it == 399) { dim[0] = dim[1] = dim[2] = 1; c = 1e30; }
     }
@@ -69,13 +73,18 @@ __global__ void k_grid_setup(PassState *st, double r2_override) {
     int ext = ef >= 1.0 && ef <= 8.0 ? (int)ef : (ef > 8.0 ? 8 : 1);
     g.ext = ext < 1 ? 1 : (ext > 8 ? 8 : ext);
     g.ncell = dim[0] * dim[1] * dim[2];
+    g.nkeys = 3 * g.ncell;
+    g.r2f = (float)r2;
+    g.r2_lo = __double2float_rd(r2 * (1.0 - 1e-6));
+    g.r2_hi = __double2float_ru(r2 * (1.0 + 1e-6));
+    g.cellf = (float)c;
     st->grid = g;
 }
 
 // exclusive scan of count[0, ncell) into start[0, ncell], zeroing count
 // (reduce -> scan of tile sums -> downsweep; no inter-block waiting)
 __global__ void __launch_bounds__(256) k_scan_reduce(const uint32_t *count, const PassState *st, uint32_t *block_sums) {
-    const long long n = st->grid.ncell;
+    const long long n = st->grid.nkeys;
     const long long base = (long long)blockIdx.x * SCAN_TILE;
     if (base >= n) return;
     uint32_t s = 0;
@@ -96,7 +105,7 @@ __global__ void __launch_bounds__(256) k_scan_reduce(const uint32_t *count, cons
 }
 
 __global__ void __launch_bounds__(1024) k_scan_top(uint32_t *block_sums, const PassState *st) {
-    const long long n = st->grid.ncell;
+    const long long n = st->grid.nkeys;
     const int nb = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
     __shared__ uint32_t sh[1024];
     // each thread owns up to 4 consecutive tile sums
@@ -124,7 +133,7 @@ __global__ void __launch_bounds__(1024) k_scan_top(uint32_t *block_sums, const P
 
 __global__ void __launch_bounds__(256) k_scan_down(uint32_t *count, const PassState *st, const uint32_t *block_sums,
                                                    uint32_t *start) {
-    const long long n = st->grid.ncell;
+    const long long n = st->grid.nkeys;
     const long long base = (long long)blockIdx.x * SCAN_TILE;
     if (base >= n) return;
     constexpr int PER = SCAN_TILE / 256;   // 16 consecutive cells per thread
@@ -187,5 +196,22 @@ void launch_accum(const double *pass_img, double *sum, long long n, cudaStream_t
     k_accum<<<(unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096), 256, 0, s>>>(pass_img, sum, n);
 }
 void launch_pass_end(PassState *st, cudaStream_t s) { k_pass_end<<<1, 32, 0, s>>>(st); }
+
+// FP32 path: pass image = direct + gathered * pw / (pi r2) in FP64 (the flux
+// normalisation by the emitted photon count), added to the FP64 running sum
+__global__ void k_accum_mixed(const float *direct, const float *gathered, const PassState *st, double pw,
+                              double *pass_img, double *sum, long long n) {
+    const double kk = pw * (ONE_PI_D / st->r2);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double v = (double)direct[i] + (double)gathered[i] * kk;
+        pass_img[i] = v;
+        sum[i] += v;
+    }
+}
+void launch_accum_mixed(const float *direct, const float *gathered, const PassState *st, double pw, double *pass_img,
+                        double *sum, long long n, cudaStream_t s) {
+    k_accum_mixed<<<(unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096), 256, 0, s>>>(direct, gathered, st, pw,
+                                                                                             pass_img, sum, n);
+}
 
 }  // namespace ppm

@@ -50,6 +50,8 @@ struct ppm_ctx {
     DevBuf objs_d, mats_d, lights_d, objs_f, mats_f, lights_f;
     SceneView<double> sv_d{};
     SceneView<float> sv_f{};
+    const SceneView<double> &sv_of(double) const { return sv_d; }
+    const SceneView<float> &sv_of(float) const { return sv_f; }
     bool have_scene = false;
     ppm_camera cam{};
     DCamera<double> cam_d{};
@@ -60,9 +62,14 @@ struct ppm_ctx {
     PassState *st = nullptr;
     DevBuf raw_d, spos, sdir, raw_f, sorted_f, sidx, keyrank, count, start, block_sums;
     long long photon_cap_d = 0, photon_cap_f = 0;
+    DevBuf rq[4];                 // photon ray queues: level ping-pong A(a, b), B(a, b)
+    long long rq_cap = 0;         // entries per queue
+    DevBuf eqb[6];                // eye queues: A(a, b, c), B(a, b, c)
+    long long eq_cap = 0;
     DevBuf hits_d, hits_f;
     long long hit_cap = 0;
     DevBuf pass_img, sum_img;
+    DevBuf pass_direct32, pass_gather32;   // FP32 path per-pass buffers
     long long npx = 0;
     DevBuf scratch;   // parity entry-point staging
 
@@ -327,6 +334,49 @@ static int ensure_grid(ppm_ctx *ctx) {
 
 static int grid_blocks(ppm_ctx *ctx, int per_sm) { return ctx->sm_count * per_sm; }
 
+constexpr int EYE_QUEUE_PER_PIXEL = 2;   // eye-tree vertices per pixel a level may hold
+
+static int ensure_ray_queues(ppm_ctx *ctx, long long n, size_t vec_bytes) {
+    for (DevBuf &b : ctx->rq) TRY(ensure(ctx, b, vec_bytes * (size_t)std::max(1LL, n)));
+    ctx->rq_cap = std::max(1LL, n);
+    return PPM_OK;
+}
+
+static int ensure_eye_queues(ppm_ctx *ctx, long long npx, size_t vec_bytes) {
+    long long cap = std::max(1LL, npx * EYE_QUEUE_PER_PIXEL);
+    for (DevBuf &b : ctx->eqb) TRY(ensure(ctx, b, vec_bytes * (size_t)cap));
+    ctx->eq_cap = cap;
+    return PPM_OK;
+}
+
+// emission + MAX_TRACE bounce levels over ping-pong ray queues; returns kernels launched
+template <typename T, typename Emit, typename Bounce>
+static int enqueue_photon_trace(ppm_ctx *ctx, const EmitPlan &plan, uint64_t seed, int uc, PhotonBuf<T> pb,
+                                Emit emit, Bounce bounce, cudaStream_t s) {
+    using V = vec4_t<T>;
+    RayQueue<T> qa{as<V>(ctx->rq[0]), as<V>(ctx->rq[1])}, qb{as<V>(ctx->rq[2]), as<V>(ctx->rq[3])};
+    const long long n_emit = plan.first[plan.n_lights];
+    const long long blocks = (n_emit + 255) / 256;
+    const int g_emit = (int)std::max(1LL, std::min<long long>(blocks, (long long)ctx->sm_count * 8));
+    emit(ctx->sv_of(T()), plan, seed, ctx->st, qa, g_emit, s);
+    for (int l = 0; l < MAX_TRACE; l++)
+        bounce(ctx->sv_of(T()), seed, ctx->st, uc, l, n_emit, (l & 1) ? qb : qa, (l & 1) ? qa : qb,
+               (unsigned long long)ctx->rq_cap, pb, grid_blocks(ctx, 8), s);
+    return 1 + MAX_TRACE;
+}
+
+template <typename T, typename Level>
+static int enqueue_eye(ppm_ctx *ctx, HitPoint<T> *hits, Level level_fn, cudaStream_t s) {
+    using V = vec4_t<T>;
+    EyeQueue<T> qa{as<V>(ctx->eqb[0]), as<V>(ctx->eqb[1]), as<V>(ctx->eqb[2])};
+    EyeQueue<T> qb{as<V>(ctx->eqb[3]), as<V>(ctx->eqb[4]), as<V>(ctx->eqb[5])};
+    const int g0 = (int)std::max(1LL, std::min<long long>((ctx->npx + 127) / 128, (long long)ctx->sm_count * 16));
+    for (int l = 0; l < MAX_TRACE; l++)
+        level_fn(l, (l & 1) ? qb : qa, (l & 1) ? qa : qb, (unsigned long long)ctx->eq_cap, hits,
+                 l == 0 ? g0 : grid_blocks(ctx, 16), s);
+    return MAX_TRACE;
+}
+
 // ---------------------------------------------------------------------------
 // context
 // ---------------------------------------------------------------------------
@@ -392,8 +442,10 @@ extern "C" int ppm_ctx_destroy(ppm_ctx *ctx) {
     DevBuf *bufs[] = {&ctx->objs_d, &ctx->mats_d, &ctx->lights_d, &ctx->objs_f, &ctx->mats_f, &ctx->lights_f,
                       &ctx->raw_d, &ctx->spos, &ctx->sdir, &ctx->raw_f, &ctx->sorted_f, &ctx->sidx,
                       &ctx->keyrank, &ctx->count, &ctx->start, &ctx->block_sums, &ctx->hits_d, &ctx->hits_f,
-                      &ctx->pass_img, &ctx->sum_img, &ctx->scratch};
+                      &ctx->pass_img, &ctx->sum_img, &ctx->scratch, &ctx->pass_direct32, &ctx->pass_gather32};
     for (DevBuf *b : bufs) release(*b);
+    for (DevBuf &b : ctx->rq) release(b);
+    for (DevBuf &b : ctx->eqb) release(b);
     if (ctx->st) cudaFree(ctx->st);
     if (ctx->tev_made)
         for (int i = 0; i < TIMING_SLOTS; i++)
@@ -551,10 +603,11 @@ extern "C" int ppm_trace_photons(ppm_ctx *ctx, int64_t nphoton, int32_t use_clas
     if (nem > 0x7fffffffLL) return set_err(ctx, PPM_ERR_INVALID_ARG, "too many photons");
     long long cap = std::max(1LL, nem * MAX_TRACE);
     TRY(ensure_photons_d(ctx, cap));
+    TRY(ensure_ray_queues(ctx, nem, sizeof(double4)));
     TRY(upload_state(ctx, 0.0, (int)pass, 0.0, 1, 1.0, cap, 0));
+    launch_pass_begin(ctx->st, ctx->s);
     PhotonBuf<double> pb{as<PhotonD>(ctx->raw_d), as<double4>(ctx->spos), as<double4>(ctx->sdir)};
-    launch_trace_d(ctx->sv_d, plan, ctx->seed, ctx->st, use_classic ? 1 : 0, pb, (unsigned long long)cap,
-                   grid_blocks(ctx, 8), ctx->s);
+    enqueue_photon_trace<double>(ctx, plan, ctx->seed, use_classic ? 1 : 0, pb, launch_emit_d, launch_bounce_d, ctx->s);
     CK(cudaGetLastError());
     PassState h;
     TRY(read_state(ctx, h));
@@ -887,20 +940,26 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
     CK(cudaEventRecord(ctx->ev_fork, s));
     CK(cudaStreamWaitEvent(s2, ctx->ev_fork, 0));
     if (ev) CK(cudaEventRecord(ev[5], s2));
-    long long eye_grid = std::min<long long>((ctx->npx + 127) / 128, (long long)ctx->sm_count * 16);
     if (mixed)
-        launch_eye_f(ctx->sv_f, ctx->cam_f, ctx->cfg.seed, ctx->st, uc, as<HitPoint<float>>(ctx->hits_f),
-                     (unsigned long long)ctx->hit_cap, as<double>(ctx->pass_img), (int)eye_grid, s2);
+        kernels += enqueue_eye<float>(ctx, as<HitPoint<float>>(ctx->hits_f),
+            [&](int l, EyeQueue<float> in, EyeQueue<float> out, unsigned long long qcap, HitPoint<float> *h, int g,
+                cudaStream_t st) {
+                launch_eye_level_f(ctx->sv_f, ctx->cam_f, ctx->cfg.seed, ctx->st, uc, l, in, out, qcap, h,
+                                   EyeOut<float>{as<float>(ctx->pass_direct32), as<float>(ctx->pass_gather32)}, g, st);
+            }, s2);
     else
-        launch_eye_d(ctx->sv_d, ctx->cam_d, ctx->cfg.seed, ctx->st, uc, as<HitPoint<double>>(ctx->hits_d),
-                     (unsigned long long)ctx->hit_cap, as<double>(ctx->pass_img), (int)eye_grid, s2);
-    kernels++;
+        kernels += enqueue_eye<double>(ctx, as<HitPoint<double>>(ctx->hits_d),
+            [&](int l, EyeQueue<double> in, EyeQueue<double> out, unsigned long long qcap, HitPoint<double> *h, int g,
+                cudaStream_t st) {
+                launch_eye_level_d(ctx->sv_d, ctx->cam_d, ctx->cfg.seed, ctx->st, uc, l, in, out, qcap, h,
+                                   EyeOut<double>{as<double>(ctx->pass_img)}, g, st);
+            }, s2);
     if (ev) CK(cudaEventRecord(ev[6], s2));
     CK(cudaEventRecord(ctx->ev_join, s2));
     // photons
     if (mixed) {
         PhotonBuf<float> pb{as<float4>(ctx->raw_f), as<float4>(ctx->sorted_f), nullptr};
-        launch_trace_f(ctx->sv_f, ctx->plan, ctx->cfg.seed, ctx->st, uc, pb, (unsigned long long)ctx->photon_cap_f, g8, s);
+        kernels += enqueue_photon_trace<float>(ctx, ctx->plan, ctx->cfg.seed, uc, pb, launch_emit_f, launch_bounce_f, s);
         launch_bbox_f(pb, ctx->st, -1, g4, s);
         if (ev) CK(cudaEventRecord(ev[1], s));
         launch_grid_setup(ctx->st, -1.0, s);
@@ -909,7 +968,7 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
         launch_scatter_f(pb, ctx->st, -1, as<uint32_t>(ctx->start), as<uint2>(ctx->keyrank), g8, s);
     } else {
         PhotonBuf<double> pb{as<PhotonD>(ctx->raw_d), as<double4>(ctx->spos), as<double4>(ctx->sdir)};
-        launch_trace_d(ctx->sv_d, ctx->plan, ctx->cfg.seed, ctx->st, uc, pb, (unsigned long long)ctx->photon_cap_d, g8, s);
+        kernels += enqueue_photon_trace<double>(ctx, ctx->plan, ctx->cfg.seed, uc, pb, launch_emit_d, launch_bounce_d, s);
         launch_bbox_d(pb, ctx->st, -1, g4, s);
         if (ev) CK(cudaEventRecord(ev[1], s));
         launch_grid_setup(ctx->st, -1.0, s);
@@ -917,12 +976,12 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
         launch_scan(as<uint32_t>(ctx->count), ctx->st, as<uint32_t>(ctx->block_sums), as<uint32_t>(ctx->start), CELL_CAP, s);
         launch_scatter_d(pb, ctx->st, -1, as<uint32_t>(ctx->start), as<uint2>(ctx->keyrank), g8, s);
     }
-    kernels += 5 + kernels_per_scan();
+    kernels += 4 + kernels_per_scan();
     if (ev) CK(cudaEventRecord(ev[2], s));
     CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
     if (ev) CK(cudaEventRecord(ev[7], s));
     if (mixed) {
-        GatherOutF go{as<double>(ctx->pass_img), nullptr, ctx->count_gather ? &ctx->st->candidates : nullptr};
+        GatherOutF go{as<float>(ctx->pass_gather32), nullptr, ctx->count_gather ? &ctx->st->candidates : nullptr};
         launch_gather_f(as<HitPoint<float>>(ctx->hits_f), ctx->st, -1, as<float4>(ctx->sorted_f), as<uint32_t>(ctx->start),
                         ctx->pw, nullptr, ctx->cam.pfilter, 0, go, g8, s);
     } else {
@@ -932,7 +991,11 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
     }
     kernels++;
     if (ev) CK(cudaEventRecord(ev[3], s));
-    launch_accum(as<double>(ctx->pass_img), as<double>(ctx->sum_img), 3 * ctx->npx, s);
+    if (mixed)
+        launch_accum_mixed(as<float>(ctx->pass_direct32), as<float>(ctx->pass_gather32), ctx->st, ctx->pw,
+                           as<double>(ctx->pass_img), as<double>(ctx->sum_img), 3 * ctx->npx, s);
+    else
+        launch_accum(as<double>(ctx->pass_img), as<double>(ctx->sum_img), 3 * ctx->npx, s);
     launch_pass_end(ctx->st, s);
     kernels += 2;
     if (ev) CK(cudaEventRecord(ev[4], s));
@@ -969,11 +1032,19 @@ extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
     if (cfg->precision == PPM_PRECISION_MIXED) {
         TRY(ensure_photons_f(ctx, cap, false));
         TRY(ensure(ctx, ctx->hits_f, sizeof(HitPoint<float>) * ctx->hit_cap));
+        TRY(ensure_ray_queues(ctx, nem, sizeof(float4)));
+        TRY(ensure_eye_queues(ctx, ctx->npx, sizeof(float4)));
     } else {
         TRY(ensure_photons_d(ctx, cap));
         TRY(ensure(ctx, ctx->hits_d, sizeof(HitPoint<double>) * ctx->hit_cap));
+        TRY(ensure_ray_queues(ctx, nem, sizeof(double4)));
+        TRY(ensure_eye_queues(ctx, ctx->npx, sizeof(double4)));
     }
     TRY(ensure(ctx, ctx->pass_img, sizeof(double) * 3 * ctx->npx));
+    if (cfg->precision == PPM_PRECISION_MIXED) {
+        TRY(ensure(ctx, ctx->pass_direct32, sizeof(float) * 3 * ctx->npx));
+        TRY(ensure(ctx, ctx->pass_gather32, sizeof(float) * 3 * ctx->npx));
+    }
     TRY(ensure(ctx, ctx->sum_img, sizeof(double) * 3 * ctx->npx));
     CK(cudaMemsetAsync(ctx->sum_img.p, 0, sizeof(double) * 3 * ctx->npx, ctx->s));
     CK(cudaMemsetAsync(ctx->pass_img.p, 0, sizeof(double) * 3 * ctx->npx, ctx->s));

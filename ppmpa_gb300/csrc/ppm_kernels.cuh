@@ -20,6 +20,9 @@ namespace ppm {
 // ---------------------------------------------------------------------------
 // shared device state
 // ---------------------------------------------------------------------------
+// Photons are counting-sorted by key = 3 * cell + wavelength: the photons of
+// a cell row are contiguous, and inside each cell they are grouped by
+// wavelength (so a warp's flux updates mostly go to one channel).
 struct GridParams {
     double org[3];
     double cell, inv;
@@ -28,6 +31,9 @@ struct GridParams {
     int32_t dim[3];
     int32_t ext;
     int64_t ncell;
+    int64_t nkeys;            // 3 * ncell
+    float r2f, r2_lo, r2_hi;  // pass radius^2 in FP32 and its rounding band
+    float cellf;              // cell size in FP32
 };
 
 struct PassState {
@@ -47,6 +53,8 @@ struct PassState {
     int64_t cell_cap;
     unsigned long long photon_cap;   // buffers hold at most this many photons
     unsigned long long hit_cap;      // and this many hit points
+    unsigned long long qn[MAX_TRACE + 2];   // photon rays alive at each bounce level
+    unsigned long long eq[MAX_TRACE + 2];   // eye-tree vertices at each depth
 };
 
 // number of valid photons / hit points (the counters keep counting past the
@@ -139,6 +147,7 @@ template <> struct PhotonBuf<double> {
         raw[i] = r;
     }
     __device__ __forceinline__ V3<double> raw_pos(unsigned long long i) const { return ld3(raw[i].pos); }
+    __device__ __forceinline__ int raw_wl(unsigned long long i) const { return raw[i].wl; }
 };
 template <> struct PhotonBuf<float> {
     float4 *raw;           // unsorted: x, y, z, oct(dir) | wl
@@ -151,6 +160,7 @@ template <> struct PhotonBuf<float> {
         float4 r = raw[i];
         return mk3(r.x, r.y, r.z);
     }
+    __device__ __forceinline__ int raw_wl(unsigned long long i) const { return (int)(__float_as_uint(raw[i].w) >> 30); }
 };
 
 template <typename T>
@@ -162,38 +172,84 @@ struct HitPoint {
 };
 
 // ---------------------------------------------------------------------------
-// photon emission + tracing
+// wavefront queues: two 4-wide vectors per entry (xyz + a 32-bit tag each)
+// ---------------------------------------------------------------------------
+template <typename T> struct Vec4T;
+template <> struct Vec4T<float> { using type = float4; };
+template <> struct Vec4T<double> { using type = double4; };
+template <typename T> using vec4_t = typename Vec4T<T>::type;
+
+__device__ __forceinline__ float4 mk4(V3<float> v, uint32_t w) { return make_float4(v.x, v.y, v.z, __uint_as_float(w)); }
+__device__ __forceinline__ double4 mk4(V3<double> v, uint32_t w) {
+    return make_double4(v.x, v.y, v.z, __longlong_as_double((long long)w));
+}
+__device__ __forceinline__ V3<float> xyz(float4 v) { return mk3(v.x, v.y, v.z); }
+__device__ __forceinline__ V3<double> xyz(double4 v) { return mk3(v.x, v.y, v.z); }
+__device__ __forceinline__ uint32_t tag(float4 v) { return __float_as_uint(v.w); }
+__device__ __forceinline__ uint32_t tag(double4 v) { return (uint32_t)__double_as_longlong(v.w); }
+
+// photon ray queue: a = (pos, emission index), b = (dir, wl | (medium+1) << 8)
+template <typename T>
+struct RayQueue {
+    vec4_t<T> *a;
+    vec4_t<T> *b;
+};
+
+// ---------------------------------------------------------------------------
+// photon emission (light.rs:67-91; per-light counts of ppmpa.rs:30-31)
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(256) k_trace_photons(SceneView<T> sc, EmitPlan plan, uint64_t seed, PassState *st,
-                                                       int uc, PhotonBuf<T> out, unsigned long long cap) {
+__global__ void __launch_bounds__(256) k_emit(SceneView<T> sc, EmitPlan plan, uint64_t seed, const PassState *st,
+                                              RayQueue<T> q) {
     const uint32_t pass = (uint32_t)st->pass;
     const int64_t n_emit = plan.first[plan.n_lights];
-    int64_t next = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    PhotonPath<T> ph;
-    bool alive = false;
-    while (alive || next < n_emit) {
-        if (!alive) {
-            int li = 0;
-            while (li < plan.n_lights - 1 && next >= plan.first[li + 1]) li++;
-            ph.item = (uint32_t)next;
-            Rng rg;
-            rg.init(seed, ph.item, pass, TAG_EMIT);
-            generate_photon(sc.lights[li], rg, ph);
-            next += stride;
-            alive = true;
-        }
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_emit; i += (int64_t)gridDim.x * blockDim.x) {
+        int li = 0;
+        while (li < plan.n_lights - 1 && i >= plan.first[li + 1]) li++;
+        PhotonPath<T> ph;
+        Rng rg;
+        rg.init(seed, (uint32_t)i, pass, TAG_EMIT);
+        generate_photon(sc.lights[li], rg, ph);
+        q.a[i] = mk4(ph.pos, (uint32_t)i);
+        q.b[i] = mk4(ph.dir, (uint32_t)ph.wl);
+    }
+}
+
+// one bounce level of trace_photon (tracer.rs:31-125) for every live ray;
+// continuing rays are compacted into the next level's queue
+template <typename T>
+__global__ void __launch_bounds__(256) k_bounce(SceneView<T> sc, uint64_t seed, PassState *st, int uc, int level,
+                                                long long n_level0, RayQueue<T> in, RayQueue<T> out,
+                                                unsigned long long qcap, PhotonBuf<T> photons) {
+    const uint32_t pass = (uint32_t)st->pass;
+    unsigned long long n = level == 0 ? (unsigned long long)n_level0 : st->qn[level];
+    if (n > qcap) n = qcap;
+    const unsigned long long pcap = st->photon_cap;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const vec4_t<T> a = in.a[i], b = in.b[i];
+        PhotonPath<T> ph;
+        ph.pos = xyz(a);
+        ph.dir = xyz(b);
+        ph.item = tag(a);
+        const uint32_t meta = tag(b);
+        ph.wl = (int)(meta & 3u);
+        ph.medium = (int)(meta >> 8) - 1;
+        ph.level = level;
+        const PhotonPath<T> cur = ph;
         bool store;
         V3<T> spos;
-        const int lvl = ph.level;
-        PhotonPath<T> cur = ph;
-        alive = photon_event(sc, seed, pass, uc != 0, ph, store, spos);
+        const bool alive = photon_event(sc, seed, pass, uc != 0, ph, store, spos);
         if (store) {
             unsigned long long slot = agg_append(&st->n_stored);
-            if (slot < cap) {
-                cur.level = lvl;
-                out.write(slot, cur, spos);
+            if (slot < pcap) photons.write(slot, cur, spos);
+            else atomicOr(&st->overflow, 1u);
+        }
+        if (alive) {
+            unsigned long long o = agg_append(&st->qn[level + 1]);
+            if (o < qcap) {
+                out.a[o] = mk4(ph.pos, ph.item);
+                out.b[o] = mk4(ph.dir, (uint32_t)ph.wl | ((uint32_t)(ph.medium + 1) << 8));
             } else {
                 atomicOr(&st->overflow, 1u);
             }
@@ -205,33 +261,41 @@ __global__ void __launch_bounds__(256) k_trace_photons(SceneView<T> sc, EmitPlan
 template <typename T>
 __global__ void __launch_bounds__(256) k_bbox(PhotonBuf<T> buf, PassState *st, long long n_fixed) {
     unsigned long long n = n_photons(st, n_fixed);
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    // reduced in the photons' own precision; converted once per block
+    T lo[3] = {T(1e30), T(1e30), T(1e30)}, hi[3] = {T(-1e30), T(-1e30), T(-1e30)};
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
         V3<T> p = buf.raw_pos(i);
-        double v[3] = {(double)p.x, (double)p.y, (double)p.z};
+        T v[3] = {p.x, p.y, p.z};
 #pragma unroll
         for (int a = 0; a < 3; a++) {
-            if (isfinite(v[a]) && fabs(v[a]) < 1e30) { lo[a] = fmin(lo[a], v[a]); hi[a] = fmax(hi[a], v[a]); }
+            if (v[a] > T(-1e30) && v[a] < T(1e30)) {   // finite and bounded (false for NaN)
+                lo[a] = v[a] < lo[a] ? v[a] : lo[a];
+                hi[a] = v[a] > hi[a] ? v[a] : hi[a];
+            }
         }
     }
-    __shared__ double slo[3][8], shi[3][8];
+    __shared__ T slo[3][8], shi[3][8];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         for (int o = 16; o > 0; o >>= 1) {
-            lo[a] = fmin(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
-            hi[a] = fmax(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+            T ol = __shfl_xor_sync(0xffffffffu, lo[a], o), oh = __shfl_xor_sync(0xffffffffu, hi[a], o);
+            lo[a] = ol < lo[a] ? ol : lo[a];
+            hi[a] = oh > hi[a] ? oh : hi[a];
         }
         if (lane_id() == 0) { slo[a][threadIdx.x >> 5] = lo[a]; shi[a][threadIdx.x >> 5] = hi[a]; }
     }
     __syncthreads();
     if (threadIdx.x < 3) {
         int a = threadIdx.x;
-        double l = slo[a][0], h = shi[a][0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); w++) { l = fmin(l, slo[a][w]); h = fmax(h, shi[a][w]); }
+        T l = slo[a][0], h = shi[a][0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+            l = slo[a][w] < l ? slo[a][w] : l;
+            h = shi[a][w] > h ? shi[a][w] : h;
+        }
         if (l <= h) {
-            atomicMin(&st->bb_lo[a], ord_enc(l));
-            atomicMax(&st->bb_hi[a], ord_enc(h));
+            atomicMin(&st->bb_lo[a], ord_enc((double)l));
+            atomicMax(&st->bb_hi[a], ord_enc((double)h));
         }
     }
 }
@@ -266,7 +330,7 @@ __global__ void __launch_bounds__(256) k_cell_hist(PhotonBuf<T> buf, PassState *
     const GridParams g = st->grid;
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
-        uint32_t c = cell_of(g, buf.raw_pos(i));
+        uint32_t c = 3u * cell_of(g, buf.raw_pos(i)) + (uint32_t)buf.raw_wl(i);
         uint32_t r = atomicAdd(&count[c], 1u);
         keyrank[i] = make_uint2(c, r);
     }
@@ -311,61 +375,102 @@ __global__ void __launch_bounds__(256) k_scatter<float>(PhotonBuf<float> buf, Pa
 
 // ---------------------------------------------------------------------------
 // eye pass: camera rays (camera.rs:58-75) and the eye tree (tracer.rs:129-177)
+// evaluated level by level.  Every vertex carries the product of the bsdf
+// weights on its path (the bsdf is linear in di, si, ti, surface.rs:135-206),
+// adds throughput x (emittance/2pi + c_di x direct light) to its pixel and
+// appends a hit point with weight throughput x c_di for the photon estimate;
+// its reflected and refracted children go to the next level's queue.
+// Queue entry: a = (pos, pixel), b = (dir, node | (medium+1) << 16), c = (w, 0).
 // ---------------------------------------------------------------------------
 template <typename T>
-struct EyeEntry {
-    V3<T> pos, dir, w;
-    int16_t medium;
-    int16_t level;
-    uint32_t node;
+struct EyeQueue {
+    vec4_t<T> *a, *b, *c;
 };
 
-constexpr int EYE_STACK = 12;
+// Pixel output of the eye pass.  FP64 path: the pass image itself.  FP32
+// path: the per-pass direct-light buffer (FP32), and level 0 also clears the
+// per-pass gathered-flux buffer of its pixel.
+template <typename T> struct EyeOut;
+template <> struct EyeOut<double> {
+    double *img;
+    __device__ __forceinline__ void set(uint32_t p, V3<double> v) const {
+        img[3 * (size_t)p] = v.x; img[3 * (size_t)p + 1] = v.y; img[3 * (size_t)p + 2] = v.z;
+    }
+    __device__ __forceinline__ void add(uint32_t p, V3<double> v) const {
+        atomicAdd(img + 3 * (size_t)p, v.x); atomicAdd(img + 3 * (size_t)p + 1, v.y); atomicAdd(img + 3 * (size_t)p + 2, v.z);
+    }
+};
+template <> struct EyeOut<float> {
+    float *direct;
+    float *gathered;
+    __device__ __forceinline__ void set(uint32_t p, V3<float> v) const {
+        direct[3 * (size_t)p] = v.x; direct[3 * (size_t)p + 1] = v.y; direct[3 * (size_t)p + 2] = v.z;
+        gathered[3 * (size_t)p] = 0.f; gathered[3 * (size_t)p + 1] = 0.f; gathered[3 * (size_t)p + 2] = 0.f;
+    }
+    __device__ __forceinline__ void add(uint32_t p, V3<float> v) const {
+        atomicAdd(direct + 3 * (size_t)p, v.x); atomicAdd(direct + 3 * (size_t)p + 1, v.y);
+        atomicAdd(direct + 3 * (size_t)p + 2, v.z);
+    }
+};
 
 template <typename T>
-__global__ void __launch_bounds__(128) k_eye(SceneView<T> sc, DCamera<T> cam, uint64_t seed, PassState *st, int uc,
-                                             HitPoint<T> *hits, unsigned long long hit_cap, double *pass_img) {
+__global__ void __launch_bounds__(128) k_eye_level(SceneView<T> sc, DCamera<T> cam, uint64_t seed, PassState *st,
+                                                   int uc, int level, EyeQueue<T> in, EyeQueue<T> out,
+                                                   unsigned long long qcap, HitPoint<T> *hits, EyeOut<T> pix) {
     const uint32_t pass = (uint32_t)st->pass;
-    const int64_t npx = (int64_t)cam.xreso * cam.yreso;
+    const unsigned long long hit_cap = st->hit_cap;
+    const long long npx = (long long)cam.xreso * cam.yreso;
+    unsigned long long n = level == 0 ? (unsigned long long)npx : st->eq[level];
+    if (level > 0 && n > qcap) n = qcap;
     const T air[3] = {T(1), T(1), T(1)};
-    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < npx; p += (int64_t)gridDim.x * blockDim.x) {
-        const T y = (T)(p / cam.xreso), x = (T)(p % cam.xreso);
-        Rng rg;
-        rg.init(seed, (uint32_t)p, pass, TAG_CAMERA);
-        V3<T> blur = mk3(T(0), T(0), T(0));
-        if (cam.blur) {
-            T r1 = gen_range<T>(rg, T(-0.5), T(0.5));
-            T r2 = gen_range<T>(rg, T(-0.5), T(0.5));
-            blur = r1 * ld3(cam.eex) + r2 * ld3(cam.eey);
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        V3<T> rp, rd, w;
+        uint32_t p, node;
+        int medium;
+        if (level == 0) {
+            p = (uint32_t)i;
+            const T y = (T)(p / (uint32_t)cam.xreso), x = (T)(p % (uint32_t)cam.xreso);
+            Rng rg;
+            rg.init(seed, p, pass, TAG_CAMERA);
+            V3<T> blur = mk3(T(0), T(0), T(0));
+            if (cam.blur) {
+                T r1 = gen_range<T>(rg, T(-0.5), T(0.5));
+                T r2 = gen_range<T>(rg, T(-0.5), T(0.5));
+                blur = r1 * ld3(cam.eex) + r2 * ld3(cam.eey);
+            }
+            T r3 = T(0), r4 = T(0);
+            if (cam.jitter_aa) {
+                r3 = gen_range<T>(rg, T(-0.5), T(0.5));
+                r4 = gen_range<T>(rg, T(-0.5), T(0.5));
+            }
+            rp = ld3(cam.eye) + blur;
+            V3<T> ed = ((ld3(cam.origin) + (x + r3) * ld3(cam.esx)) + (y + r4) * ld3(cam.esy)) - blur;
+            rd = ed;
+            normalize(ed, rd);
+            w = mk3(T(1), T(1), T(1));
+            node = 1u;
+            medium = -1;
+        } else {
+            const vec4_t<T> a = in.a[i], b = in.b[i], c = in.c[i];
+            rp = xyz(a);
+            p = tag(a);
+            rd = xyz(b);
+            node = tag(b) & 0xffffu;
+            medium = (int)(tag(b) >> 16) - 1;
+            w = xyz(c);
         }
-        T r3 = T(0), r4 = T(0);
-        if (cam.jitter_aa) {
-            r3 = gen_range<T>(rg, T(-0.5), T(0.5));
-            r4 = gen_range<T>(rg, T(-0.5), T(0.5));
-        }
-        EyeEntry<T> stack[EYE_STACK];
-        int sp = 0;
-        stack[0].pos = ld3(cam.eye) + blur;
-        V3<T> ed = ((ld3(cam.origin) + (x + r3) * ld3(cam.esx)) + (y + r4) * ld3(cam.esy)) - blur;
-        stack[0].dir = ed;
-        normalize(ed, stack[0].dir);
-        stack[0].w = mk3(T(1), T(1), T(1));
-        stack[0].medium = -1;
-        stack[0].level = 0;
-        stack[0].node = 1u;
-        sp = 1;
         V3<T> acc = mk3(T(0), T(0), T(0));
-        while (sp > 0) {
-            EyeEntry<T> e = stack[--sp];
-            Isect<T> is;
-            if (!intersect(sc, e.pos, e.dir, is)) continue;
+        Isect<T> is;
+        if (intersect(sc, rp, rd, is)) {
             const int mid = sc.objs[is.obj].mat;
             const DMaterial<T> &mate = sc.mats[mid];
-            acc = acc + hmul(e.w, ld3(mate.emit)) * Cst<T>::sr_half();
+            acc = hmul(w, ld3(mate.emit)) * Cst<T>::sr_half();
             Coef<T> cf;
             V3<T> rdir = is.n, td = is.n;
             T cos1;
-            bool has_t = false, diffuse_only = mate.surface == SF_SIMPLE && mate.scatter == T(1);
+            bool has_t = false;
+            const bool diffuse_only = mate.surface == SF_SIMPLE && mate.scatter == T(1);
             if (diffuse_only) {
                 // Simple surface with diffuseness 1: no reflected child, the
                 // refracted child has weight 0 and c_di does not depend on cos
@@ -373,18 +478,18 @@ __global__ void __launch_bounds__(128) k_eye(SceneView<T> sc, DCamera<T> cam, ui
                 cos1 = T(0);
             } else {
                 T cos2;
-                V3<T> rdir0 = specular_reflection(is.n, e.dir, cos1);
+                V3<T> rdir0 = specular_reflection(is.n, rd, cos1);
                 Rng rv;
-                rv.init(seed, (uint32_t)p, pass, TAG_EYE | e.node);
+                rv.init(seed, p, pass, TAG_EYE | node);
                 rdir = reflection_glossy(rv, is.n, rdir0, sf_power_glossy(mate));
-                T eta = relative_ior_average(ior_of(sc, e.medium, air), mate.ior);
+                T eta = relative_ior_average(ior_of(sc, medium, air), mate.ior);
                 V3<T> hvec = is.n;
-                if (!normalize(rdir - e.dir, hvec)) hvec = is.n;
-                has_t = specular_refraction(hvec, e.dir, eta, td, cos2);
+                if (!normalize(rdir - rd, hvec)) hvec = is.n;
+                has_t = specular_refraction(hvec, rd, eta, td, cos2);
                 T cos = cos1 < cos2 ? cos1 : cos2;
                 cf = bsdf_coef(mate, cos);
             }
-            V3<T> W = hmul(e.w, cf.di);
+            const V3<T> W = hmul(w, cf.di);
             if (any_nz(W)) {
                 if (uc) {
                     V3<T> di = mk3(T(0), T(0), T(0));
@@ -403,35 +508,33 @@ __global__ void __launch_bounds__(128) k_eye(SceneView<T> sc, DCamera<T> cam, ui
                     atomicOr(&st->overflow, 2u);
                 }
             }
-            if (diffuse_only || e.level + 1 >= MAX_TRACE) continue;
-            V3<T> wt = hmul(e.w, cf.ti);
-            if (has_t && sf_refract(mate, cos1) && any_nz(wt)) {
-                if (sp < EYE_STACK) {
-                    EyeEntry<T> c;
-                    c.pos = is.pos; c.dir = td; c.w = wt;
-                    c.medium = (int16_t)(is.in ? mid : -1);
-                    c.level = (int16_t)(e.level + 1); c.node = 2u * e.node + 1u;
-                    stack[sp++] = c;
-                } else {
-                    atomicOr(&st->overflow, 4u);
+            if (!diffuse_only && level + 1 < MAX_TRACE) {
+                const V3<T> ws = hmul(w, cf.si);
+                if (sf_reflect(mate, cos1) && any_nz(ws)) {
+                    unsigned long long o = agg_append(&st->eq[level + 1]);
+                    if (o < qcap) {
+                        out.a[o] = mk4(is.pos, p);
+                        out.b[o] = mk4(rdir, (2u * node) | ((uint32_t)(medium + 1) << 16));
+                        out.c[o] = mk4(ws, 0u);
+                    } else {
+                        atomicOr(&st->overflow, 4u);
+                    }
                 }
-            }
-            V3<T> ws = hmul(e.w, cf.si);
-            if (sf_reflect(mate, cos1) && any_nz(ws)) {
-                if (sp < EYE_STACK) {
-                    EyeEntry<T> c;
-                    c.pos = is.pos; c.dir = rdir; c.w = ws;
-                    c.medium = e.medium;
-                    c.level = (int16_t)(e.level + 1); c.node = 2u * e.node;
-                    stack[sp++] = c;
-                } else {
-                    atomicOr(&st->overflow, 4u);
+                const V3<T> wt = hmul(w, cf.ti);
+                if (has_t && sf_refract(mate, cos1) && any_nz(wt)) {
+                    unsigned long long o = agg_append(&st->eq[level + 1]);
+                    if (o < qcap) {
+                        out.a[o] = mk4(is.pos, p);
+                        out.b[o] = mk4(td, (2u * node + 1u) | ((uint32_t)((is.in ? mid : -1) + 1) << 16));
+                        out.c[o] = mk4(wt, 0u);
+                    } else {
+                        atomicOr(&st->overflow, 4u);
+                    }
                 }
             }
         }
-        pass_img[3 * p] = (double)acc.x;
-        pass_img[3 * p + 1] = (double)acc.y;
-        pass_img[3 * p + 2] = (double)acc.z;
+        if (level == 0) pix.set(p, acc);
+        else if (any_nz(acc)) pix.add(p, acc);
     }
 }
 
@@ -469,7 +572,7 @@ template <typename T> struct RowCull;
 template <> struct RowCull<float> {
     __device__ static __forceinline__ bool range(const GridParams &g, V3<float> q, float r2, int yy, int zz,
                                                  int lo_x, int hi_x, int &x0, int &x1) {
-        const float c = (float)g.cell, m = 4e-3f * c;
+        const float c = g.cellf, m = 4e-3f * c;
         const float ylo = g.orgf[1] + (float)yy * c, zlo = g.orgf[2] + (float)zz * c;
         const float dy = fmaxf(0.0f, fmaxf(ylo - q.y, q.y - (ylo + c)) - m);
         const float dz = fmaxf(0.0f, fmaxf(zlo - q.z, q.z - (zlo + c)) - m);
@@ -516,8 +619,8 @@ __device__ __forceinline__ RowSet make_rows(const GridParams &g, const uint32_t 
         int yy = lo[1] + (row - zi * ny), zz = lo[2] + zi;
         if (RowCull<T>::range(g, q, r2, yy, zz, lo[0], hi[0], x0, x1)) {
             int base = (zz * g.dim[1] + yy) * g.dim[0];
-            rs.begin = start[base + x0];
-            rs.len = start[base + x1 + 1] - rs.begin;
+            rs.begin = start[3 * (base + x0)];
+            rs.len = start[3 * (base + x1 + 1)] - rs.begin;
         }
     }
     rs.nonempty = __ballot_sync(0xffffffffu, rs.len > 0);
@@ -651,6 +754,13 @@ struct Kahan {
     }
 };
 
+// pairwise (tree) sum of the lanes' compensated partial sums
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 // compensated pairwise combination (two-sum) across the warp
 __device__ __forceinline__ float warp_sum_comp(Kahan k) {
     float s = k.s, c = -k.c;
@@ -690,12 +800,14 @@ __device__ __forceinline__ float filter_wt_f(int pfilter, float d, float r2) {
 }
 
 struct GatherOutF {
-    double *pass_img;
-    double *out_rgb;
+    float *gathered;     // render: per-pass gathered flux W * sum (normalised later in FP64)
+    double *out_rgb;     // estimate entry: per-query radiance
     unsigned long long *count;
 };
 
 #if defined(PPM_BUILD_F32)
+// PERQ: per-query radii (the estimate entry point); otherwise the pass radius
+template <bool COUNT, bool PERQ>
 __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed,
                                                   const float4 *smap, const uint32_t *start, double pw,
                                                   const double *q_r2, int pfilter, int mode, GatherOutF out) {
@@ -706,19 +818,28 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
     const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
     for (unsigned long long qi = warp; qi < nq; qi += nwarps) {
         const HitPoint<float> h = hits[qi];
-        const double r2 = q_r2 ? q_r2[qi] : st->r2;
-        const float r2_lo = __double2float_rd(r2 * (1.0 - 1e-6));
-        const float r2_hi = __double2float_ru(r2 * (1.0 + 1e-6));
-        const float r2f = (float)r2;
+        double r2;
+        float r2_lo, r2_hi, r2f;
         int ext = g.ext;
-        if (q_r2) ext = min(g.ext, max(1, (int)ceil(sqrt(r2) * g.inv + 3e-3)));
+        if constexpr (PERQ) {
+            r2 = q_r2[qi];
+            r2_lo = __double2float_rd(r2 * (1.0 - 1e-6));
+            r2_hi = __double2float_ru(r2 * (1.0 + 1e-6));
+            r2f = (float)r2;
+            ext = min(g.ext, max(1, (int)ceil(sqrt(r2) * g.inv + 3e-3)));
+        } else {
+            r2 = st->r2;
+            r2_lo = g.r2_lo;
+            r2_hi = g.r2_hi;
+            r2f = g.r2f;
+        }
         V3<float> q = ld3(h.pos), n = ld3(h.nrm);
         int c[3], lo[3], hi[3];
         query_cells(g, q, ext, c, lo, hi);
         Kahan k0 = {0.f, 0.f}, k1 = {0.f, 0.f}, k2 = {0.f, 0.f};
         unsigned long long c_slots = 0, c_valid = 0, c_hits = 0;
         for_each_candidate(g, start, q, r2f, lo, hi, [&](uint32_t idx, bool valid) {
-            if (out.count) {
+            if (COUNT) {
                 c_slots += 1;
                 c_valid += valid;
             }
@@ -731,15 +852,15 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
                 float cos0 = dot(n, pd);
                 float val = cos0 < 0.0f ? -cos0 : 0.0f;
                 if (pfilter != PF_NONE) val *= filter_wt_f(pfilter, d2f, r2f);
-                int wl = (int)(m >> 30);
-                k0.add(wl == 0 ? val : 0.0f);
-                k1.add(wl == 1 ? val : 0.0f);
-                k2.add(wl == 2 ? val : 0.0f);
-                if (out.count) c_hits += 1;
+                const uint32_t wl = m >> 30;   // photons of a cell are grouped by wavelength
+                if (wl == 0u) k0.add(val);
+                else if (wl == 1u) k1.add(val);
+                else k2.add(val);
+                if (COUNT) c_hits += 1;
             }
         });
-        float s0 = warp_sum_comp(k0), s1 = warp_sum_comp(k1), s2 = warp_sum_comp(k2);
-        if (out.count) {
+        float s0 = warp_sum(k0.s - k0.c), s1 = warp_sum(k1.s - k1.c), s2 = warp_sum(k2.s - k2.c);
+        if (COUNT) {
             for (int o = 16; o > 0; o >>= 1) {
                 c_slots += __shfl_xor_sync(0xffffffffu, c_slots, o);
                 c_valid += __shfl_xor_sync(0xffffffffu, c_valid, o);
@@ -752,13 +873,15 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
             }
         }
         if (lane == 0) {
-            double kk = pw * (ONE_PI_D / r2);
             if (mode == 0) {
-                double *px = out.pass_img + 3 * (long long)h.pixel;
-                atomicAdd(px, (double)h.w[0] * ((double)s0 * kk));
-                atomicAdd(px + 1, (double)h.w[1] * ((double)s1 * kk));
-                atomicAdd(px + 2, (double)h.w[2] * ((double)s2 * kk));
+                // FP32 only here: an FP64 instruction costs a warp-wide slot of
+                // the narrow FP64 pipe even with one active lane
+                float *px = out.gathered + 3 * (size_t)h.pixel;
+                atomicAdd(px, h.w[0] * s0);
+                atomicAdd(px + 1, h.w[1] * s1);
+                atomicAdd(px + 2, h.w[2] * s2);
             } else {
+                double kk = pw * (ONE_PI_D / r2);
                 out.out_rgb[3 * qi] = (double)s0 * kk;
                 out.out_rgb[3 * qi + 1] = (double)s1 * kk;
                 out.out_rgb[3 * qi + 2] = (double)s2 * kk;

@@ -8,15 +8,19 @@
 namespace ppm {
 
 // ---- FP64 path -------------------------------------------------------------
-void launch_trace_d(const SceneView<double> &sc, const EmitPlan &plan, uint64_t seed, PassState *st, int uc,
-                    PhotonBuf<double> out, unsigned long long cap, int grid, cudaStream_t s);
+void launch_emit_d(const SceneView<double> &sc, const EmitPlan &plan, uint64_t seed, const PassState *st,
+                   RayQueue<double> q, int grid, cudaStream_t s);
+void launch_bounce_d(const SceneView<double> &sc, uint64_t seed, PassState *st, int uc, int level, long long n_level0,
+                     RayQueue<double> in, RayQueue<double> out, unsigned long long qcap, PhotonBuf<double> photons,
+                     int grid, cudaStream_t s);
 void launch_bbox_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s);
 void launch_hist_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, uint32_t *count, uint2 *keyrank, int grid,
                    cudaStream_t s);
 void launch_scatter_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, const uint32_t *start,
                       const uint2 *keyrank, int grid, cudaStream_t s);
-void launch_eye_d(const SceneView<double> &sc, const DCamera<double> &cam, uint64_t seed, PassState *st, int uc,
-                  HitPoint<double> *hits, unsigned long long hit_cap, double *pass_img, int grid, cudaStream_t s);
+void launch_eye_level_d(const SceneView<double> &sc, const DCamera<double> &cam, uint64_t seed, PassState *st, int uc,
+                        int level, EyeQueue<double> in, EyeQueue<double> out, unsigned long long qcap,
+                        HitPoint<double> *hits, EyeOut<double> pix, int grid, cudaStream_t s);
 void launch_gather_d(const HitPoint<double> *hits, PassState *st, long long n_fixed, const double4 *spos,
                      const double4 *sdir, const uint32_t *start, double pw, int pfilter, int mode, GatherOutD out,
                      int grid, cudaStream_t s);
@@ -28,15 +32,19 @@ void launch_intersect_d(const SceneView<double> &sc, const double *rays, long lo
                         double *nrm, cudaStream_t s);
 
 // ---- FP32 mixed path ---------------------------------------------------------
-void launch_trace_f(const SceneView<float> &sc, const EmitPlan &plan, uint64_t seed, PassState *st, int uc,
-                    PhotonBuf<float> out, unsigned long long cap, int grid, cudaStream_t s);
+void launch_emit_f(const SceneView<float> &sc, const EmitPlan &plan, uint64_t seed, const PassState *st,
+                   RayQueue<float> q, int grid, cudaStream_t s);
+void launch_bounce_f(const SceneView<float> &sc, uint64_t seed, PassState *st, int uc, int level, long long n_level0,
+                     RayQueue<float> in, RayQueue<float> out, unsigned long long qcap, PhotonBuf<float> photons,
+                     int grid, cudaStream_t s);
 void launch_bbox_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s);
 void launch_hist_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, uint32_t *count, uint2 *keyrank, int grid,
                    cudaStream_t s);
 void launch_scatter_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, const uint32_t *start,
                       const uint2 *keyrank, int grid, cudaStream_t s);
-void launch_eye_f(const SceneView<float> &sc, const DCamera<float> &cam, uint64_t seed, PassState *st, int uc,
-                  HitPoint<float> *hits, unsigned long long hit_cap, double *pass_img, int grid, cudaStream_t s);
+void launch_eye_level_f(const SceneView<float> &sc, const DCamera<float> &cam, uint64_t seed, PassState *st, int uc,
+                        int level, EyeQueue<float> in, EyeQueue<float> out, unsigned long long qcap,
+                        HitPoint<float> *hits, EyeOut<float> pix, int grid, cudaStream_t s);
 void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
                      const uint32_t *start, double pw, const double *q_r2, int pfilter, int mode, GatherOutF out,
                      int grid, cudaStream_t s);
@@ -56,6 +64,8 @@ void launch_grid_setup(PassState *st, double r2_override, cudaStream_t s);
 void launch_scan(uint32_t *count, const PassState *st, uint32_t *block_sums, uint32_t *start, long long cell_cap,
                  cudaStream_t s);
 void launch_accum(const double *pass_img, double *sum, long long n, cudaStream_t s);
+void launch_accum_mixed(const float *direct, const float *gathered, const PassState *st, double pw, double *pass_img,
+                        double *sum, long long n, cudaStream_t s);
 void launch_pass_end(PassState *st, cudaStream_t s);
 int kernels_per_scan();
 
