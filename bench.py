@@ -230,8 +230,8 @@ def run_gpu(args, w):
                             alpha=w["alpha"], schedule_offset=1, precision=precision, use_graph=graph,
                             seed=args.seed if seed is None else seed, first_pass=first, cell_factor=args.cell_factor)
 
-    def timed_passes(precision, steps, warmup, first):
-        ctx.render_begin(cfg(precision, steps + warmup, first=first))
+    def timed_passes(precision, steps, warmup, seed):
+        ctx.render_begin(cfg(precision, steps + warmup, seed=seed))
         ctx.render_step(warmup)
         ctx.sync()
         torch.cuda.synchronize()
@@ -256,18 +256,21 @@ def run_gpu(args, w):
             ms = float(t.item())
         return ms
 
-    base_pass = rank * 1_000_000
+    # every run renders passes from pass 0 (the PA radius schedule starts
+    # there); independent random streams come from distinct seeds
+    seed_rank = args.seed + 1000 * rank
     clocks = Clocks(local)
     clocks.start()
-    ms = timed_passes(MIXED, args.steps, max(3, args.warmup), base_pass)
+    ms = timed_passes(MIXED, args.steps, max(3, args.warmup), seed_rank)
     clk = clocks.stop()
     st = ctx.stats()
     value = world * args.steps * w["nphoton"] / (ms / 1e3) / 1e6
     kernels_per_pass = st["kernels_per_pass"]
 
     # per-stage device time (eager passes with CUDA events between stages)
-    ctx.render_begin(cfg(MIXED, args.steps, first=base_pass + 500_000, graph=False))
-    ctx.set_stage_timing(True)
+    ctx.render_begin(cfg(MIXED, args.steps + max(3, args.warmup), seed=seed_rank + 1, graph=False))
+    ctx.render_step(max(3, args.warmup))
+    ctx.set_stage_timing(1)
     ctx.render_step(args.steps)
     ctx.sync()
     st_t = ctx.stats()
@@ -289,16 +292,16 @@ def run_gpu(args, w):
 
     # plain FP64 path on the same workload
     steps_plain = max(3, min(args.steps, 10))
-    ms_plain = timed_passes(PLAIN, steps_plain, 2, base_pass + 800_000)
+    ms_plain = timed_passes(PLAIN, steps_plain, 3, seed_rank + 2)
     value_plain = world * steps_plain * w["nphoton"] / (ms_plain / 1e3) / 1e6
 
     out_rmse = None
     if not args.no_rmse and rank == 0:
         P = w["passes"]
-        ctx.render_begin(cfg(MIXED, P))
+        ctx.render_begin(cfg(MIXED, P, seed=seed_rank))
         ctx.render_step(P)
         img_mixed = ctx.render_image()
-        ctx.render_begin(cfg(PLAIN, P))
+        ctx.render_begin(cfg(PLAIN, P, seed=seed_rank))
         ctx.render_step(P)
         img_plain = ctx.render_image()
         t0 = time.perf_counter()
@@ -320,7 +323,7 @@ def run_gpu(args, w):
     for k in range(e2e_steps):
         ctx.upload_scene(sc)
         ctx.set_camera(cam)
-        img = ctx.render(cfg(MIXED, w["passes"], first=base_pass + 900_000 + k * w["passes"]))
+        img = ctx.render(cfg(MIXED, w["passes"], seed=seed_rank + 3 + k))
     t_e2e = time.perf_counter() - t0
     e2e_value = world * e2e_steps * w["passes"] * w["nphoton"] / t_e2e / 1e6
     import ctypes

@@ -33,6 +33,7 @@ def nvcc() -> str:
 
 def _sources_mtime() -> float:
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    files.append(os.path.join(HERE, "cli", "ppmpa.cpp"))
     files.append(os.path.join(ROOT, "include", "ppm_api.h"))
     files.append(os.path.abspath(__file__))
     return max(os.path.getmtime(f) for f in files)
@@ -67,7 +68,23 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, LIB)
+    _build_cli()
     return LIB
+
+
+CLI = os.path.join(OUT, "ppmpa")
+
+
+def _build_cli() -> str:
+    """The `ppmpa` command-line program (same argv and output as the reference binary)."""
+    src = os.path.join(HERE, "cli", "ppmpa.cpp")
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), src,
+           "-o", CLI + ".tmp", "-L", OUT, "-lppmpa_gb300", "-Wl,-rpath,$ORIGIN"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"ppmpa CLI build failed:\n{res.stderr}")
+    os.replace(CLI + ".tmp", CLI)
+    return CLI
 
 
 if __name__ == "__main__":

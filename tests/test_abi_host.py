@@ -99,3 +99,21 @@ def test_ctx_create_without_gpu_reports_no_device(built_lib):
     st = lib.ppm_ctx_create(C.byref(h), 0, 1)
     assert st == 7 and not h.value
     assert lib.ppm_last_error(None).startswith(b"no CUDA device")
+
+
+def test_cli_usage_and_rust_number_format(built_lib):
+    import subprocess
+    from ppmpa_gb300 import build as lib_build
+    cli = lib_build.CLI
+    out = subprocess.run([cli, "-h"], capture_output=True, text=True)
+    assert out.returncode == 0 and out.stderr.startswith("Usage: ppmpa [-nc|-h]")
+    out = subprocess.run([cli, "1000", "0.1"], capture_output=True, text=True)   # too few arguments
+    assert out.returncode == 0 and "Usage" in out.stderr
+    # format!("{:e}") and format!("{}") of f64 (shortest round-trip digits)
+    vals = ["0.001234", "1.0", "0.0", "123456.0", "0.30000000000000004", "0.01", "250", "4.0", "1e21", "1.5e-7", "-2.5"]
+    want = [("1.234e-3", "0.001234"), ("1e0", "1"), ("0e0", "0"), ("1.23456e5", "123456"),
+            ("3.0000000000000004e-1", "0.30000000000000004"), ("1e-2", "0.01"), ("2.5e2", "250"), ("4e0", "4"),
+            ("1e21", "1000000000000000000000"), ("1.5e-7", "0.00000015"), ("-2.5e0", "-2.5")]
+    out = subprocess.run([cli, "--format-test", *vals], capture_output=True, text=True, check=True)
+    got = [tuple(l.split()) for l in out.stdout.strip().split("\n")]
+    assert got == want

@@ -271,3 +271,17 @@ def test_cell_factors_give_the_same_image(ctx):
     assert np.allclose(imgs[1], imgs[0], rtol=2e-5, atol=1e-7 * imgs[0].max())
     assert np.allclose(imgs[3], imgs[2], rtol=1e-12, atol=1e-14 * imgs[2].max())
     assert imgs[0].max() > 0
+
+
+def test_cli_renders_one_pass_in_reference_format(built_lib):
+    import subprocess
+    from ppmpa_gb300 import build as lib_build
+    out = subprocess.run([lib_build.CLI, "20000", "0.2", "cam.scr", "scene.scene"], capture_output=True, text=True,
+                         check=True, timeout=120)
+    lines = out.stdout.split("\n")
+    assert lines[0] == "P3" and lines[1] == "## max radiance = 0.01"
+    assert lines[2] == "## image parameters = 1/250, F4, ISO100" and lines[3] == "256 256" and lines[4] == "255"
+    px = [l.split() for l in lines[5:5 + 256 * 256]]
+    assert len(px) == 65536 and all(len(p) == 3 for p in px)
+    vals = np.array([[float(v) for v in p] for p in px])
+    assert np.isfinite(vals).all() and vals.max() > 0
