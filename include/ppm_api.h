@@ -200,6 +200,22 @@ int ppm_query_within(ppm_ctx *ctx, const double *q, int64_t nq, const double *r2
 int ppm_estimate(ppm_ctx *ctx, const double *pos, const double *nrm, int64_t nq,
                  int32_t pfilter, double *rgb);
 
+/* ppm_estimate_noalloc: no counterpart in the reference.  Same arguments and
+ * results as ppm_estimate, for at most PPM_ESTIMATE_NOALLOC_MAX_QUERIES
+ * queries per call (more returns PPM_ERR_INVALID_ARG with a message), but it
+ * never allocates or frees device memory.  It is for callers that cannot
+ * let the library allocate mid-run: a host whose own memory pool already
+ * holds nearly all of the device, or one that cannot take the device-wide
+ * wait a cudaFree implies while its other streams run.  The queries and
+ * results are staged in one fixed device array (about 5 MB) per device,
+ * shared by every context and call in the process.  The first call on a
+ * device looks up that array's address; make it before any stream capture
+ * begins.  Calls whose GPU work overlaps (two host threads, or two contexts
+ * on the same device) race on the array: serialise them. */
+#define PPM_ESTIMATE_NOALLOC_MAX_QUERIES 32768
+int ppm_estimate_noalloc(ppm_ctx *ctx, const double *pos, const double *nrm, int64_t nq,
+                         int32_t pfilter, double *rgb);
+
 /* ---- FP32 photon map (gather sweep) --------------------------------------- */
 /* A map of FP32 photons (n x 3 float positions, directions, wl).  Queries are
  * FP32 positions with FP64 radii^2; membership is decided exactly as the f64

@@ -43,6 +43,7 @@ SIGNATURES = {
     "ppm_photonmap_from_trace": (C.c_int, [_P, C.c_double]),
     "ppm_query_within": (C.c_int, [_P, _dp, C.c_int64, _dp, _i64p, _i32p, C.c_int64, _i64p]),
     "ppm_estimate": (C.c_int, [_P, _dp, _dp, C.c_int64, C.c_int32, _dp]),
+    "ppm_estimate_noalloc": (C.c_int, [_P, _dp, _dp, C.c_int64, C.c_int32, _dp]),
     "ppm_photonmap_build_f32": (C.c_int, [_P, _fp, _fp, _u8p, C.c_int64, C.c_double, C.c_double]),
     "ppm_query_within_f32": (C.c_int, [_P, _fp, C.c_int64, _dp, _i64p, _i32p, C.c_int64, _i64p]),
     "ppm_estimate_f32": (C.c_int, [_P, _fp, _fp, C.c_int64, _dp, _dp]),

@@ -10,6 +10,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -779,6 +780,98 @@ extern "C" int ppm_estimate(ppm_ctx *ctx, const double *pos, const double *nrm, 
                     ctx->map_pw, pfilter, 1, go, grid_blocks(ctx, 8), ctx->s);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(rgb, d_o, ob, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return PPM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free estimate.
+//
+// ppm_estimate stages its queries and results in the context's scratch
+// buffer, which it frees and re-allocates whenever a call is larger than any
+// before it.  Some callers cannot have the library allocate at that point:
+// a host that has already given nearly all device memory to its own pool
+// (where a cudaMalloc could fail in the middle of a run), or one running
+// other streams on the same GPU that cannot take the device-wide wait a
+// cudaFree implies.  ppm_estimate_noalloc computes the same estimates from a
+// fixed array in device memory instead, so it never allocates or frees.
+//
+// The array is one per device, shared by every context and every call in
+// this process.  Its device address is looked up the first time the entry
+// point runs on a device (with that device current); make that first call
+// before any stream capture begins.  Calls whose GPU work overlaps -- from
+// two host threads, or two contexts on the same device -- race on the array
+// and must be serialised by the caller.
+// ---------------------------------------------------------------------------
+namespace {
+
+// Per-query staging: position and normal as the caller passes them, the hit
+// point the gather reads, and the output row.  Each section is sized for the
+// maximum query count, so every section starts on a 256-byte boundary.
+constexpr size_t NOALLOC_Q = PPM_ESTIMATE_NOALLOC_MAX_QUERIES;
+constexpr size_t NOALLOC_POS_OFF = 0;
+constexpr size_t NOALLOC_NRM_OFF = NOALLOC_POS_OFF + sizeof(double) * 3 * NOALLOC_Q;
+constexpr size_t NOALLOC_HIT_OFF = NOALLOC_NRM_OFF + sizeof(double) * 3 * NOALLOC_Q;
+constexpr size_t NOALLOC_OUT_OFF = NOALLOC_HIT_OFF + sizeof(HitPoint<double>) * NOALLOC_Q;
+constexpr size_t NOALLOC_BYTES = NOALLOC_OUT_OFF + sizeof(double) * 3 * NOALLOC_Q;
+static_assert(NOALLOC_NRM_OFF % 256 == 0 && NOALLOC_HIT_OFF % 256 == 0 && NOALLOC_OUT_OFF % 256 == 0,
+              "staging sections must stay 256-byte aligned");
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_estimate_scratch[NOALLOC_BYTES];
+
+// Device address of g_estimate_scratch on ctx->device, looked up once per
+// device; ctx->device must be current.
+static int noalloc_scratch(ppm_ctx *ctx, char **out) {
+    if (ctx->device < 0 || ctx->device >= NOALLOC_MAX_DEVICES)
+        return set_err(ctx, PPM_ERR_INVALID_ARG, "device %d: the allocation-free estimate supports devices 0..%d",
+                       ctx->device, NOALLOC_MAX_DEVICES - 1);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    void *&addr = g_noalloc_addr[ctx->device];
+    if (!addr) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_estimate_scratch);
+        if (e != cudaSuccess || !p)
+            return set_err(ctx, PPM_ERR_CUDA, "cudaGetSymbolAddress(estimate scratch) on device %d failed: %s",
+                           ctx->device, cudaGetErrorString(e));
+        addr = p;
+    }
+    *out = static_cast<char *>(addr);
+    return PPM_OK;
+}
+
+extern "C" int ppm_estimate_noalloc(ppm_ctx *ctx, const double *pos, const double *nrm, int64_t nq,
+                                    int32_t pfilter, double *rgb) {
+    if (!ctx || nq < 0 || (nq && (!pos || !nrm || !rgb)) || pfilter < 0 || pfilter > 2) return PPM_ERR_INVALID_ARG;
+    if (nq > PPM_ESTIMATE_NOALLOC_MAX_QUERIES)
+        return set_err(ctx, PPM_ERR_INVALID_ARG,
+                       "%lld queries: the allocation-free estimate takes at most %d per call (split the batch "
+                       "or use ppm_estimate)", (long long)nq, PPM_ESTIMATE_NOALLOC_MAX_QUERIES);
+    if (ctx->map_kind != 1) return set_err(ctx, PPM_ERR_NOT_READY, "no FP64 photon map built");
+    if (nq == 0) return PPM_OK;
+    CK(cudaSetDevice(ctx->device));
+    char *base = nullptr;
+    TRY(noalloc_scratch(ctx, &base));
+    double *d_p = (double *)(base + NOALLOC_POS_OFF), *d_n = (double *)(base + NOALLOC_NRM_OFF);
+    HitPoint<double> *d_h = (HitPoint<double> *)(base + NOALLOC_HIT_OFF);
+    double *d_o = (double *)(base + NOALLOC_OUT_OFF);
+    size_t pb = sizeof(double) * 3 * nq;
+    CK(cudaMemcpyAsync(d_p, pos, pb, cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(d_n, nrm, pb, cudaMemcpyHostToDevice, ctx->s));
+    // The gather writes every output row it owns; the rows are cleared anyway
+    // so that no row can ever carry an earlier call's value.
+    CK(cudaMemsetAsync(d_o, 0, pb, ctx->s));
+    launch_make_queries_d(d_p, d_n, nq, d_h, ctx->s);
+    GatherOutD go{nullptr, d_o, nullptr};
+    launch_gather_d(d_h, ctx->st, nq, as<double4>(ctx->spos), as<double4>(ctx->sdir), as<uint32_t>(ctx->start),
+                    ctx->map_pw, pfilter, 1, go, grid_blocks(ctx, 8), ctx->s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(rgb, d_o, pb, cudaMemcpyDeviceToHost, ctx->s));
     CK(cudaStreamSynchronize(ctx->s));
     return PPM_OK;
 }
