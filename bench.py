@@ -30,11 +30,20 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
-    # BASELINE config 2: glass box, 512^2, 1M photons/pass, 64 passes
+    # glass box (glass sphere IOR 1.5 + mirror sphere), 512^2, 1M photons/pass, 64 passes
     "glass_box_512": dict(scene="c2", reso=512, nphoton=1_000_000, passes=64, r0=0.05, alpha=0.7),
-    # BASELINE config 1: diffuse-sphere box, 256^2, 200k photons/pass, 10 passes
+    # diffuse-sphere box, 256^2, 200k photons/pass, 10 passes
     "box_256": dict(scene="c1", reso=256, nphoton=200_000, passes=10, r0=0.05, alpha=0.7),
+    # box + displaced icosphere of 1,310,720 triangles (half glass), spot light,
+    # 1024^2, 10M photons/pass, 32 passes; rays walk the GPU-built BVH.  The CPU
+    # leg tests every object per ray as the reference does, so it times a
+    # sample of photons only; no many-pass FP64 image is rendered for RMSE.
+    "mesh_1024": dict(scene="mesh", mesh_level=8, reso=1024, nphoton=10_000_000, passes=32, r0=0.05, alpha=0.7,
+                      rmse=False, cpu_sample_photons=256),
 }
+# gather sweep over an FP32 photon map: 100M photons, 4M queries with radii
+# log-uniform over [1e-3, 2e-2] (ppmpa_gb300/workloads.py)
+SWEEPS = {"gather_sweep_uniform": "uniform", "gather_sweep_clustered": "clustered"}
 L2_BYTES = 129 * 1024 * 1024
 
 
@@ -51,7 +60,11 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="glass_box_512", choices=list(WORKLOADS))
+    p.add_argument("--workload", default="glass_box_512", choices=list(WORKLOADS) + list(SWEEPS))
+    p.add_argument("--sweep-photons", type=int, default=100_000_000)
+    p.add_argument("--sweep-queries", type=int, default=4_000_000)
+    p.add_argument("--sweep-cells", type=float, default=0.0,
+                   help="FP32 map cells per radius for the sweep (0: autotune on a query sample)")
     p.add_argument("--oracle-passes", type=int, default=4096,
                    help="passes of the FP64 high-pass image the RMSE is measured against")
     p.add_argument("--no-rmse", action="store_true")
@@ -91,8 +104,9 @@ def run_profile(args, w):
 
 
 def scene_of(w):
-    from ppmpa_gb300 import scene as S
-    return S.box_scene(w["scene"]), S.box_camera(w["reso"])
+    from ppmpa_gb300 import mesh as M, scene as S
+    sc = M.mesh_scene(w["mesh_level"]) if w["scene"] == "mesh" else S.box_scene(w["scene"])
+    return sc, S.box_camera(w["reso"])
 
 
 def dist_env():
@@ -154,6 +168,12 @@ def cpu_pass_rate(w, seed, passes=1):
     from oracle.binding import Oracle, radius_schedule
     sc, cam = scene_of(w)
     orc = Oracle(sc, cam, threads=0)
+    if "cpu_sample_photons" in w:      # photon tracing of a sample only
+        n = w["cpu_sample_photons"]
+        t0 = time.perf_counter()
+        orc.trace_photons(n, True, seed, 0)
+        dt = time.perf_counter() - t0
+        return n / dt / 1e6, orc.L.orc_get_threads(), dt
     r2 = radius_schedule(w["r0"], w["alpha"], 1, passes)
     img = np.zeros((cam.yreso, cam.xreso, 3))
     t0 = time.perf_counter()
@@ -170,12 +190,16 @@ def run_reference(args, w):
         return
     for k in range(args.warmup):
         cpu_pass_rate(w, args.seed + 1000 + k)
-    total = 0.0
+    total = done = 0.0
     threads = 1
     for k in range(args.steps):
-        _, threads, dt = cpu_pass_rate(w, args.seed + k)
+        rate, threads, dt = cpu_pass_rate(w, args.seed + k)
         total += dt
-    value = w["nphoton"] * args.steps / total / 1e6
+        done += rate * dt * 1e6                     # photons of this step's sample
+    value = done / total / 1e6
+    what = (f"photon tracing of {w['cpu_sample_photons']} photons per step (every object tested per ray)"
+            if "cpu_sample_photons" in w else
+            f"one full pass per step ({w['nphoton']} photons, {w['reso']}x{w['reso']} eye rays)")
     out = {
         "impl": "reference", "metric": METRIC, "value": value,
         "unit": "Mphotons/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
@@ -183,8 +207,7 @@ def run_reference(args, w):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene, seeded photon streams)",
         "config": {"workload": args.workload, **w},
         "cpu_baseline": {"value": value, "unit": "Mphotons/s", "cores": threads, "kind": "port",
-                         "sample": f"one full pass per step ({w['nphoton']} photons, {w['reso']}x{w['reso']} eye "
-                                   f"rays), FP64 restatement of the reference CPU path, {threads} threads"},
+                         "sample": f"{what}, FP64 restatement of the reference CPU path, {threads} threads"},
         "e2e": {"value": value, "unit": "Mphotons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
@@ -303,7 +326,7 @@ def run_gpu(args, w):
     value_plain = world * steps_plain * w["nphoton"] / (ms_plain / 1e3) / 1e6
 
     out_rmse = None
-    if not args.no_rmse and rank == 0:
+    if not args.no_rmse and w.get("rmse", True) and rank == 0:
         P = w["passes"]
         ctx.render_begin(cfg(MIXED, P, seed=seed_rank))
         ctx.render_step(P)
@@ -335,16 +358,17 @@ def run_gpu(args, w):
     e2e_value = world * e2e_steps * w["passes"] * w["nphoton"] / t_e2e / 1e6
     import ctypes
     from ppmpa_gb300 import scene as S
-    h2d = (ctypes.sizeof(S.Object) * len(sc.objects) + ctypes.sizeof(S.Material) * len(sc.materials) +
+    h2d = (ctypes.sizeof(S.Object) * sc.n_objects + ctypes.sizeof(S.Material) * len(sc.materials) +
            ctypes.sizeof(S.Light) * len(sc.lights) + ctypes.sizeof(S.Camera))
     d2h = img.nbytes
 
     cpu = None
     if rank == 0:
         rate, threads, dt = cpu_pass_rate(w, args.seed, 1)
+        what = (f"photon tracing of {w['cpu_sample_photons']} photons (every object tested per ray)"
+                if "cpu_sample_photons" in w else f"one full pass ({w['nphoton']} photons, {w['reso']}x{w['reso']})")
         cpu = {"value": rate, "unit": "Mphotons/s", "cores": threads, "kind": "port",
-               "sample": f"one full pass ({w['nphoton']} photons, {w['reso']}x{w['reso']}), FP64 restatement "
-                         f"of the reference CPU path, {threads} threads, {dt:.2f} s"}
+               "sample": f"{what}, FP64 restatement of the reference CPU path, {threads} threads, {dt:.2f} s"}
 
     ctx.close()
     if rank != 0:
@@ -375,8 +399,130 @@ def run_gpu(args, w):
     print(json.dumps(out))
 
 
+def hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        return json.load(open(path))["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+def sweep_inputs(args, kind):
+    from ppmpa_gb300 import workloads as W
+    pos, d, wl = W.photons(args.sweep_photons, kind)
+    q, nrm, r2 = W.queries(args.sweep_queries, kind)
+    return pos, d, wl, q, nrm, r2
+
+
+def run_sweep(args, kind):
+    """One step = one ppm_estimate_f32 call over all queries (host arrays in,
+    host results out).  value: estimates per second of the device work (query
+    sort + gather); e2e: the same through the call with its copies."""
+    import torch
+    from ppmpa_gb300 import Context, workloads as W
+    t0 = time.perf_counter()
+    pos, d, wl, q, nrm, r2 = sweep_inputs(args, kind)
+    gen_s = time.perf_counter() - t0
+    n_ph, n_q = len(pos), len(q)
+    ctx = Context(0, seed=args.seed)
+    ctx.set_stage_timing(1)
+    ctx.build_photonmap_f32(pos, d, wl, 1.0 / n_ph, W.R_MAX ** 2)
+    ctx.build_photonmap_f32(pos, d, wl, 1.0 / n_ph, W.R_MAX ** 2)   # second build: warm
+    build_ms = ctx.stats()["stage_ms"]["map_build"] / 2
+    if args.sweep_cells > 0:
+        ctx.regrid_photonmap_f32(args.sweep_cells)
+        cells, tune = args.sweep_cells, None
+    else:
+        sub = np.random.default_rng(11).choice(n_q, min(n_q, 262144), replace=False)
+        cells, tune_ms = ctx.tune_photonmap_f32(q[sub], nrm[sub], r2[sub])
+        tune = {"sample_queries": len(sub), "best_ms": tune_ms}
+    ctx.set_stage_timing(2)                         # one counted run: candidates and hits
+    ctx.estimate_f32(q, nrm, r2)
+    cnt = ctx.stats()
+    ctx.set_stage_timing(1)
+    for _ in range(max(3, args.warmup)):
+        ctx.estimate_f32(q, nrm, r2)
+    base = ctx.stats()
+    clocks = Clocks(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.estimate_f32(q, nrm, r2)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    st = ctx.stats()
+    ctx.close()
+    gather_ms = (st["stage_ms"]["gather"] - base["stage_ms"]["gather"]) / args.steps
+    sort_ms = (st["stage_ms"]["query_sort"] - base["stage_ms"]["query_sort"]) / args.steps
+    dev_ms = gather_ms + sort_ms
+    peak, src = hbm_peak()
+    photon_bytes = 16                               # float3 position + packed direction/wavelength
+    query_bytes = 12 + 12 + 8 + 24                  # position, normal, radius^2 in; RGB out
+    ab = n_ph * photon_bytes + n_q * query_bytes
+    achieved = ab / (gather_ms / 1e3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        traffic = json.load(open(prof)).get(args.workload)
+    out = {
+        "metric": f"gather sweep estimates/s ({n_ph} FP32 photons, {n_q} queries, r log-uniform 1e-3..2e-2)",
+        "value": n_q / (dev_ms / 1e3) / 1e6, "unit": "Mqueries/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": dev_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 positions/tests, f64 rounding-band recheck and normalisation",
+        "data": "synthetic (seeded photons and queries)",
+        "config": {"workload": args.workload, "distribution": kind, "photons": n_ph, "queries": n_q,
+                   "r_min": W.R_MIN, "r_max": W.R_MAX, "cells_per_radius": cells, "autotune": tune,
+                   "l2": f"inputs larger than L2 (map {n_ph * photon_bytes / 2**30:.2f} GiB)"},
+        "gather_ms": gather_ms, "query_sort_ms": sort_ms, "map_build_ms": build_ms,
+        "photon_tests_per_s": cnt["candidates"] / (gather_ms / 1e3), "in_radius_per_s": cnt["in_radius"] / (gather_ms / 1e3),
+        "candidates": cnt["candidates"], "in_radius": cnt["in_radius"], "lane_slots": cnt["gather_slots"],
+        "e2e": {"value": n_q * args.steps / wall / 1e6, "unit": "Mqueries/s",
+                "h2d_bytes_per_step": n_q * (12 + 12 + 8), "d2h_bytes_per_step": n_q * 24,
+                "step": "ppm_estimate_f32 over all queries, pageable host arrays"},
+        "gpu_launches": 6 * args.steps,
+        "roofline": {"kernel": "gather", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": src, "algorithmic_bytes": ab},
+        "input_generation_s": gen_s, "clocks": clk,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_sweep_reference(args, kind):
+    """The FP64 restatement of the reference's estimate (grid in place of the
+    kd-tree) over the same map, on a bounded sample of the queries."""
+    from oracle.binding import Oracle
+    from ppmpa_gb300 import scene as S
+    pos, d, wl, q, nrm, r2 = sweep_inputs(args, kind)
+    orc = Oracle(S.Scene(), threads=0)
+    threads = orc.L.orc_get_threads()
+    p64, d64 = pos.astype(np.float64), d.astype(np.float64)
+    n_s = min(len(q), 20000)
+    qs, ns, rs = q[:n_s].astype(np.float64), nrm[:n_s].astype(np.float64), r2[:n_s]
+    total = 0.0
+    for k in range(max(1, args.warmup) + args.steps):
+        orc.estimate_radii(p64, d64, wl, qs, ns, rs, 1.0 / len(pos))
+        if k >= max(1, args.warmup):
+            total += orc.L.orc_last_query_seconds()   # query phase; the grid build is not timed
+    value = n_s * args.steps / total / 1e6
+    sample = f"{n_s} of the queries per step over the full map, {threads} threads, grid build excluded"
+    print(json.dumps({
+        "impl": "reference", "metric": f"gather sweep estimates/s ({len(pos)} FP32 photons, {len(q)} queries, "
+                                       f"r log-uniform 1e-3..2e-2)",
+        "value": value, "unit": "Mqueries/s", "n_gpus": 0, "steps": args.steps, "warmup": max(1, args.warmup),
+        "ms_per_step": total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded photons and queries)",
+        "config": {"workload": args.workload, "distribution": kind, "photons": len(pos), "queries": len(q)},
+        "cpu_baseline": {"value": value, "unit": "Mqueries/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "Mqueries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload in SWEEPS:
+        rank, world, _ = dist_env()
+        if rank == 0:
+            (run_sweep_reference if args.impl == "reference" else run_sweep)(args, SWEEPS[args.workload])
+        return
     w = WORKLOADS[args.workload]
     if args.profile:
         run_profile(args, w)

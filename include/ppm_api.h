@@ -38,7 +38,7 @@ typedef enum ppm_status {
 enum { PPM_SHAPE_POINT = 0, PPM_SHAPE_PLAIN = 1, PPM_SHAPE_SPHERE = 2,
        PPM_SHAPE_POLYGON = 3, PPM_SHAPE_PARALLELOGRAM = 4 };
 enum { PPM_SURF_NOTHING = 0, PPM_SURF_SIMPLE = 1, PPM_SURF_TS = 2 };
-enum { PPM_LIGHT_POINT = 0, PPM_LIGHT_PARALLELOGRAM = 1, PPM_LIGHT_SUN = 2 };
+enum { PPM_LIGHT_POINT = 0, PPM_LIGHT_PARALLELOGRAM = 1, PPM_LIGHT_SUN = 2, PPM_LIGHT_SPOT = 3 };
 enum { PPM_FILTER_NONE = 0, PPM_FILTER_CONE = 1, PPM_FILTER_GAUSS = 2 };
 enum { PPM_WL_RED = 0, PPM_WL_GREEN = 1, PPM_WL_BLUE = 2 };
 
@@ -77,7 +77,11 @@ typedef struct ppm_material {
 } ppm_material;
 
 /* Light (src/ray/light.rs:16-39).  color is used as given: the reference's
- * scene code normalises it (Color::normalize) before building the light. */
+ * scene code normalises it (Color::normalize) before building the light.
+ * PPM_LIGHT_SPOT has no reference counterpart: a point light at pos whose
+ * photons leave uniformly over the cone around the unit axis dir with
+ * cos(half-angle) = dir1[0]; like the reference's point light it adds no
+ * direct light (one sample, see get_radiance_from_light). */
 typedef struct ppm_light {
     int32_t kind;
     int32_t pad_;
@@ -158,6 +162,29 @@ int  ppm_scene_upload(ppm_ctx *ctx, const ppm_object *objs, int32_t n_objs,
                       const ppm_light *lights, int32_t n_lights);
 /* Replaces read_camera (src/camera.rs:108): derives, then stores. */
 int  ppm_camera_set(ppm_ctx *ctx, const ppm_camera *cam);
+/* Scene and camera files.  The reference ships example/*.scene and *.scr
+ * files (camera grammar: doc/ebnf-camera.txt) but its read_scene and
+ * read_camera ignore them (src/scene.rs:20, src/camera.rs:108); these
+ * readers turn the files into the structs above.  ppm_scene_parse: on input
+ * *n_objs, *n_mats, *n_lights are the capacities of the arrays; with all
+ * three arrays NULL it only counts.  ppm_camera_parse overrides the fields
+ * the file sets (start from the reference camera) and derives the rest;
+ * *nphoton gets the file's nphoton if present.  A syntax error, an unknown
+ * type or name returns PPM_ERR_INVALID_ARG; ppm_parse_error() says where. */
+int ppm_scene_parse(const char *text, ppm_object *objs, int32_t *n_objs, ppm_material *mats, int32_t *n_mats,
+                    ppm_light *lights, int32_t *n_lights);
+int ppm_camera_parse(const char *text, ppm_camera *cam, int64_t *nphoton);
+const char *ppm_parse_error(void);
+
+/* Ray acceleration.  The reference tests every object per ray
+ * (tracer.rs:321-329).  From 32 bounded objects (spheres, triangles,
+ * parallelograms) up, scene upload builds a BVH on the GPU and rays walk it;
+ * results are the same (nearest t, then lowest index).  PPM_ACCEL_BVH forces
+ * the hierarchy from 2 objects, PPM_ACCEL_NONE the loop; applies at once. */
+enum { PPM_ACCEL_AUTO = 0, PPM_ACCEL_BVH = 1, PPM_ACCEL_NONE = 2 };
+int  ppm_set_accel(ppm_ctx *ctx, int32_t mode);
+/* objects in the hierarchy (0: none) and unbounded objects tested per ray */
+int  ppm_accel_info(ppm_ctx *ctx, int32_t *bvh_objects, int32_t *unbounded);
 /* Host helpers: camera.rs:150-175 and Surface::new_simple/new_ts (surface.rs:45-66). */
 void ppm_camera_derive(ppm_camera *cam);
 void ppm_material_derive(ppm_material *mat);
@@ -224,8 +251,20 @@ int ppm_photonmap_build_f32(ppm_ctx *ctx, const float *pos, const float *dir,
                             const uint8_t *wl, int64_t n, double power, double radius2_max);
 int ppm_query_within_f32(ppm_ctx *ctx, const float *q, int64_t nq, const double *r2,
                          int64_t *offsets, int32_t *idx, int64_t cap, int64_t *total);
+/* Queries are gathered in the map's cell order on the device; rgb comes back
+ * in the caller's order. */
 int ppm_estimate_f32(ppm_ctx *ctx, const float *pos, const float *nrm, int64_t nq,
                      const double *r2, double *rgb);
+/* Grid cell size of the FP32 map: cells_per_radius cells per maximum query
+ * radius (default 2, range [0.5, 8]).  Re-sorts the map on the device; sets
+ * and estimates do not change, only their cost.  No reference counterpart
+ * (the reference's kd-tree has no cell size). */
+int ppm_photonmap_regrid_f32(ppm_ctx *ctx, double cells_per_radius);
+/* Autotuner: times sort + gather of a sample of queries with 1, 1.5, 2, 3
+ * and 4 cells per radius, leaves the map on the fastest grid and returns it
+ * (best_cells) with its device time in ms (best_ms).  No reference counterpart. */
+int ppm_photonmap_tune_f32(ppm_ctx *ctx, const float *pos, const float *nrm, int64_t nq,
+                           const double *r2, double *best_cells, double *best_ms);
 
 /* ---- progressive render ---------------------------------------------------- */
 /* Runs cfg->passes passes (emit + trace photons, build the map, eye trace,

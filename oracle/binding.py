@@ -63,6 +63,9 @@ def lib() -> C.CDLL:
             "orc_within": (C.c_int64, [_dp, C.c_int64, _dp, C.c_int64, _dp, _i64p, _i32p, C.c_int64]),
             "orc_estimate": (None, [_dp, _dp, _u8p, C.c_int64, _dp, _dp, C.c_int64, C.c_double, C.c_double,
                                     C.c_int, _dp]),
+            "orc_estimate_radii": (None, [_dp, _dp, _u8p, C.c_int64, _dp, _dp, C.c_int64, _dp, C.c_double,
+                                          C.c_int, _dp]),
+            "orc_last_query_seconds": (C.c_double, []),
             "orc_trace_photons": (C.c_int64, [C.POINTER(_Scene), C.c_int64, C.c_int, C.c_uint64, C.c_uint32,
                                               _dp, _dp, _u8p, _i32p, _i8p, C.c_int64, _dp, _i64p]),
             "orc_eye_pass": (None, [C.POINTER(_Scene), C.c_void_p, _dp, _dp, _u8p, C.c_int64, C.c_double,
@@ -130,17 +133,36 @@ class Oracle:
         return dict(pos=pos[:n], dir=dirs[:n], wl=wl[:n], emit=emit[:n], level=level[:n], power=pw.value,
                     n_emitted=nem.value)
 
-    def within(self, ppos, q, r2):
+    def within(self, ppos, q, r2, cap_hint: int = 0):
+        """In-radius sets (offsets, ascending indices).  With cap_hint >= the
+        total, one call (one grid build) counts and fills."""
         ppos = np.ascontiguousarray(ppos, np.float64).reshape(-1, 3)
         q = np.ascontiguousarray(q, np.float64).reshape(-1, 3)
         r2 = np.ascontiguousarray(np.broadcast_to(np.asarray(r2, np.float64), (q.shape[0],)))
         off = np.zeros(q.shape[0] + 1, np.int64)
+        idx = np.zeros(max(1, cap_hint), np.int32)
         tot = self.L.orc_within(_p(ppos, C.c_double), ppos.shape[0], _p(q, C.c_double), q.shape[0],
-                                _p(r2, C.c_double), _p(off, C.c_int64), None, 0)
-        idx = np.zeros(max(1, tot), np.int32)
-        self.L.orc_within(_p(ppos, C.c_double), ppos.shape[0], _p(q, C.c_double), q.shape[0], _p(r2, C.c_double),
-                          _p(off, C.c_int64), _p(idx, C.c_int32), idx.size)
+                                _p(r2, C.c_double), _p(off, C.c_int64), _p(idx, C.c_int32) if cap_hint else None,
+                                cap_hint)
+        if tot > cap_hint:
+            idx = np.zeros(max(1, tot), np.int32)
+            self.L.orc_within(_p(ppos, C.c_double), ppos.shape[0], _p(q, C.c_double), q.shape[0],
+                              _p(r2, C.c_double), _p(off, C.c_int64), _p(idx, C.c_int32), idx.size)
         return off, idx[:tot]
+
+    def estimate_radii(self, ppos, pdir, pwl, qpos, qnrm, r2, pw, pfilter=0):
+        """estimate with one radius^2 per query."""
+        ppos = np.ascontiguousarray(ppos, np.float64).reshape(-1, 3)
+        pdir = np.ascontiguousarray(pdir, np.float64).reshape(-1, 3)
+        pwl = np.ascontiguousarray(pwl, np.uint8)
+        qpos = np.ascontiguousarray(qpos, np.float64).reshape(-1, 3)
+        qnrm = np.ascontiguousarray(qnrm, np.float64).reshape(-1, 3)
+        r2 = np.ascontiguousarray(np.broadcast_to(np.asarray(r2, np.float64), (qpos.shape[0],)))
+        rgb = np.zeros((qpos.shape[0], 3))
+        self.L.orc_estimate_radii(_p(ppos, C.c_double), _p(pdir, C.c_double), _p(pwl, C.c_uint8), ppos.shape[0],
+                                  _p(qpos, C.c_double), _p(qnrm, C.c_double), qpos.shape[0], _p(r2, C.c_double),
+                                  float(pw), int(pfilter), _p(rgb, C.c_double))
+        return rgb
 
     def estimate(self, ppos, pdir, pwl, qpos, qnrm, r2, pw, pfilter=0):
         ppos = np.ascontiguousarray(ppos, np.float64).reshape(-1, 3)

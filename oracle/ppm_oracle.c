@@ -23,6 +23,7 @@
 #include "ppm_oracle.h"
 
 #include <math.h>
+#include <time.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -627,6 +628,27 @@ static const orc_material *mat_of(const orc_scene *sc, int m) { return m < 0 ? &
 /* ------------------------------------------------------------------------ */
 typedef struct { int wl; V3 pos, dir; } photon_t;
 
+/* Spot light: an extension with no reference counterpart (light.rs:16-38
+ * has point, parallelogram and sun lights).  A point light whose photons
+ * leave uniformly over the solid angle of the cone around the unit axis
+ * l->dir with cos(half-angle) l->dir1[0]: u -> cos(theta) = 1 - u (1 - cc),
+ * then phi in [0, 2 pi); frame b1 = normalize(h x a), b2 = a x b1, h = x
+ * unless |a.x| >= 0.9, then y. */
+static V3 spot_dir(rng_t *rg, V3 a, double cc) {
+    double u = gen_range(rg, 0.0, 1.0);
+    double phi = gen_range(rg, 0.0, 2.0 * PI_D);
+    double c = 1.0 - u * (1.0 - cc);
+    double s = sqrt(1.0 - c * c);
+    double sn = m_sin(phi), cs = m_cos(phi);
+    V3 h = fabs(a.x) < 0.9 ? v3(1.0, 0.0, 0.0) : v3(0.0, 1.0, 0.0);
+    V3 b1 = v3(1.0, 0.0, 0.0);
+    vnormalize(vcross(h, a), &b1);
+    V3 b2 = vcross(a, b1);
+    V3 d = a;
+    vnormalize(vadd(vadd(vmul(b1, s * cs), vmul(b2, s * sn)), vmul(a, c)), &d);
+    return d;
+}
+
 /* Light::generate_photon, light.rs:67-91; select_wavelength, light.rs:157-160 */
 static photon_t generate_photon(const orc_light *l, rng_t *rg) {
     photon_t ph;
@@ -634,6 +656,9 @@ static photon_t generate_photon(const orc_light *l, rng_t *rg) {
     if (l->kind == ORC_LPOINT) {
         ph.pos = v3p(l->pos);
         ph.dir = random_dir(rg);
+    } else if (l->kind == ORC_LSPOT) {
+        ph.pos = v3p(l->pos);
+        ph.dir = spot_dir(rg, v3p(l->dir), l->dir1[0]);
     } else if (l->kind == ORC_LPARALLELOGRAM) {
         double t1 = gen_range(rg, 0.0, 1.0);
         double t2 = gen_range(rg, 0.0, 1.0);
@@ -982,6 +1007,40 @@ void orc_estimate(const double *ppos, const double *pdir, const uint8_t *pwl, in
     grid_free(&pm.g);
 }
 
+static double g_last_query_seconds = 0.0;
+double orc_last_query_seconds(void) { return g_last_query_seconds; }
+
+static double wall_seconds(void) {
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
+}
+
+void orc_estimate_radii(const double *ppos, const double *pdir, const uint8_t *pwl, int64_t np,
+                        const double *qpos, const double *qnrm, int64_t nq,
+                        const double *r2, double pw, int pfilter, double *rgb) {
+    double rmax2 = 0.0;
+    for (int64_t i = 0; i < nq; i++) if (r2[i] > rmax2) rmax2 = r2[i];
+    pmap_t pm = {ppos, pdir, pwl, np, pw, rmax2, pfilter, {{0}, 0, {0}, NULL, NULL}};
+    grid_build(&pm.g, ppos, np, sqrt(rmax2));
+    double t0 = wall_seconds();
+#pragma omp parallel num_threads(orc_get_threads())
+    {
+        nb_t *buf = NULL;
+        int64_t bc = 0;
+        pmap_t qm = pm;
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t i = 0; i < nq; i++) {
+            qm.r2 = r2[i];
+            V3 r = estimate_radiance(&qm, v3p(qpos + 3 * i), v3p(qnrm + 3 * i), &buf, &bc);
+            rgb[3 * i] = r.x; rgb[3 * i + 1] = r.y; rgb[3 * i + 2] = r.z;
+        }
+        free(buf);
+    }
+    g_last_query_seconds = wall_seconds() - t0;
+    grid_free(&pm.g);
+}
+
 /* ------------------------------------------------------------------------ */
 /* Direct light: get_radiance_from_light / illuminated, tracer.rs:263-290;  */
 /* Light::get_direction / get_radiance, light.rs:93-150.  The reference     */
@@ -993,7 +1052,7 @@ static const double TSS[5] = {0.1, 0.3, 0.5, 0.7, 0.9};
 
 static V3 light_radiance(const orc_light *l, double d) {
     double l0;
-    if (l->kind == ORC_LPOINT) l0 = l->flux / (PI4_D * d);
+    if (l->kind == ORC_LPOINT || l->kind == ORC_LSPOT) l0 = l->flux / (PI4_D * d);
     else if (l->kind == ORC_LPARALLELOGRAM) l0 = (2.0 * l->flux * PARA_DIV * PARA_DIV) / (PI4_D * d);
     else l0 = l->flux;
     return v3(l->color[0] * l0, l->color[1] * l0, l->color[2] * l0);
@@ -1002,7 +1061,7 @@ static V3 light_radiance(const orc_light *l, double d) {
 static V3 radiance_from_light(const orc_scene *sc, V3 p, V3 n, const orc_light *l) {
     V3 lds[25];
     int nl = 0;
-    if (l->kind == ORC_LPOINT) {
+    if (l->kind == ORC_LPOINT || l->kind == ORC_LSPOT) {
         lds[nl++] = vsub(v3p(l->pos), p);
     } else if (l->kind == ORC_LPARALLELOGRAM) {
         for (int a = 0; a < 5; a++)

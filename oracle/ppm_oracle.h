@@ -40,7 +40,7 @@ enum { ORC_POINT = 0, ORC_PLAIN = 1, ORC_SPHERE = 2, ORC_POLYGON = 3, ORC_PARALL
 /* Surface kinds: src/ray/surface.rs:16-41 */
 enum { ORC_NOTHING = 0, ORC_SIMPLE = 1, ORC_TS = 2 };
 /* Light kinds: src/ray/light.rs:16-39 */
-enum { ORC_LPOINT = 0, ORC_LPARALLELOGRAM = 1, ORC_LSUN = 2 };
+enum { ORC_LPOINT = 0, ORC_LPARALLELOGRAM = 1, ORC_LSUN = 2, ORC_LSPOT = 3 };
 /* Photon filters: src/ray/optics.rs:17-21 */
 enum { ORC_PF_NONE = 0, ORC_PF_CONE = 1, ORC_PF_GAUSS = 2 };
 
@@ -132,6 +132,14 @@ int64_t orc_within(const double *ppos, int64_t np, const double *q, int64_t nq,
 void orc_estimate(const double *ppos, const double *pdir, const uint8_t *pwl, int64_t np,
                   const double *qpos, const double *qnrm, int64_t nq,
                   double r2, double pw, int pfilter, double *rgb);
+
+/* The same estimate with a radius per query (r2[i]), as the FP32 photon map's
+ * estimate entry point takes them; one grid over the photons serves all. */
+void orc_estimate_radii(const double *ppos, const double *pdir, const uint8_t *pwl, int64_t np,
+                        const double *qpos, const double *qnrm, int64_t nq,
+                        const double *r2, double pw, int pfilter, double *rgb);
+/* wall seconds of the query phase (grid build excluded) of the last call above */
+double orc_last_query_seconds(void);
 
 /* ---- photon tracing (src/tracer.rs:31-125, src/ray/light.rs:67-91) ------ */
 /* Emits the per-light counts of src/bin/ppmpa.rs:30-31 (pw = sum flux / nphoton,

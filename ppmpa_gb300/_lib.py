@@ -47,6 +47,14 @@ SIGNATURES = {
     "ppm_photonmap_build_f32": (C.c_int, [_P, _fp, _fp, _u8p, C.c_int64, C.c_double, C.c_double]),
     "ppm_query_within_f32": (C.c_int, [_P, _fp, C.c_int64, _dp, _i64p, _i32p, C.c_int64, _i64p]),
     "ppm_estimate_f32": (C.c_int, [_P, _fp, _fp, C.c_int64, _dp, _dp]),
+    "ppm_set_accel": (C.c_int, [_P, C.c_int32]),
+    "ppm_scene_parse": (C.c_int, [C.c_char_p, C.c_void_p, C.POINTER(C.c_int32), C.c_void_p, C.POINTER(C.c_int32),
+                                  C.c_void_p, C.POINTER(C.c_int32)]),
+    "ppm_camera_parse": (C.c_int, [C.c_char_p, C.c_void_p, C.POINTER(C.c_int64)]),
+    "ppm_parse_error": (C.c_char_p, []),
+    "ppm_accel_info": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "ppm_photonmap_regrid_f32": (C.c_int, [_P, C.c_double]),
+    "ppm_photonmap_tune_f32": (C.c_int, [_P, _fp, _fp, C.c_int64, _dp, _dp, _dp]),
     "ppm_render": (C.c_int, [_P, C.POINTER(S.RenderCfg), _dp]),
     "ppm_render_begin": (C.c_int, [_P, C.POINTER(S.RenderCfg)]),
     "ppm_render_step": (C.c_int, [_P, C.c_int32]),

@@ -175,7 +175,8 @@ class Context:
                                                      _ptr(wl, C.c_uint8), pos.shape[0], float(power),
                                                      float(radius2_max)))
 
-    def query_within_f32(self, q, r2):
+    def query_within_f32(self, q, r2, count_only: bool = False):
+        """(offsets, indices); with count_only the offsets alone (sizes of the sets)."""
         q = np.ascontiguousarray(q, np.float32).reshape(-1, 3)
         nq = q.shape[0]
         r2 = np.ascontiguousarray(np.broadcast_to(np.asarray(r2, np.float64), (nq,)))
@@ -183,6 +184,8 @@ class Context:
         tot = C.c_int64()
         self._check(self.lib.ppm_query_within_f32(self.h, _ptr(q, C.c_float), nq, _ptr(r2, C.c_double),
                                                   _ptr(off, C.c_int64), None, 0, C.byref(tot)))
+        if count_only:
+            return off, None
         idx = np.zeros(max(1, tot.value), np.int32)
         self._check(self.lib.ppm_query_within_f32(self.h, _ptr(q, C.c_float), nq, _ptr(r2, C.c_double),
                                                   _ptr(off, C.c_int64), _ptr(idx, C.c_int32), idx.size,
@@ -198,6 +201,29 @@ class Context:
         self._check(self.lib.ppm_estimate_f32(self.h, _ptr(pos, C.c_float), _ptr(nrm, C.c_float), nq,
                                               _ptr(r2, C.c_double), _ptr(rgb, C.c_double)))
         return rgb
+
+    def set_accel(self, mode: int):
+        """0 automatic (BVH from 32 bounded objects), 1 BVH, 2 loop over the objects."""
+        self._check(self.lib.ppm_set_accel(self.h, int(mode)))
+
+    def accel_info(self) -> dict:
+        m, u = C.c_int32(), C.c_int32()
+        self._check(self.lib.ppm_accel_info(self.h, C.byref(m), C.byref(u)))
+        return dict(bvh_objects=m.value, unbounded=u.value)
+
+    def regrid_photonmap_f32(self, cells_per_radius: float):
+        self._check(self.lib.ppm_photonmap_regrid_f32(self.h, float(cells_per_radius)))
+
+    def tune_photonmap_f32(self, pos, nrm, r2):
+        """Picks the FP32 map's cell size for these queries; returns (cells per radius, ms)."""
+        pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+        nrm = np.ascontiguousarray(nrm, np.float32).reshape(-1, 3)
+        nq = pos.shape[0]
+        r2 = np.ascontiguousarray(np.broadcast_to(np.asarray(r2, np.float64), (nq,)))
+        best, ms = C.c_double(), C.c_double()
+        self._check(self.lib.ppm_photonmap_tune_f32(self.h, _ptr(pos, C.c_float), _ptr(nrm, C.c_float), nq,
+                                                    _ptr(r2, C.c_double), C.byref(best), C.byref(ms)))
+        return best.value, ms.value
 
     # -- progressive render ------------------------------------------------------------
     def _image_shape(self):

@@ -20,6 +20,8 @@ UNITS = {
     "k_f64.cu": ["--fmad=false"],
     "k_f32.cu": [],
     "k_grid.cu": [],
+    "k_bvh.cu": [],
+    "scene_file.cpp": [],
     "ppm_api.cu": [],
 }
 
@@ -41,7 +43,7 @@ def _sources_mtime() -> float:
 
 def _compile(unit: str, extra, verbose_ptxas: bool) -> str:
     src = os.path.join(CSRC, unit)
-    obj = os.path.join(OUT, unit.replace(".cu", ".o"))
+    obj = os.path.join(OUT, os.path.splitext(unit)[0] + ".o")
     cmd = [nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "--expt-relaxed-constexpr",
            "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
            *extra, "-c", src, "-o", obj]

@@ -13,7 +13,10 @@ void launch_emit_f(const SceneView<float> &sc, const EmitPlan &plan, uint64_t se
 void launch_bounce_f(const SceneView<float> &sc, uint64_t seed, PassState *st, int uc, int level, long long n_level0,
                      RayQueue<float> in, RayQueue<float> out, unsigned long long qcap, PhotonBuf<float> photons,
                      int grid, cudaStream_t s) {
-    k_bounce<float><<<grid, 256, 0, s>>>(sc, seed, st, uc, level, n_level0, in, out, qcap, photons);
+    if (sc.bvh)
+        k_bounce<float, true><<<grid, 256, 0, s>>>(with_bvh(sc), seed, st, uc, level, n_level0, in, out, qcap, photons);
+    else
+        k_bounce<float, false><<<grid, 256, 0, s>>>(sc, seed, st, uc, level, n_level0, in, out, qcap, photons);
 }
 void launch_bbox_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s) {
     k_bbox<float><<<grid, 256, 0, s>>>(buf, st, n_fixed);
@@ -29,12 +32,17 @@ void launch_scatter_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, co
 void launch_eye_level_f(const SceneView<float> &sc, const DCamera<float> &cam, uint64_t seed, PassState *st, int uc,
                         int level, EyeQueue<float> in, EyeQueue<float> out, unsigned long long qcap,
                         HitPoint<float> *hits, EyeOut<float> pix, int grid, cudaStream_t s) {
-    k_eye_level<float><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
+    if (sc.bvh)
+        k_eye_level_bvh<float><<<grid, 128, 0, s>>>(with_bvh(sc), cam, seed, st, uc, level, in, out, qcap, hits, pix);
+    else
+        k_eye_level<float><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
 }
 void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
                      const uint32_t *start, double pw, const double *q_r2, int pfilter, int mode, GatherOutF out,
                      int grid, cudaStream_t s) {
-    if (q_r2)
+    if (q_r2 && out.count)
+        k_gather_f<true, true><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pw, q_r2, pfilter, mode, out);
+    else if (q_r2)
         k_gather_f<false, true><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pw, q_r2, pfilter, mode, out);
     else if (out.count)
         k_gather_f<true, false><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pw, q_r2, pfilter, mode, out);
@@ -50,10 +58,22 @@ void launch_make_queries_f(const float *pos, const float *nrm, long long n, HitP
     if (n <= 0) return;
     k_make_queries<float><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(pos, nrm, n, hits);
 }
+void launch_query_sort_f(const float *pos, const float *nrm, const double *r2, long long n, PassState *st,
+                         uint32_t *count, uint32_t *block_sums, uint32_t *qstart, long long cell_cap, uint2 *keyrank,
+                         HitPoint<float> *hits, double *r2_sorted, int grid, cudaStream_t s) {
+    if (n <= 0) return;
+    k_query_hist<<<grid, 256, 0, s>>>(pos, n, st, count, keyrank);
+    launch_scan(count, st, block_sums, qstart, cell_cap, s);
+    k_query_place<<<grid, 256, 0, s>>>(pos, nrm, r2, n, qstart, keyrank, hits, r2_sorted);
+}
 void launch_intersect_f(const SceneView<float> &sc, const double *rays, long long n, double *t, int32_t *obj,
                         cudaStream_t s) {
     if (n <= 0) return;
-    k_intersect<float><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(sc, rays, n, t, obj, nullptr);
+    const unsigned g = (unsigned)((n + 127) / 128);
+    if (sc.bvh)
+        k_intersect<float, true><<<g, 128, 0, s>>>(with_bvh(sc), rays, n, t, obj, nullptr);
+    else
+        k_intersect<float, false><<<g, 128, 0, s>>>(sc, rays, n, t, obj, nullptr);
 }
 
 __global__ void k_pack_photons(const float *pos, const float *dir, const uint8_t *wl, long long n, float4 *raw) {

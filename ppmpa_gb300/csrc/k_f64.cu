@@ -13,7 +13,10 @@ void launch_emit_d(const SceneView<double> &sc, const EmitPlan &plan, uint64_t s
 void launch_bounce_d(const SceneView<double> &sc, uint64_t seed, PassState *st, int uc, int level, long long n_level0,
                      RayQueue<double> in, RayQueue<double> out, unsigned long long qcap, PhotonBuf<double> photons,
                      int grid, cudaStream_t s) {
-    k_bounce<double><<<grid, 256, 0, s>>>(sc, seed, st, uc, level, n_level0, in, out, qcap, photons);
+    if (sc.bvh)
+        k_bounce<double, true><<<grid, 256, 0, s>>>(with_bvh(sc), seed, st, uc, level, n_level0, in, out, qcap, photons);
+    else
+        k_bounce<double, false><<<grid, 256, 0, s>>>(sc, seed, st, uc, level, n_level0, in, out, qcap, photons);
 }
 void launch_bbox_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s) {
     k_bbox<double><<<grid, 256, 0, s>>>(buf, st, n_fixed);
@@ -29,7 +32,10 @@ void launch_scatter_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, c
 void launch_eye_level_d(const SceneView<double> &sc, const DCamera<double> &cam, uint64_t seed, PassState *st, int uc,
                         int level, EyeQueue<double> in, EyeQueue<double> out, unsigned long long qcap,
                         HitPoint<double> *hits, EyeOut<double> pix, int grid, cudaStream_t s) {
-    k_eye_level<double><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
+    if (sc.bvh)
+        k_eye_level_bvh<double><<<grid, 128, 0, s>>>(with_bvh(sc), cam, seed, st, uc, level, in, out, qcap, hits, pix);
+    else
+        k_eye_level<double><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
 }
 void launch_gather_d(const HitPoint<double> *hits, PassState *st, long long n_fixed, const double4 *spos,
                      const double4 *sdir, const uint32_t *start, double pw, int pfilter, int mode, GatherOutD out,
@@ -48,7 +54,11 @@ void launch_make_queries_d(const double *pos, const double *nrm, long long n, Hi
 void launch_intersect_d(const SceneView<double> &sc, const double *rays, long long n, double *t, int32_t *obj,
                         double *nrm, cudaStream_t s) {
     if (n <= 0) return;
-    k_intersect<double><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(sc, rays, n, t, obj, nrm);
+    const unsigned g = (unsigned)((n + 127) / 128);
+    if (sc.bvh)
+        k_intersect<double, true><<<g, 128, 0, s>>>(with_bvh(sc), rays, n, t, obj, nrm);
+    else
+        k_intersect<double, false><<<g, 128, 0, s>>>(sc, rays, n, t, obj, nrm);
 }
 
 }  // namespace ppm

@@ -16,6 +16,7 @@ __global__ void k_pass_begin(PassState *st) {
     st->in_radius = 0;
     st->slots = 0;
     st->rows = 0;
+    st->gather_next = 0;
     for (int l = 0; l < MAX_TRACE + 2; l++) {
         st->qn[l] = 0;
         st->eq[l] = 0;

@@ -26,11 +26,15 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
-constexpr int N_STAGES = 5;
-const char *STAGE_NAMES[N_STAGES] = {"photon_trace", "map_build", "eye_trace", "gather", "accumulate"};
+// stages 0-4 are timed per render pass; map_build, gather and query_sort are
+// also timed by the FP32 map entry points (photon map build, estimate)
+constexpr int N_RENDER_STAGES = 5;
+constexpr int N_STAGES = 6;
+const char *STAGE_NAMES[N_STAGES] = {"photon_trace", "map_build", "eye_trace", "gather", "accumulate", "query_sort"};
 constexpr int TIMING_SLOTS = 256;
 constexpr int HITS_PER_PIXEL = 8;
 constexpr long long CELL_CAP = 1LL << 24;
+constexpr int BVH_MIN_OBJECTS = 32;   // below this a loop over the objects is faster
 
 thread_local std::string g_create_error;
 
@@ -49,6 +53,9 @@ struct ppm_ctx {
     std::vector<ppm_material> mats;
     std::vector<ppm_light> lights;
     DevBuf objs_d, mats_d, lights_d, objs_f, mats_f, lights_f;
+    DevBuf bvh_nodes, bvh_bounded, bvh_unb;   // hierarchy over the bounded objects
+    int accel_mode = 0;                        // PPM_ACCEL_*
+    int bvh_m = 0;                             // objects in the hierarchy (0: none)
     SceneView<double> sv_d{};
     SceneView<float> sv_f{};
     const SceneView<double> &sv_of(double) const { return sv_d; }
@@ -73,11 +80,13 @@ struct ppm_ctx {
     DevBuf pass_direct32, pass_gather32;   // FP32 path per-pass buffers
     long long npx = 0;
     DevBuf scratch;   // parity entry-point staging
+    DevBuf qstart;    // estimate queries: cell starts of the query sort
 
     // parity photon map
     int map_kind = 0;  // 0 none, 1 f64, 2 f32
     long long map_n = 0;
     double map_pw = 0.0, map_r2 = 0.0;
+    double map_cells = 2.0;   // FP32 map: grid cells per maximum query radius
     int last_trace_uc = 1;
     double last_trace_pw = 0.0;
 
@@ -96,6 +105,7 @@ struct ppm_ctx {
     bool count_gather = false;
     cudaEvent_t tev[TIMING_SLOTS][8];
     bool tev_made = false;
+    cudaEvent_t xev[4];   // FP32 map entry points: build / sort / gather brackets
     int slot_head = 0, slot_pending = 0;
     double stage_ms[16] = {0};
     long long stage_calls[16] = {0};
@@ -323,6 +333,14 @@ static int read_state(ppm_ctx *ctx, PassState &h) {
     return PPM_OK;
 }
 
+static int add_stage_time(ppm_ctx *ctx, int stage, cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, a, b));
+    ctx->stage_ms[stage] += ms;
+    ctx->stage_calls[stage] += 1;
+    return PPM_OK;
+}
+
 static int ensure_grid(ppm_ctx *ctx) {
     if (ctx->count.bytes == 0) {
         TRY(ensure(ctx, ctx->count, sizeof(uint32_t) * CELL_CAP));
@@ -443,14 +461,17 @@ extern "C" int ppm_ctx_destroy(ppm_ctx *ctx) {
     DevBuf *bufs[] = {&ctx->objs_d, &ctx->mats_d, &ctx->lights_d, &ctx->objs_f, &ctx->mats_f, &ctx->lights_f,
                       &ctx->raw_d, &ctx->spos, &ctx->sdir, &ctx->raw_f, &ctx->sorted_f, &ctx->sidx,
                       &ctx->keyrank, &ctx->count, &ctx->start, &ctx->block_sums, &ctx->hits_d, &ctx->hits_f,
-                      &ctx->pass_img, &ctx->sum_img, &ctx->scratch, &ctx->pass_direct32, &ctx->pass_gather32};
+                      &ctx->pass_img, &ctx->sum_img, &ctx->scratch, &ctx->pass_direct32, &ctx->pass_gather32,
+                      &ctx->qstart, &ctx->bvh_nodes, &ctx->bvh_bounded, &ctx->bvh_unb};
     for (DevBuf *b : bufs) release(*b);
     for (DevBuf &b : ctx->rq) release(b);
     for (DevBuf &b : ctx->eqb) release(b);
     if (ctx->st) cudaFree(ctx->st);
-    if (ctx->tev_made)
+    if (ctx->tev_made) {
         for (int i = 0; i < TIMING_SLOTS; i++)
             for (int j = 0; j < 8; j++) cudaEventDestroy(ctx->tev[i][j]);
+        for (cudaEvent_t e : ctx->xev) cudaEventDestroy(e);
+    }
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->s) cudaStreamDestroy(ctx->s);
@@ -471,6 +492,47 @@ extern "C" int ppm_ctx_sync(ppm_ctx *ctx) {
 // ---------------------------------------------------------------------------
 // scene and camera
 // ---------------------------------------------------------------------------
+// Objects reached through the hierarchy: spheres, triangles, parallelograms.
+// Infinite planes are tested on every ray; points are never hit.
+static bool bounded_shape(int shape) {
+    return shape == PPM_SHAPE_SPHERE || shape == PPM_SHAPE_POLYGON || shape == PPM_SHAPE_PARALLELOGRAM;
+}
+
+static int build_accel(ppm_ctx *ctx) {
+    std::vector<int32_t> bounded, unb;
+    for (int i = 0; i < (int)ctx->objs.size(); i++) {
+        if (bounded_shape(ctx->objs[i].shape)) bounded.push_back(i);
+        else if (ctx->objs[i].shape == PPM_SHAPE_PLAIN) unb.push_back(i);
+    }
+    const int m = (int)bounded.size();
+    const bool use = ctx->accel_mode == PPM_ACCEL_BVH ? m >= 2
+                   : ctx->accel_mode == PPM_ACCEL_NONE ? false : m >= BVH_MIN_OBJECTS;
+    ctx->sv_d.bvh = nullptr; ctx->sv_d.unb = nullptr; ctx->sv_d.n_unb = 0; ctx->sv_d.bvh_root = 0; ctx->sv_d.bvh_steps = 0;
+    ctx->sv_f.bvh = nullptr; ctx->sv_f.unb = nullptr; ctx->sv_f.n_unb = 0; ctx->sv_f.bvh_root = 0; ctx->sv_f.bvh_steps = 0;
+    ctx->bvh_m = 0;
+    if (!use) return PPM_OK;
+    if (m > (1 << 28)) return set_err(ctx, PPM_ERR_INVALID_ARG, "at most 2^28 bounded objects");
+    TRY(upload_vec(ctx, ctx->bvh_bounded, bounded));
+    if (!unb.empty()) TRY(upload_vec(ctx, ctx->bvh_unb, unb));
+    TRY(ensure(ctx, ctx->bvh_nodes, sizeof(BvhNode) * (size_t)(m - 1)));
+    DevBuf scratch;
+    if (cudaMalloc(&scratch.p, sizeof(uint32_t) * (size_t)bvh_scratch_words(m)) != cudaSuccess)
+        return set_err(ctx, PPM_ERR_OOM, "no device memory for the BVH build of %d objects", m);
+    launch_bvh_build(as<DObject<double>>(ctx->objs_d), as<int32_t>(ctx->bvh_bounded), m, as<BvhNode>(ctx->bvh_nodes),
+                     as<uint32_t>(scratch), ctx->s);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->s);
+    cudaFree(scratch.p);
+    if (e != cudaSuccess) return set_err(ctx, PPM_ERR_CUDA, "BVH build: %s", cudaGetErrorString(e));
+    const BvhNode *nodes = as<BvhNode>(ctx->bvh_nodes);
+    const int32_t *u = unb.empty() ? nullptr : as<int32_t>(ctx->bvh_unb);
+    const int32_t steps = 2 * m + 64;
+    ctx->sv_d.bvh = nodes; ctx->sv_d.unb = u; ctx->sv_d.n_unb = (int32_t)unb.size(); ctx->sv_d.bvh_steps = steps;
+    ctx->sv_f.bvh = nodes; ctx->sv_f.unb = u; ctx->sv_f.n_unb = (int32_t)unb.size(); ctx->sv_f.bvh_steps = steps;
+    ctx->bvh_m = m;
+    return PPM_OK;
+}
+
 extern "C" int ppm_scene_upload(ppm_ctx *ctx, const ppm_object *objs, int32_t n_objs, const ppm_material *mats,
                                 int32_t n_mats, const ppm_light *lights, int32_t n_lights) {
     if (!ctx) return PPM_ERR_INVALID_ARG;
@@ -482,9 +544,13 @@ extern "C" int ppm_scene_upload(ppm_ctx *ctx, const ppm_object *objs, int32_t n_
         if (objs[i].material < 0 || objs[i].material >= n_mats || objs[i].shape < 0 || objs[i].shape > 4)
             return set_err(ctx, PPM_ERR_INVALID_ARG, "object %d: bad material index %d or shape %d", i,
                            objs[i].material, objs[i].shape);
-    for (int i = 0; i < n_lights; i++)
-        if (lights[i].kind < 0 || lights[i].kind > 2)
+    for (int i = 0; i < n_lights; i++) {
+        if (lights[i].kind < 0 || lights[i].kind > PPM_LIGHT_SPOT)
             return set_err(ctx, PPM_ERR_INVALID_ARG, "light %d: bad kind %d", i, lights[i].kind);
+        if (lights[i].kind == PPM_LIGHT_SPOT && !(lights[i].dir1[0] >= -1.0 && lights[i].dir1[0] <= 1.0))
+            return set_err(ctx, PPM_ERR_INVALID_ARG, "light %d: spot cos(half-angle) %g outside [-1, 1]", i,
+                           lights[i].dir1[0]);
+    }
     cudaSetDevice(ctx->device);
     ctx->objs.assign(objs, objs + n_objs);
     ctx->mats.assign(mats, mats + n_mats);
@@ -509,12 +575,29 @@ extern "C" int ppm_scene_upload(ppm_ctx *ctx, const ppm_object *objs, int32_t n_
     TRY(upload_vec(ctx, ctx->lights_f, lf));
     CK(cudaStreamSynchronize(ctx->s));
     ctx->sv_d = SceneView<double>{as<DObject<double>>(ctx->objs_d), as<DMaterial<double>>(ctx->mats_d),
-                                  as<DLight<double>>(ctx->lights_d), n_objs, n_mats, n_lights, 0};
+                                  as<DLight<double>>(ctx->lights_d), n_objs, n_mats, n_lights, 0, nullptr, nullptr, 0, 0};
     ctx->sv_f = SceneView<float>{as<DObject<float>>(ctx->objs_f), as<DMaterial<float>>(ctx->mats_f),
-                                 as<DLight<float>>(ctx->lights_f), n_objs, n_mats, n_lights, 0};
+                                 as<DLight<float>>(ctx->lights_f), n_objs, n_mats, n_lights, 0, nullptr, nullptr, 0, 0};
     ctx->have_scene = true;
     ctx->render_ready = false;
     drop_graph(ctx);
+    return build_accel(ctx);
+}
+
+extern "C" int ppm_set_accel(ppm_ctx *ctx, int32_t mode) {
+    if (!ctx || mode < PPM_ACCEL_AUTO || mode > PPM_ACCEL_NONE) return PPM_ERR_INVALID_ARG;
+    ctx->accel_mode = mode;
+    if (!ctx->have_scene) return PPM_OK;
+    cudaSetDevice(ctx->device);
+    ctx->render_ready = false;
+    drop_graph(ctx);
+    return build_accel(ctx);
+}
+
+extern "C" int ppm_accel_info(ppm_ctx *ctx, int32_t *bvh_objects, int32_t *unbounded) {
+    if (!ctx) return PPM_ERR_INVALID_ARG;
+    if (bvh_objects) *bvh_objects = ctx->bvh_m;
+    if (unbounded) *unbounded = ctx->sv_d.n_unb;
     return PPM_OK;
 }
 
@@ -879,6 +962,24 @@ extern "C" int ppm_estimate_noalloc(ppm_ctx *ctx, const double *pos, const doubl
 // ---------------------------------------------------------------------------
 // FP32 photon map (gather sweep)
 // ---------------------------------------------------------------------------
+// Sorts the packed photons in raw_f into cells of r_max / k (bounds, cell
+// histogram, scan, scatter); the map's original order stays in raw_f, so the
+// grid can be rebuilt with another k without the host arrays.
+static int grid_map_f32(ppm_ctx *ctx, long long n, double r2max, double k) {
+    PhotonBuf<float> pb{as<float4>(ctx->raw_f), as<float4>(ctx->sorted_f), as<int32_t>(ctx->sidx)};
+    TRY(upload_state(ctx, r2max, 0, 0.0, 1, k, n, 0));
+    launch_pass_begin(ctx->st, ctx->s);
+    int g = grid_blocks(ctx, 4);
+    launch_bbox_f(pb, ctx->st, n, g, ctx->s);
+    launch_grid_setup(ctx->st, r2max, ctx->s);
+    launch_hist_f(pb, ctx->st, n, as<uint32_t>(ctx->count), as<uint2>(ctx->keyrank), g, ctx->s);
+    launch_scan(as<uint32_t>(ctx->count), ctx->st, as<uint32_t>(ctx->block_sums), as<uint32_t>(ctx->start), CELL_CAP,
+                ctx->s);
+    launch_scatter_f(pb, ctx->st, n, as<uint32_t>(ctx->start), as<uint2>(ctx->keyrank), g, ctx->s);
+    CK(cudaGetLastError());
+    return PPM_OK;
+}
+
 extern "C" int ppm_photonmap_build_f32(ppm_ctx *ctx, const float *pos, const float *dir, const uint8_t *wl, int64_t n,
                                        double power, double radius2_max) {
     if (!ctx || n < 0 || (n && (!pos || !dir || !wl)) || !(radius2_max > 0.0)) return PPM_ERR_INVALID_ARG;
@@ -901,22 +1002,25 @@ extern "C" int ppm_photonmap_build_f32(ppm_ctx *ctx, const float *pos, const flo
         CK(cudaMemcpyAsync(d_wl, wl, n, cudaMemcpyHostToDevice, ctx->s));
     }
     launch_pack_photons_f(d_pos, d_dir, d_wl, n, as<float4>(ctx->raw_f), ctx->s);
-    PhotonBuf<float> pb{as<float4>(ctx->raw_f), as<float4>(ctx->sorted_f), as<int32_t>(ctx->sidx)};
-    TRY(upload_state(ctx, radius2_max, 0, 0.0, 1, 2.0, n, 0));
-    launch_pass_begin(ctx->st, ctx->s);
-    int g = grid_blocks(ctx, 4);
-    launch_bbox_f(pb, ctx->st, n, g, ctx->s);
-    launch_grid_setup(ctx->st, radius2_max, ctx->s);
-    launch_hist_f(pb, ctx->st, n, as<uint32_t>(ctx->count), as<uint2>(ctx->keyrank), g, ctx->s);
-    launch_scan(as<uint32_t>(ctx->count), ctx->st, as<uint32_t>(ctx->block_sums), as<uint32_t>(ctx->start), CELL_CAP,
-                ctx->s);
-    launch_scatter_f(pb, ctx->st, n, as<uint32_t>(ctx->start), as<uint2>(ctx->keyrank), g, ctx->s);
-    CK(cudaGetLastError());
+    if (ctx->timing) CK(cudaEventRecord(ctx->xev[0], ctx->s));
+    TRY(grid_map_f32(ctx, n, radius2_max, ctx->map_cells));
+    if (ctx->timing) CK(cudaEventRecord(ctx->xev[1], ctx->s));
     CK(cudaStreamSynchronize(ctx->s));
+    if (ctx->timing) TRY(add_stage_time(ctx, 1, ctx->xev[0], ctx->xev[1]));
     ctx->map_kind = 2;
     ctx->map_n = n;
     ctx->map_pw = power;
     ctx->map_r2 = radius2_max;
+    return PPM_OK;
+}
+
+extern "C" int ppm_photonmap_regrid_f32(ppm_ctx *ctx, double cells_per_radius) {
+    if (!ctx || !(cells_per_radius >= 0.5 && cells_per_radius <= 8.0)) return PPM_ERR_INVALID_ARG;
+    if (ctx->map_kind != 2) return set_err(ctx, PPM_ERR_NOT_READY, "no FP32 photon map built");
+    cudaSetDevice(ctx->device);
+    TRY(grid_map_f32(ctx, ctx->map_n, ctx->map_r2, cells_per_radius));
+    CK(cudaStreamSynchronize(ctx->s));
+    ctx->map_cells = cells_per_radius;
     return PPM_OK;
 }
 
@@ -944,31 +1048,124 @@ extern "C" int ppm_query_within_f32(ppm_ctx *ctx, const float *q, int64_t nq, co
                        });
 }
 
+// Device staging of an FP32 estimate batch in the scratch buffer.
+struct EstBatch {
+    float *p, *n;
+    double *r2, *r2s, *o;
+    HitPoint<float> *h;
+    uint2 *kr;
+};
+
+static int stage_estimate_f32(ppm_ctx *ctx, const float *pos, const float *nrm, int64_t nq, const double *r2,
+                              EstBatch &b) {
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t pb = al(sizeof(float) * 3 * nq), hb = al(sizeof(HitPoint<float>) * nq);
+    const size_t rb = al(sizeof(double) * nq), kb = al(sizeof(uint2) * nq), ob = sizeof(double) * 3 * nq;
+    TRY(ensure(ctx, ctx->scratch, 2 * pb + hb + 2 * rb + kb + ob + 256));
+    TRY(ensure(ctx, ctx->qstart, sizeof(uint32_t) * (CELL_CAP + 1)));
+    char *base = as<char>(ctx->scratch);
+    b.p = (float *)base;
+    b.n = (float *)(base + pb);
+    b.h = (HitPoint<float> *)(base + 2 * pb);
+    b.r2 = (double *)(base + 2 * pb + hb);
+    b.r2s = (double *)(base + 2 * pb + hb + rb);
+    b.kr = (uint2 *)(base + 2 * pb + hb + 2 * rb);
+    b.o = (double *)(base + 2 * pb + hb + 2 * rb + kb);
+    CK(cudaMemcpyAsync(b.p, pos, sizeof(float) * 3 * nq, cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(b.n, nrm, sizeof(float) * 3 * nq, cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(b.r2, r2, sizeof(double) * nq, cudaMemcpyHostToDevice, ctx->s));
+    return PPM_OK;
+}
+
+// Queries are sorted by map cell on the device before the gather (see
+// k_query_hist), so results land in the caller's order whatever the order of
+// the gather.  e0/e1/e2 (optional) bracket the sort and the gather.
+static int run_estimate_f32(ppm_ctx *ctx, const EstBatch &b, int64_t nq, bool count, cudaEvent_t e0, cudaEvent_t e1,
+                            cudaEvent_t e2) {
+    if (e0) CK(cudaEventRecord(e0, ctx->s));
+    launch_query_sort_f(b.p, b.n, b.r2, nq, ctx->st, as<uint32_t>(ctx->count), as<uint32_t>(ctx->block_sums),
+                        as<uint32_t>(ctx->qstart), CELL_CAP, b.kr, b.h, b.r2s, grid_blocks(ctx, 8), ctx->s);
+    GatherOutF go{nullptr, b.o, nullptr};
+    if (count) {
+        CK(cudaMemsetAsync(&ctx->st->candidates, 0, 3 * sizeof(unsigned long long), ctx->s));
+        go.count = &ctx->st->candidates;
+    }
+    CK(cudaMemsetAsync(&ctx->st->gather_next, 0, sizeof(unsigned long long), ctx->s));
+    if (e1) CK(cudaEventRecord(e1, ctx->s));
+    launch_gather_f(b.h, ctx->st, nq, as<float4>(ctx->sorted_f), as<uint32_t>(ctx->start), ctx->map_pw, b.r2s, PF_NONE,
+                    1, go, grid_blocks(ctx, 8), ctx->s);
+    CK(cudaGetLastError());
+    if (e2) CK(cudaEventRecord(e2, ctx->s));
+    return PPM_OK;
+}
+
 extern "C" int ppm_estimate_f32(ppm_ctx *ctx, const float *pos, const float *nrm, int64_t nq, const double *r2,
                                 double *rgb) {
     if (!ctx || nq < 0 || (nq && (!pos || !nrm || !r2 || !rgb))) return PPM_ERR_INVALID_ARG;
     if (ctx->map_kind != 2) return set_err(ctx, PPM_ERR_NOT_READY, "no FP32 photon map built");
+    if (nq > 0x7fffffffLL) return set_err(ctx, PPM_ERR_INVALID_ARG, "at most 2^31-1 queries per call");
     TRY(check_r2(ctx, r2, nq));
     if (nq == 0) return PPM_OK;
     cudaSetDevice(ctx->device);
-    size_t pb = (sizeof(float) * 3 * nq + 15) & ~(size_t)15, hb = sizeof(HitPoint<float>) * nq;
-    size_t rb = sizeof(double) * nq, ob = sizeof(double) * 3 * nq;
-    TRY(ensure(ctx, ctx->scratch, 2 * pb + hb + rb + ob + 256));
-    char *base = as<char>(ctx->scratch);
-    float *d_p = (float *)base, *d_n = (float *)(base + pb);
-    HitPoint<float> *d_h = (HitPoint<float> *)(base + 2 * pb);
-    double *d_r2 = (double *)(base + 2 * pb + hb);
-    double *d_o = (double *)(base + 2 * pb + hb + rb);
-    CK(cudaMemcpyAsync(d_p, pos, sizeof(float) * 3 * nq, cudaMemcpyHostToDevice, ctx->s));
-    CK(cudaMemcpyAsync(d_n, nrm, sizeof(float) * 3 * nq, cudaMemcpyHostToDevice, ctx->s));
-    CK(cudaMemcpyAsync(d_r2, r2, rb, cudaMemcpyHostToDevice, ctx->s));
-    launch_make_queries_f(d_p, d_n, nq, d_h, ctx->s);
-    GatherOutF go{nullptr, d_o, nullptr};
-    launch_gather_f(d_h, ctx->st, nq, as<float4>(ctx->sorted_f), as<uint32_t>(ctx->start), ctx->map_pw, d_r2, PF_NONE,
-                    1, go, grid_blocks(ctx, 8), ctx->s);
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(rgb, d_o, ob, cudaMemcpyDeviceToHost, ctx->s));
+    EstBatch b;
+    TRY(stage_estimate_f32(ctx, pos, nrm, nq, r2, b));
+    const bool t = ctx->timing;
+    TRY(run_estimate_f32(ctx, b, nq, ctx->count_gather, t ? ctx->xev[0] : nullptr, t ? ctx->xev[1] : nullptr,
+                         t ? ctx->xev[2] : nullptr));
+    CK(cudaMemcpyAsync(rgb, b.o, sizeof(double) * 3 * nq, cudaMemcpyDeviceToHost, ctx->s));
     CK(cudaStreamSynchronize(ctx->s));
+    if (t) {
+        TRY(add_stage_time(ctx, 5, ctx->xev[0], ctx->xev[1]));
+        TRY(add_stage_time(ctx, 3, ctx->xev[1], ctx->xev[2]));
+    }
+    return PPM_OK;
+}
+
+// Gather cell-size autotuner: re-grids the map with each candidate number of
+// cells per maximum radius, times sort + gather of the sample on the device
+// (best of three), and keeps the fastest grid.  Smaller cells cut the
+// candidates a query tests; larger cells cut rows and scan overhead and fit
+// clustered maps whose dense cells would otherwise hit the cell cap.
+extern "C" int ppm_photonmap_tune_f32(ppm_ctx *ctx, const float *pos, const float *nrm, int64_t nq, const double *r2,
+                                      double *best_cells, double *best_ms) {
+    if (!ctx || nq <= 0 || !pos || !nrm || !r2) return PPM_ERR_INVALID_ARG;
+    if (ctx->map_kind != 2) return set_err(ctx, PPM_ERR_NOT_READY, "no FP32 photon map built");
+    if (nq > 0x7fffffffLL) return set_err(ctx, PPM_ERR_INVALID_ARG, "at most 2^31-1 queries");
+    TRY(check_r2(ctx, r2, nq));
+    cudaSetDevice(ctx->device);
+    cudaEvent_t e[2];
+    CK(cudaEventCreate(&e[0]));
+    if (cudaEventCreate(&e[1]) != cudaSuccess) {
+        cudaEventDestroy(e[0]);
+        return set_err(ctx, PPM_ERR_CUDA, "cudaEventCreate failed");
+    }
+    const double cand[] = {1.0, 1.5, 2.0, 3.0, 4.0};
+    double best = ctx->map_cells, best_t = 1e30;
+    int rc = PPM_OK;
+    EstBatch b;
+    rc = stage_estimate_f32(ctx, pos, nrm, nq, r2, b);
+    for (double k : cand) {
+        if (rc != PPM_OK) break;
+        if ((rc = grid_map_f32(ctx, ctx->map_n, ctx->map_r2, k)) != PPM_OK) break;
+        float t = 1e30f;
+        for (int rep = 0; rep < 3 && rc == PPM_OK; rep++) {
+            if ((rc = run_estimate_f32(ctx, b, nq, false, e[0], nullptr, e[1])) != PPM_OK) break;
+            float ms = 0.0f;
+            cudaError_t ce = cudaEventSynchronize(e[1]);
+            if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e[0], e[1]);
+            if (ce != cudaSuccess) rc = set_err(ctx, PPM_ERR_CUDA, "tuner timing: %s", cudaGetErrorString(ce));
+            t = std::min(t, ms);
+        }
+        if (rc == PPM_OK && t < best_t) { best_t = t; best = k; }
+    }
+    cudaEventDestroy(e[0]);
+    cudaEventDestroy(e[1]);
+    if (rc != PPM_OK) return rc;
+    TRY(grid_map_f32(ctx, ctx->map_n, ctx->map_r2, best));
+    CK(cudaStreamSynchronize(ctx->s));
+    ctx->map_cells = best;
+    if (best_cells) *best_cells = best;
+    if (best_ms) *best_ms = best_t;
     return PPM_OK;
 }
 
@@ -985,6 +1182,7 @@ extern "C" int ppm_set_stage_timing(ppm_ctx *ctx, int32_t on) {
     if (on && !ctx->tev_made) {
         for (int i = 0; i < TIMING_SLOTS; i++)
             for (int j = 0; j < 8; j++) CK(cudaEventCreate(&ctx->tev[i][j]));
+        for (cudaEvent_t &e : ctx->xev) CK(cudaEventCreate(&e));
         ctx->tev_made = true;
     }
     ctx->timing = on != 0;
@@ -1003,8 +1201,8 @@ static int drain_timing(ppm_ctx *ctx) {
         int slot = (ctx->slot_head - ctx->slot_pending + k + TIMING_SLOTS) % TIMING_SLOTS;
         cudaEvent_t *e = ctx->tev[slot];
         float ms;
-        const int pairs[N_STAGES][2] = {{0, 1}, {1, 2}, {5, 6}, {7, 3}, {3, 4}};
-        for (int st = 0; st < N_STAGES; st++) {
+        const int pairs[N_RENDER_STAGES][2] = {{0, 1}, {1, 2}, {5, 6}, {7, 3}, {3, 4}};
+        for (int st = 0; st < N_RENDER_STAGES; st++) {
             CK(cudaEventElapsedTime(&ms, e[pairs[st][0]], e[pairs[st][1]]));
             ctx->stage_ms[st] += ms;
             ctx->stage_calls[st] += 1;

@@ -28,7 +28,7 @@ constexpr uint32_t TAG_EYE = 0x04000000u;
 
 enum { SH_POINT = 0, SH_PLAIN = 1, SH_SPHERE = 2, SH_POLYGON = 3, SH_PARALLELOGRAM = 4 };
 enum { SF_NOTHING = 0, SF_SIMPLE = 1, SF_TS = 2 };
-enum { LT_POINT = 0, LT_PARALLELOGRAM = 1, LT_SUN = 2 };
+enum { LT_POINT = 0, LT_PARALLELOGRAM = 1, LT_SUN = 2, LT_SPOT = 3 };
 enum { PF_NONE = 0, PF_CONE = 1, PF_GAUSS = 2 };
 
 // ---------------------------------------------------------------------------
@@ -313,14 +313,30 @@ struct DCamera {
     int32_t xreso, yreso, jitter_aa, blur;
 };
 
-template <typename T>
+struct BvhNode;
+
+// Scene tables of one precision.  With a hierarchy (bvh != nullptr) the
+// bounded objects are reached through it and the unbounded ones (infinite
+// planes) are listed in unb; without one every object is tested.
+template <typename T, bool HAS_BVH = false>
 struct SceneView {
     const DObject<T> *objs;
     const DMaterial<T> *mats;
     const DLight<T> *lights;
     int32_t n_objs, n_mats, n_lights;
-    int32_t pad;
+    int32_t bvh_root;          // root node (>= 0), or ~object when one object is bounded
+    const BvhNode *bvh;
+    const int32_t *unb;
+    int32_t n_unb;
+    int32_t bvh_steps;         // bound on one walk: 2 * objects in the tree + 64
 };
+
+// the same tables typed for the kernels that walk the hierarchy
+template <typename T>
+__host__ __device__ inline SceneView<T, true> with_bvh(const SceneView<T, false> &v) {
+    return SceneView<T, true>{v.objs, v.mats, v.lights, v.n_objs, v.n_mats, v.n_lights, v.bvh_root,
+                              v.bvh, v.unb, v.n_unb, v.bvh_steps};
+}
 
 // Emission bookkeeping (src/bin/ppmpa.rs:30-31): light l owns emission
 // indices [first[l], first[l+1]).

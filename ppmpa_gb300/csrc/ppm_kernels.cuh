@@ -49,6 +49,7 @@ struct PassState {
     GridParams grid;
     unsigned long long candidates, in_radius;   // gather counters (valid candidates, hits)
     unsigned long long slots, rows;             // lane slots issued, non-empty rows visited
+    unsigned long long gather_next;             // next query chunk of the FP32 gather
     double cell_factor;
     int64_t cell_cap;
     unsigned long long photon_cap;   // buffers hold at most this many photons
@@ -217,8 +218,8 @@ __global__ void __launch_bounds__(256) k_emit(SceneView<T> sc, EmitPlan plan, ui
 
 // one bounce level of trace_photon (tracer.rs:31-125) for every live ray;
 // continuing rays are compacted into the next level's queue
-template <typename T>
-__global__ void __launch_bounds__(256) k_bounce(SceneView<T> sc, uint64_t seed, PassState *st, int uc, int level,
+template <typename T, bool B>
+__global__ void __launch_bounds__(256) k_bounce(SceneView<T, B> sc, uint64_t seed, PassState *st, int uc, int level,
                                                 long long n_level0, RayQueue<T> in, RayQueue<T> out,
                                                 unsigned long long qcap, PhotonBuf<T> photons) {
     const uint32_t pass = (uint32_t)st->pass;
@@ -413,10 +414,10 @@ template <> struct EyeOut<float> {
     }
 };
 
-template <typename T>
-__global__ void __launch_bounds__(128) k_eye_level(SceneView<T> sc, DCamera<T> cam, uint64_t seed, PassState *st,
-                                                   int uc, int level, EyeQueue<T> in, EyeQueue<T> out,
-                                                   unsigned long long qcap, HitPoint<T> *hits, EyeOut<T> pix) {
+template <typename T, bool B>
+__device__ __forceinline__ void eye_level(const SceneView<T, B> &sc, const DCamera<T> &cam, uint64_t seed,
+                                          PassState *st, int uc, int level, EyeQueue<T> in, EyeQueue<T> out,
+                                          unsigned long long qcap, HitPoint<T> *hits, EyeOut<T> pix) {
     const uint32_t pass = (uint32_t)st->pass;
     const unsigned long long hit_cap = st->hit_cap;
     const long long npx = (long long)cam.xreso * cam.yreso;
@@ -536,6 +537,22 @@ __global__ void __launch_bounds__(128) k_eye_level(SceneView<T> sc, DCamera<T> c
         if (level == 0) pix.set(p, acc);
         else if (any_nz(acc)) pix.add(p, acc);
     }
+}
+
+// Two entry points over the same body: without a hierarchy the compiler's
+// own register choice (no spills, more resident warps); with one, a cap of
+// 128 registers, under which the traversal stack does not spill.
+template <typename T>
+__global__ void __launch_bounds__(128) k_eye_level(SceneView<T, false> sc, DCamera<T> cam, uint64_t seed,
+                                                   PassState *st, int uc, int level, EyeQueue<T> in, EyeQueue<T> out,
+                                                   unsigned long long qcap, HitPoint<T> *hits, EyeOut<T> pix) {
+    eye_level(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
+}
+template <typename T>
+__global__ void __maxnreg__(128) k_eye_level_bvh(SceneView<T, true> sc, DCamera<T> cam, uint64_t seed, PassState *st,
+                                                 int uc, int level, EyeQueue<T> in, EyeQueue<T> out,
+                                                 unsigned long long qcap, HitPoint<T> *hits, EyeOut<T> pix) {
+    eye_level(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
 }
 
 // ---------------------------------------------------------------------------
@@ -806,6 +823,8 @@ struct GatherOutF {
 };
 
 #if defined(PPM_BUILD_F32)
+constexpr unsigned GATHER_CHUNK = 4;   // queries a warp takes per counter increment
+
 // PERQ: per-query radii (the estimate entry point); otherwise the pass radius
 template <bool COUNT, bool PERQ>
 __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed,
@@ -814,9 +833,20 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
     const unsigned long long nq = n_hitpoints(st, n_fixed);
     const GridParams g = st->grid;
     const unsigned lane = lane_id();
-    const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-    for (unsigned long long qi = warp; qi < nq; qi += nwarps) {
+    // Warps take GATHER_CHUNK queries at a time from a counter, so the
+    // queries in flight stay a narrow window of the (cell-ordered) batch and
+    // their photons stay in L2; a fixed warp stride lets slow warps fall
+    // behind and spreads the window over the whole map.
+    unsigned long long qi = 0, qend = 0;
+    for (;;) {
+        if (qi == qend) {
+            unsigned long long c = 0;
+            if (lane == 0) c = atomicAdd(&st->gather_next, (unsigned long long)GATHER_CHUNK);
+            c = __shfl_sync(0xffffffffu, c, 0);
+            if (c >= nq) break;
+            qi = c;
+            qend = c + GATHER_CHUNK < nq ? c + GATHER_CHUNK : nq;
+        }
         const HitPoint<float> h = hits[qi];
         double r2;
         float r2_lo, r2_hi, r2f;
@@ -881,12 +911,45 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
                 atomicAdd(px + 1, h.w[1] * s1);
                 atomicAdd(px + 2, h.w[2] * s2);
             } else {
+                // the estimate entry point gathers its queries in cell order;
+                // h.pixel is the query's slot in the caller's arrays
                 double kk = pw * (ONE_PI_D / r2);
-                out.out_rgb[3 * qi] = (double)s0 * kk;
-                out.out_rgb[3 * qi + 1] = (double)s1 * kk;
-                out.out_rgb[3 * qi + 2] = (double)s2 * kk;
+                double *o = out.out_rgb + 3 * (size_t)h.pixel;
+                o[0] = (double)s0 * kk;
+                o[1] = (double)s1 * kk;
+                o[2] = (double)s2 * kk;
             }
         }
+        ++qi;
+    }
+}
+
+// Estimate queries are gathered in the map's cell order, so that the warps
+// running at the same time walk the same cells and share photons in L2
+// (random query order re-reads the map from HBM once per neighbourhood).
+// k_query_hist ranks each query inside its cell (key 3*cell, the map's key
+// space, so the map's scan sizes apply); k_query_place writes the hit point
+// and its radius to the sorted slot, keeping the caller's index in pixel.
+__global__ void __launch_bounds__(256) k_query_hist(const float *pos, long long n, const PassState *st,
+                                                    uint32_t *count, uint2 *keyrank) {
+    const GridParams g = st->grid;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        uint32_t c = 3u * cell_of(g, ld3(pos + 3 * i));
+        keyrank[i] = make_uint2(c, atomicAdd(&count[c], 1u));
+    }
+}
+
+__global__ void __launch_bounds__(256) k_query_place(const float *pos, const float *nrm, const double *r2, long long n,
+                                                     const uint32_t *start, const uint2 *keyrank,
+                                                     HitPoint<float> *hits, double *r2_sorted) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const uint2 kr = keyrank[i];
+        const uint32_t dst = start[kr.x] + kr.y;
+        HitPoint<float> h;
+        for (int a = 0; a < 3; a++) { h.pos[a] = pos[3 * i + a]; h.nrm[a] = nrm[3 * i + a]; h.w[a] = 1.0f; }
+        h.pixel = (int32_t)i;
+        hits[dst] = h;
+        r2_sorted[dst] = r2[i];
     }
 }
 
@@ -947,8 +1010,8 @@ __global__ void k_make_queries(const T *pos, const T *nrm, long long n, HitPoint
 }
 
 // first-hit parity kernel: calc_intersection for a batch of rays
-template <typename T>
-__global__ void k_intersect(SceneView<T> sc, const double *rays, long long n, double *t, int32_t *obj, double *nrm) {
+template <typename T, bool B>
+__global__ void k_intersect(SceneView<T, B> sc, const double *rays, long long n, double *t, int32_t *obj, double *nrm) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double *r = rays + 6 * i;

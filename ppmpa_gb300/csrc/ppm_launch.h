@@ -52,10 +52,21 @@ void launch_within_f(const float *q, long long nq, const double *q_r2, const Pas
                      const uint32_t *start, const int32_t *sidx, unsigned long long *counts,
                      const unsigned long long *offsets, int32_t *idx_out, int grid, cudaStream_t s);
 void launch_make_queries_f(const float *pos, const float *nrm, long long n, HitPoint<float> *hits, cudaStream_t s);
+// sorts estimate queries by map cell (count -> scan -> place); count is left zeroed
+void launch_query_sort_f(const float *pos, const float *nrm, const double *r2, long long n, PassState *st,
+                         uint32_t *count, uint32_t *block_sums, uint32_t *qstart, long long cell_cap, uint2 *keyrank,
+                         HitPoint<float> *hits, double *r2_sorted, int grid, cudaStream_t s);
 void launch_intersect_f(const SceneView<float> &sc, const double *rays, long long n, double *t, int32_t *obj,
                         cudaStream_t s);
 void launch_pack_photons_f(const float *pos, const float *dir, const uint8_t *wl, long long n, float4 *raw,
                            cudaStream_t s);
+
+// ---- BVH over the bounded objects (k_bvh.cu) --------------------------------------
+// 32-bit words of device scratch launch_bvh_build needs for m objects
+int bvh_scratch_words(int m);
+// builds the m - 1 internal nodes over objs[bounded[0..m)] (m >= 2)
+void launch_bvh_build(const DObject<double> *objs, const int32_t *bounded, int m, BvhNode *nodes, uint32_t *scratch,
+                      cudaStream_t s);
 
 // ---- grid / scan / pass bookkeeping ------------------------------------------------
 constexpr int SCAN_TILE = 4096;

@@ -13,7 +13,14 @@ template <typename T> struct Cst {
     __device__ static constexpr T one_pi() { return T(ONE_PI_D); }
     __device__ static constexpr T sr_half() { return T(SR_HALF_D); }
     __device__ static constexpr T pi4() { return T(PI4_D); }
+    __device__ static T inf() { return T(INFINITY); }
 };
+
+}  // namespace ppm
+
+#include "ppm_bvh.cuh"
+
+namespace ppm {
 
 // ---------------------------------------------------------------------------
 // Shapes: src/ray/geometry.rs:132-202
@@ -90,16 +97,37 @@ struct Isect {
 // calc_intersection, src/tracer.rs:306-350: nearest t >= NEARLY0, the first
 // object in list order among equal t (stable sort); normal flipped to face
 // the ray (io = Out when flipped).
-template <typename T>
-__device__ __forceinline__ bool intersect(const SceneView<T> &sc, V3<T> rp, V3<T> rd, Isect<T> &is) {
+template <typename T, bool B>
+__device__ __forceinline__ bool intersect(const SceneView<T, B> &sc, V3<T> rp, V3<T> rd, Isect<T> &is) {
     T best = T(0);
     int bi = -1;
-    for (int i = 0; i < sc.n_objs; i++) {
-        T ta, tb;
-        const DObject<T> o = load_object(sc.objs, i);
-        int k = shape_distance(o, rp, rd, ta, tb);
-        if (k >= 1 && ta >= Cst<T>::nearly0() && (bi < 0 || ta < best)) { best = ta; bi = i; }
-        if (k == 2 && tb >= Cst<T>::nearly0() && (bi < 0 || tb < best)) { best = tb; bi = i; }
+    if constexpr (!B) {
+        for (int i = 0; i < sc.n_objs; i++) {
+            T ta, tb;
+            const DObject<T> o = load_object(sc.objs, i);
+            int k = shape_distance(o, rp, rd, ta, tb);
+            if (k >= 1 && ta >= Cst<T>::nearly0() && (bi < 0 || ta < best)) { best = ta; bi = i; }
+            if (k == 2 && tb >= Cst<T>::nearly0() && (bi < 0 || tb < best)) { best = tb; bi = i; }
+        }
+    } else {
+        // the list-order rule of the loop above, for any visiting order:
+        // smallest t, then smallest index
+        auto test = [&](int i) {
+            T ta, tb;
+            const DObject<T> o = load_object(sc.objs, i);
+            int k = shape_distance(o, rp, rd, ta, tb);
+            if (k >= 1 && ta >= Cst<T>::nearly0() && (bi < 0 || ta < best || (ta == best && i < bi))) {
+                best = ta;
+                bi = i;
+            }
+            if (k == 2 && tb >= Cst<T>::nearly0() && (bi < 0 || tb < best || (tb == best && i < bi))) {
+                best = tb;
+                bi = i;
+            }
+        };
+        for (int k = 0; k < sc.n_unb; k++) test(sc.unb[k]);
+        bvh_walk<T>(sc.bvh, sc.bvh_root, sc.bvh_steps, rp, rd, test,
+                    [&]() { return bi < 0 ? Cst<T>::inf() : best; });
     }
     if (bi < 0) return false;
     const DObject<T> o = load_object(sc.objs, bi);
@@ -254,7 +282,8 @@ template <typename T> __device__ __forceinline__ T sf_power_glossy(const DMateri
 }
 
 // M_AIR (src/scene.rs:13-18): ior (1,1,1)
-template <typename T> __device__ __forceinline__ const T *ior_of(const SceneView<T> &sc, int m, const T *air) {
+template <typename T, bool B>
+__device__ __forceinline__ const T *ior_of(const SceneView<T, B> &sc, int m, const T *air) {
     return m < 0 ? air : sc.mats[m].ior;
 }
 
@@ -268,6 +297,29 @@ struct PhotonPath {
     uint32_t item;
 };
 
+// Spot light (no reference counterpart: the reference has point,
+// parallelogram and sun lights, light.rs:16-38): a point light whose photons
+// leave uniformly over the solid angle of the cone around axis a with
+// cos(half-angle) cos_cut.  Two draws: u for cos(theta) = 1 - u (1 - cos_cut),
+// then phi in [0, 2 pi); the frame is b1 = normalize(h x a), b2 = a x b1 with
+// h = x unless |a.x| >= 0.9, then y.
+template <typename T>
+__device__ __forceinline__ V3<T> spot_dir(Rng &rg, V3<T> a, T cos_cut) {
+    T u = gen_range<T>(rg, T(0), T(1));
+    T phi = gen_range<T>(rg, T(0), T(2.0 * PI_D));
+    T c = T(1) - u * (T(1) - cos_cut);
+    T s = dsqrt(T(1) - c * c);
+    T sn, cs;
+    Math<T>::sincos_(phi, sn, cs);
+    V3<T> h = (a.x < T(0) ? -a.x : a.x) < T(0.9) ? mk3(T(1), T(0), T(0)) : mk3(T(0), T(1), T(0));
+    V3<T> b1 = mk3(T(1), T(0), T(0));
+    normalize(cross(h, a), b1);
+    V3<T> b2 = cross(a, b1);
+    V3<T> d = a;
+    normalize((b1 * (s * cs) + b2 * (s * sn)) + a * c, d);
+    return d;
+}
+
 template <typename T>
 __device__ __forceinline__ void generate_photon(const DLight<T> &l, Rng &rg, PhotonPath<T> &ph) {
     T p = gen_range<T>(rg, T(0), T(1));
@@ -275,6 +327,9 @@ __device__ __forceinline__ void generate_photon(const DLight<T> &l, Rng &rg, Pho
     if (l.kind == LT_POINT) {
         ph.pos = ld3(l.pos);
         ph.dir = random_dir<T>(rg);
+    } else if (l.kind == LT_SPOT) {
+        ph.pos = ld3(l.pos);
+        ph.dir = spot_dir<T>(rg, ld3(l.dir), l.d1[0]);
     } else {
         T t1 = gen_range<T>(rg, T(0), T(1));
         T t2 = gen_range<T>(rg, T(0), T(1));
@@ -289,8 +344,8 @@ __device__ __forceinline__ void generate_photon(const DLight<T> &l, Rng &rg, Pho
 // One level of trace_photon (tracer.rs:31-125, surface.rs:211-258).
 // Returns true if the path continues (ph updated); `store` / `spos` report
 // whether the incoming photon is stored at this hit (tracer.rs:77-79).
-template <typename T>
-__device__ __forceinline__ bool photon_event(const SceneView<T> &sc, uint64_t seed, uint32_t pass, bool uc,
+template <typename T, bool B>
+__device__ __forceinline__ bool photon_event(const SceneView<T, B> &sc, uint64_t seed, uint32_t pass, bool uc,
                                              PhotonPath<T> &ph, bool &store, V3<T> &spos) {
     store = false;
     Isect<T> is;
@@ -363,14 +418,14 @@ __device__ __forceinline__ bool photon_event(const SceneView<T> &sc, uint64_t se
 template <typename T>
 __device__ __forceinline__ V3<T> light_radiance(const DLight<T> &l, T d) {
     T l0;
-    if (l.kind == LT_POINT) l0 = l.flux / (Cst<T>::pi4() * d);
+    if (l.kind == LT_POINT || l.kind == LT_SPOT) l0 = l.flux / (Cst<T>::pi4() * d);
     else if (l.kind == LT_PARALLELOGRAM) l0 = (T(2) * l.flux * T(PARA_DIV) * T(PARA_DIV)) / (Cst<T>::pi4() * d);
     else l0 = l.flux;
     return mk3(l.color[0] * l0, l.color[1] * l0, l.color[2] * l0);
 }
 
-template <typename T>
-__device__ __forceinline__ bool light_sample(const SceneView<T> &sc, V3<T> p, V3<T> n, V3<T> ld, T &dist2, T &cos2) {
+template <typename T, bool B>
+__device__ __forceinline__ bool light_sample(const SceneView<T, B> &sc, V3<T> p, V3<T> n, V3<T> ld, T &dist2, T &cos2) {
     V3<T> ld3;
     if (!normalize(ld, ld3)) return false;
     T cos0 = dot(n, ld3);
@@ -385,8 +440,8 @@ __device__ __forceinline__ bool light_sample(const SceneView<T> &sc, V3<T> p, V3
     return true;
 }
 
-template <typename T>
-__device__ __forceinline__ V3<T> radiance_from_light(const SceneView<T> &sc, V3<T> p, V3<T> n, const DLight<T> &l) {
+template <typename T, bool B>
+__device__ __forceinline__ V3<T> radiance_from_light(const SceneView<T, B> &sc, V3<T> p, V3<T> n, const DLight<T> &l) {
     V3<T> rad = mk3(T(0), T(0), T(0));
     if (l.kind != LT_PARALLELOGRAM) return rad;   // at most one sample: contributes zero
     const T tss[5] = {T(0.1), T(0.3), T(0.5), T(0.7), T(0.9)};

@@ -24,7 +24,7 @@ D3 = C.c_double * 3
 
 SHAPE_POINT, SHAPE_PLAIN, SHAPE_SPHERE, SHAPE_POLYGON, SHAPE_PARALLELOGRAM = 0, 1, 2, 3, 4
 SURF_NOTHING, SURF_SIMPLE, SURF_TS = 0, 1, 2
-LIGHT_POINT, LIGHT_PARALLELOGRAM, LIGHT_SUN = 0, 1, 2
+LIGHT_POINT, LIGHT_PARALLELOGRAM, LIGHT_SUN, LIGHT_SPOT = 0, 1, 2, 3
 FILTER_NONE, FILTER_CONE, FILTER_GAUSS = 0, 1, 2
 WL_RED, WL_GREEN, WL_BLUE = 0, 1, 2
 
@@ -209,6 +209,16 @@ def parallelogram_light(color, flux, pos, nvec, dir1, dir2) -> Lgt:
                tuple(map(float, nvec)), tuple(map(float, dir1)), tuple(map(float, dir2)))
 
 
+def spot_light(color, flux, pos, axis, half_angle_deg) -> Lgt:
+    """Spot light (no reference counterpart): a point light emitting only into
+    the cone of the given half-angle around axis; the C ABI carries the unit
+    axis in dir and cos(half-angle) in dir1[0]."""
+    a = normalize(tuple(map(float, axis)))
+    cc = math.cos(math.radians(float(half_angle_deg)))
+    return Lgt(LIGHT_SPOT, tuple(map(float, color)), float(flux), tuple(map(float, pos)), (0.0, 0.0, 0.0),
+               (cc, 0.0, 0.0), (0.0, 0.0, 0.0), a)
+
+
 def sun_light(color, flux, pos, nvec, dir1, dir2, direction) -> Lgt:
     return Lgt(LIGHT_SUN, tuple(map(float, color)), float(flux), tuple(map(float, pos)), tuple(map(float, nvec)),
                tuple(map(float, dir1)), tuple(map(float, dir2)), tuple(map(float, direction)))
@@ -222,6 +232,31 @@ class Scene:
     objects: List[tuple] = field(default_factory=list)   # (Shape, material index)
     materials: List[Mat] = field(default_factory=list)
     lights: List[Lgt] = field(default_factory=list)
+    # triangles added in bulk (numpy arrays), placed after `objects`
+    tri_p0: object = None
+    tri_d1: object = None
+    tri_d2: object = None
+    tri_n: object = None
+    tri_mat: object = None
+
+    def add_triangles(self, p0, p1, p2, mats):
+        """Triangles p0 p1 p2 (n x 3 each, counter-clockwise seen from the
+        normal's side) as Shape::new_polygon builds them (geometry.rs:93-103):
+        dir1 = p1 - p0, dir2 = p2 - p0, nvec = normalize(dir1 x dir2)."""
+        import numpy as np
+        p0 = np.ascontiguousarray(p0, np.float64)
+        d1 = np.ascontiguousarray(p1, np.float64) - p0
+        d2 = np.ascontiguousarray(p2, np.float64) - p0
+        n = np.cross(d1, d2)
+        n /= np.linalg.norm(n, axis=1, keepdims=True)
+        mats = np.broadcast_to(np.asarray(mats, np.int32), (len(p0),))
+        cat = (lambda a, b: b if a is None else np.concatenate([a, b]))
+        self.tri_p0, self.tri_d1, self.tri_d2 = cat(self.tri_p0, p0), cat(self.tri_d1, d1), cat(self.tri_d2, d2)
+        self.tri_n, self.tri_mat = cat(self.tri_n, n), cat(self.tri_mat, np.array(mats))
+
+    @property
+    def n_objects(self) -> int:
+        return len(self.objects) + (0 if self.tri_p0 is None else len(self.tri_p0))
 
     def add_material(self, m: Mat) -> int:
         self.materials.append(m)
@@ -232,13 +267,25 @@ class Scene:
         return len(self.objects) - 1
 
     def c_objects(self):
-        arr = (Object * max(1, len(self.objects)))()
+        n = self.n_objects
+        arr = (Object * max(1, n))()
         for i, (s, m) in enumerate(self.objects):
             o = arr[i]
             o.shape, o.material = s.shape, m
             o.position[:], o.nvec[:], o.dir1[:], o.dir2[:] = s.position, s.nvec, s.dir1, s.dir2
             o.dist, o.radius = s.dist, s.radius
-        return arr, len(self.objects)
+        if self.tri_p0 is not None:
+            import numpy as np
+            k = len(self.objects)
+            view = np.frombuffer(arr, dtype=np.dtype({
+                "names": ["shape", "material", "position", "nvec", "dir1", "dir2", "dist", "radius"],
+                "formats": ["<i4", "<i4", ("<f8", 3), ("<f8", 3), ("<f8", 3), ("<f8", 3), "<f8", "<f8"],
+                "offsets": [0, 4, 8, 32, 56, 80, 104, 112], "itemsize": C.sizeof(Object)}))
+            t = view[k:n]
+            t["shape"], t["material"] = SHAPE_POLYGON, self.tri_mat
+            t["position"], t["nvec"], t["dir1"], t["dir2"] = self.tri_p0, self.tri_n, self.tri_d1, self.tri_d2
+            t["dist"], t["radius"] = 0.0, 0.0
+        return arr, n
 
     def c_materials(self):
         arr = (Material * max(1, len(self.materials)))()

@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 from oracle.binding import Oracle
-from ppmpa_gb300 import MIXED, PLAIN, Context, PPMError, RenderConfig, scene as S
+from ppmpa_gb300 import MIXED, PLAIN, Context, PPMError, RenderConfig, scene as S, workloads as W
 
 pytestmark = pytest.mark.gpu
 
@@ -112,6 +112,50 @@ def _photon_cloud(rng, n, clustered=False):
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     wl = rng.integers(0, 3, n).astype(np.uint8)
     return pos, d, wl
+
+
+@pytest.mark.parametrize("clustered", [False, True])
+def test_within_fp64_sets_equal(ctx, clustered):
+    rng = np.random.default_rng(5)
+    pos, d, wl = _photon_cloud(rng, 60000, clustered)
+    R2 = 0.03 ** 2
+    ctx.build_photonmap(pos, d, wl, 0.01, R2)
+    q = np.vstack([rng.random((3000, 3)), pos[rng.integers(0, len(pos), 1000)]])
+    r2 = np.concatenate([np.full(2000, R2), rng.uniform(0, R2, len(q) - 2000)])
+    off, idx = ctx.query_within(q, r2)
+    ooff, oidx = Oracle(S.Scene()).within(pos, q, r2)
+    assert np.array_equal(off, ooff)
+    assert np.array_equal(idx, oidx)
+    assert len(idx) > 10000
+
+
+def test_within_fp64_boundary_equality(ctx):
+    # photons placed exactly at distance^2 == r2 (in f64) are inside (<=)
+    pos = np.array([[0.5, 0.5, 0.5], [0.75, 0.5, 0.5], [0.5, 0.25, 0.5], [0.5, 0.5, 0.8]])
+    d = np.tile([0.0, 0.0, -1.0], (4, 1))
+    wl = np.zeros(4, np.uint8)
+    ctx.build_photonmap(pos, d, wl, 1.0, 0.0625)
+    off, idx = ctx.query_within(np.array([[0.5, 0.5, 0.5]]), 0.0625)
+    assert sorted(idx.tolist()) == [0, 1, 2]
+
+
+def test_estimate_fp64(ctx):
+    rng = np.random.default_rng(6)
+    pos, d, wl = _photon_cloud(rng, 50000)
+    R2 = 0.04 ** 2
+    ctx.build_photonmap(pos, d, wl, 0.002, R2)
+    q = rng.random((4000, 3))
+    n = rng.normal(size=(4000, 3))
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    orc = Oracle(S.Scene())
+    for pf in (S.FILTER_NONE, S.FILTER_CONE, S.FILTER_GAUSS):
+        g = ctx.estimate(q, n, pf)
+        o = orc.estimate(pos, d, wl, q, n, R2, 0.002, pf)
+        assert np.allclose(g, o, rtol=1e-9, atol=1e-12), pf
+        assert (o > 0).mean() > 0.3
+
+
+_oct_roundtrip = W.oct_roundtrip
 
 
 @pytest.mark.parametrize("clustered", [False, True])
