@@ -44,6 +44,9 @@ WORKLOADS = {
 # gather sweep over an FP32 photon map: 100M photons, 4M queries with radii
 # log-uniform over [1e-3, 2e-2] (ppmpa_gb300/workloads.py)
 SWEEPS = {"gather_sweep_uniform": "uniform", "gather_sweep_clustered": "clustered"}
+# 64 seeded render jobs of uneven sizes (ppmpa_gb300/workloads.py batch_jobs),
+# 8 passes each, rendered as one batch (one graph launch per pass for all jobs)
+BATCHES = {"batch_64": dict(n_jobs=64, passes=8)}
 L2_BYTES = 129 * 1024 * 1024
 
 
@@ -60,7 +63,7 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="glass_box_512", choices=list(WORKLOADS) + list(SWEEPS))
+    p.add_argument("--workload", default="glass_box_512", choices=list(WORKLOADS) + list(SWEEPS) + list(BATCHES))
     p.add_argument("--sweep-photons", type=int, default=100_000_000)
     p.add_argument("--sweep-queries", type=int, default=4_000_000)
     p.add_argument("--sweep-cells", type=float, default=0.0,
@@ -73,6 +76,7 @@ def parse():
                    help="only run this many mixed passes (one warm-up) and exit: the profiler's command")
     p.add_argument("--precision", default="mixed", choices=["mixed", "plain"])
     p.add_argument("--cell-factor", type=int, default=0, help="grid cells per radius (0: library default)")
+    p.add_argument("--nphoton", type=int, default=0, help="photons per pass (0: the workload's); for profiling")
     return p.parse_args()
 
 
@@ -516,8 +520,72 @@ def run_sweep_reference(args, kind):
     }), flush=True)
 
 
+def run_batch(args, bw):
+    """A step = one pass of every job.  value: photons of all jobs per second
+    of batch device time; sequential: the same jobs rendered one after
+    another, each with its own pass graph; e2e: Batch.render wall time
+    (scene uploads, BVH builds, cell tuning, graph capture, passes, images)."""
+    import torch
+    from ppmpa_gb300 import Batch, Context, workloads as W
+    jobs = W.batch_jobs(bw["n_jobs"], seed=args.seed + 6, passes=bw["passes"])
+    photons = sum(cfg.nphoton for _, _, cfg in jobs) * bw["passes"]
+    with Batch(0, seed=args.seed) as b:
+        b.render(jobs)                                   # warm-up: allocations, module loads
+        clocks = Clocks(0)
+        clocks.start()
+        t0 = time.perf_counter()
+        imgs, dev_ms = b.render(jobs)
+        wall = time.perf_counter() - t0
+        clk = clocks.stop()
+    seq_ms = 0.0
+    with Context(0, seed=args.seed) as ctx:
+        for sc, cam, cfg in jobs:
+            ctx.upload_scene(sc)
+            ctx.set_camera(cam)
+            ctx.render_begin(cfg)
+            ctx.sync()
+            a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            st = torch.cuda.ExternalStream(ctx.stream)
+            a.record(st)
+            ctx.render_step(cfg.passes)
+            e.record(st)
+            ctx.sync()
+            torch.cuda.synchronize()
+            seq_ms += a.elapsed_time(e)
+    prims = [sc.n_objects for sc, _, _ in jobs]
+    out = {
+        "metric": f"batched render Mphotons/s ({len(jobs)} uneven jobs, one graph launch per pass)",
+        "value": photons / (dev_ms / 1e3) / 1e6, "unit": "Mphotons/s", "n_gpus": 1, "steps": bw["passes"],
+        "warmup": 1, "ms_per_step": dev_ms / bw["passes"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 trace/gather, f64 radius/average", "data": "synthetic (seeded scenes)",
+        "config": {"workload": args.workload, "jobs": len(jobs), "passes": bw["passes"],
+                   "primitives": [min(prims), max(prims), sum(prims)],
+                   "photons_per_pass": [min(c.nphoton for _, _, c in jobs), max(c.nphoton for _, _, c in jobs)],
+                   "reso": [min(c.xreso for _, c, _ in jobs), max(c.xreso for _, c, _ in jobs)],
+                   "cell_tuning": True},
+        "sequential": {"value": photons / (seq_ms / 1e3) / 1e6, "unit": "Mphotons/s", "ms": seq_ms},
+        "batch_over_sequential": seq_ms / dev_ms,
+        "e2e": {"value": photons / wall / 1e6, "unit": "Mphotons/s",
+                "h2d_bytes_per_step": sum(120 * sc.n_objects + 168 * len(sc.materials) + 160 * len(sc.lights) + 336
+                                          for sc, _, _ in jobs),
+                "d2h_bytes_per_step": sum(i.nbytes for i in imgs),
+                "step": "Batch.render: uploads, BVH builds, tuning, capture, all passes, images"},
+        "mean_radiance": float(np.mean([i.mean() for i in imgs])), "clocks": clk,
+    }
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload in BATCHES:
+        if dist_env()[0] == 0 and args.impl != "reference":
+            run_batch(args, BATCHES[args.workload])
+        elif dist_env()[0] == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the batch workload has no CPU leg: the reference "
+                              "tests every object per ray and renders one scene per process"}))
+        return
+    if args.nphoton > 0 and args.workload in WORKLOADS:
+        WORKLOADS[args.workload] = dict(WORKLOADS[args.workload], nphoton=args.nphoton)
     if args.workload in SWEEPS:
         rank, world, _ = dist_env()
         if rank == 0:

@@ -124,8 +124,18 @@ typedef struct ppm_render_cfg {
     int32_t cell_factor;      /* grid cells per radius (1 or 2; 0 = auto) */
     uint64_t seed;
     int32_t first_pass;       /* index of the first pass (for sharded/resumed runs) */
-    int32_t flags;            /* reserved, 0 */
+    int32_t flags;            /* PPM_RENDER_* bits; others must be 0 */
 } ppm_render_cfg;
+
+/* Render flags.  PPM_RENDER_TUNE_CELLS: pick the photon-map cells per radius
+ * (1 or 2) by timing one trial pass with each before the render starts; the
+ * trial passes leave no trace in the image.  No reference counterpart. */
+enum { PPM_RENDER_TUNE_CELLS = 1,
+/* PPM_RENDER_CLASSIC: the reference's classic ray tracer trace_ray_classic
+ * (src/tracer.rs:221-259, the `rtc` binary) instead of photon mapping: each
+ * pass traces the eye rays only (direct light + ambient, mirror and
+ * refraction children); passes average anti-aliased images. */
+       PPM_RENDER_CLASSIC = 2 };
 
 /* Per-pass statistics of the last rendered pass and accumulated timings. */
 typedef struct ppm_stats {
@@ -142,6 +152,7 @@ typedef struct ppm_stats {
     int64_t candidates;        /* photons tested by the gather (last pass, stage timing level 2) */
     int64_t in_radius;         /* photons found in radius (last pass, stage timing level 2) */
     int64_t gather_slots;      /* lane slots the gather issued (last pass, stage timing level 2) */
+    int32_t cell_factor;       /* grid cells per radius the render uses (tuned or given) */
 } ppm_stats;
 
 typedef struct ppm_ctx ppm_ctx;
@@ -243,6 +254,12 @@ int ppm_estimate(ppm_ctx *ctx, const double *pos, const double *nrm, int64_t nq,
 int ppm_estimate_noalloc(ppm_ctx *ctx, const double *pos, const double *nrm, int64_t nq,
                          int32_t pfilter, double *rgb);
 
+/* One eye pass over the FP64 map of ppm_photonmap_build, as the reference's
+ * `rt` renders a map read from `pm` (src/bin/rt.rs:41-46): trace_ray
+ * (tracer.rs:129-177) for every pixel with the map's power and radius^2;
+ * pass selects the random streams.  image_out: yreso x xreso x 3. */
+int ppm_eye_pass(ppm_ctx *ctx, int32_t use_classic, uint64_t seed, int32_t pass, double *image_out);
+
 /* ---- FP32 photon map (gather sweep) --------------------------------------- */
 /* A map of FP32 photons (n x 3 float positions, directions, wl).  Queries are
  * FP32 positions with FP64 radii^2; membership is decided exactly as the f64
@@ -285,6 +302,45 @@ int ppm_render_stats(ppm_ctx *ctx, ppm_stats *out);
  * eagerly, not as a graph); on = 2: also count gather candidates and hits. */
 int ppm_set_stage_timing(ppm_ctx *ctx, int32_t on);
 const char *ppm_stage_name(int32_t stage);
+
+/* ---- output ------------------------------------------------------------------ */
+/* Camera::radiance_to_rgb (src/camera.rs:92-100) for n values:
+ * floor(min(1, L / max_radiance)^(1/2.2) * 255); the averager's P3 output
+ * (util/averager.rb:66-76) is this map of the averaged image. */
+int ppm_tone_map(const double *img, int64_t n, double max_radiance, int32_t *rgb_out);
+/* The uncompressed scanline OpenEXR file of util/averager2.rb:154-218 (B, G,
+ * R float channels) with values img * scale; averager2 divides the averaged
+ * image by max radiance (scale = 1 / max_radiance). */
+int ppm_write_exr(const char *path, const double *img, int32_t xreso, int32_t yreso, double scale);
+
+/* ---- batched rendering ------------------------------------------------------ */
+/* No reference counterpart (the reference renders one scene per process,
+ * one pass per run).  A batch renders many independent jobs -- scenes of any
+ * size, cameras, photon budgets, alphas, pass counts -- on one GPU: each job
+ * has its own context and captured pass graph, and every pass of the whole
+ * batch is a single graph launch whose branches are the jobs, so small jobs
+ * share the GPU instead of running one after another.  Jobs whose passes are
+ * done drop out.  Each job's image is the same as ppm_render would give for
+ * it alone (up to the order of floating-point atomic adds).  device_ms
+ * (optional) receives the device time of all the passes. */
+typedef struct ppm_job {
+    const ppm_object *objs;
+    int32_t n_objs;
+    int32_t n_mats;
+    const ppm_material *mats;
+    const ppm_light *lights;
+    int32_t n_lights;
+    int32_t pad_;
+    const ppm_camera *cam;
+    ppm_render_cfg cfg;       /* use_graph is forced on */
+    double *image_out;        /* yreso x xreso x 3 */
+} ppm_job;
+
+typedef struct ppm_batch ppm_batch;
+int         ppm_batch_create(ppm_batch **out, int device, uint64_t seed);
+int         ppm_batch_destroy(ppm_batch *b);
+const char *ppm_batch_last_error(const ppm_batch *b);
+int         ppm_batch_render(ppm_batch *b, const ppm_job *jobs, int32_t njobs, double *device_ms);
 
 #ifdef __cplusplus
 }

@@ -68,6 +68,7 @@ def lib() -> C.CDLL:
             "orc_last_query_seconds": (C.c_double, []),
             "orc_trace_photons": (C.c_int64, [C.POINTER(_Scene), C.c_int64, C.c_int, C.c_uint64, C.c_uint32,
                                               _dp, _dp, _u8p, _i32p, _i8p, C.c_int64, _dp, _i64p]),
+            "orc_classic_pass": (None, [C.POINTER(_Scene), C.c_void_p, C.c_uint64, C.c_uint32, _dp]),
             "orc_eye_pass": (None, [C.POINTER(_Scene), C.c_void_p, _dp, _dp, _u8p, C.c_int64, C.c_double,
                                     C.c_double, C.c_int, C.c_uint64, C.c_uint32, _dp]),
             "orc_render": (None, [C.POINTER(_Scene), C.c_void_p, C.c_int64, C.c_int, C.c_double, C.c_double,
@@ -185,6 +186,13 @@ class Oracle:
         self.L.orc_eye_pass(C.byref(self.sc), C.byref(cam), _p(pos, C.c_double), _p(dirs, C.c_double),
                             _p(wl, C.c_uint8), pos.shape[0], float(r2), float(photons["power"]),
                             int(bool(use_classic)), int(seed), int(pass_index), _p(img, C.c_double))
+        return img
+
+    def classic_pass(self, seed: int = 1, pass_index: int = 0):
+        """One pass of trace_ray_classic over the camera's pixels."""
+        cam = self.camera
+        img = np.zeros((cam.yreso, cam.xreso, 3))
+        self.L.orc_classic_pass(C.byref(self.sc), C.byref(cam), int(seed), int(pass_index), _p(img, C.c_double))
         return img
 
     def render(self, nphoton, passes, r0, alpha, schedule_offset=1, use_classic=True, seed=1):

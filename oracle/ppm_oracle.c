@@ -1187,6 +1187,49 @@ void orc_camera_derive(orc_camera *c) {
     for (int i = 0; i < 6; i++) { dst[i][0] = src[i].x; dst[i][1] = src[i].y; dst[i][2] = src[i].z; }
 }
 
+/* trace_ray_classic, tracer.rs:221-259 (Whitted-style: no photon map).
+ * di = direct light of every light (always) + the camera's ambient; the
+ * reflected child follows the exact mirror direction; refraction bends about
+ * the surface normal and the child's medium is the hit material when the
+ * refracted ray goes into the surface (tdir . n < 0), air otherwise; the
+ * bsdf takes cos1. */
+static V3 trace_ray_classic(const orc_scene *sc, const orc_camera *cam, int m0, int l, V3 rp, V3 rd) {
+    if (l >= MAX_TRACE) return v3(0, 0, 0);
+    isect_t is;
+    if (!intersect(sc, rp, rd, &is)) return v3(0, 0, 0);
+    int mid = sc->objs[is.obj].material;
+    const orc_material *mate = &sc->mats[mid];
+    double cos1, cos2;
+    V3 rdir = specular_reflection(is.n, rd, &cos1);
+    V3 di = v3(0, 0, 0);
+    for (int i = 0; i < sc->n_lights; i++) di = vadd(di, radiance_from_light(sc, is.pos, is.n, &sc->lights[i]));
+    di = vadd(di, v3p(cam->ambient));
+    V3 si = v3(0, 0, 0);
+    if (sf_reflect(mate, cos1)) si = trace_ray_classic(sc, cam, m0, l + 1, is.pos, rdir);
+    double eta = relative_ior_average(mat_of(sc, m0)->ior, mate->ior);
+    V3 td;
+    int has_t = specular_refraction(is.n, rd, eta, &td, &cos2);
+    V3 ti = v3(0, 0, 0);
+    if (has_t && sf_refract(mate, cos1))
+        ti = trace_ray_classic(sc, cam, vdot(td, is.n) < 0.0 ? mid : -1, l + 1, is.pos, td);
+    V3 em = vmul(v3p(mate->emittance), SR_HALF);
+    return vadd(em, sf_bsdf(mate, cos1, di, si, ti));
+}
+
+void orc_classic_pass(const orc_scene *sc, const orc_camera *cam, uint64_t seed, uint32_t pass, double *image) {
+    int64_t npx = (int64_t)cam->xreso * cam->yreso;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(orc_get_threads())
+    for (int64_t p = 0; p < npx; p++) {
+        int64_t y = p / cam->xreso, x = p % cam->xreso;
+        rng_t rg;
+        rng_init(&rg, seed, (uint32_t)p, pass, TAG_CAMERA);
+        V3 rp, rd;
+        generate_ray(cam, &rg, (double)y, (double)x, &rp, &rd);
+        V3 r = trace_ray_classic(sc, cam, -1, 0, rp, rd);
+        image[3 * p] += r.x; image[3 * p + 1] += r.y; image[3 * p + 2] += r.z;
+    }
+}
+
 void orc_eye_pass(const orc_scene *sc, const orc_camera *cam,
                   const double *ppos, const double *pdir, const uint8_t *pwl, int64_t np,
                   double r2, double pw, int uc, uint64_t seed, uint32_t pass, double *image) {

@@ -153,6 +153,9 @@ int64_t orc_trace_photons(const orc_scene *sc, int64_t nphoton, int uc, uint64_t
 
 /* One eye pass over a given photon map (src/bin/ppmpa.rs:81-82, src/tracer.rs:129-216):
  * image[3*pixel] += radiance of trace_ray for pixel (row-major). */
+/* one pass of the classic (Whitted-style) tracer, trace_ray_classic
+ * (tracer.rs:221-259) for every pixel's camera ray; adds into image. */
+void orc_classic_pass(const orc_scene *sc, const orc_camera *cam, uint64_t seed, uint32_t pass, double *image);
 void orc_eye_pass(const orc_scene *sc, const orc_camera *cam,
                   const double *ppos, const double *pdir, const uint8_t *pwl, int64_t np,
                   double r2, double pw, int uc, uint64_t seed, uint32_t pass, double *image);

@@ -6,7 +6,7 @@ eye-hit radiance estimate, the PA radius shrink and the running average of
 pass images, all on one GPU behind the C ABI of include/ppm_api.h.
 """
 from . import scene
-from .api import MIXED, PLAIN, Context, RenderConfig
+from .api import MIXED, PLAIN, Batch, Context, RenderConfig
 from ._lib import PPMError
 
-__all__ = ["scene", "Context", "RenderConfig", "PLAIN", "MIXED", "PPMError"]
+__all__ = ["scene", "Batch", "Context", "RenderConfig", "PLAIN", "MIXED", "PPMError"]

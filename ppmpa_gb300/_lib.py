@@ -48,6 +48,13 @@ SIGNATURES = {
     "ppm_query_within_f32": (C.c_int, [_P, _fp, C.c_int64, _dp, _i64p, _i32p, C.c_int64, _i64p]),
     "ppm_estimate_f32": (C.c_int, [_P, _fp, _fp, C.c_int64, _dp, _dp]),
     "ppm_set_accel": (C.c_int, [_P, C.c_int32]),
+    "ppm_eye_pass": (C.c_int, [_P, C.c_int32, C.c_uint64, C.c_int32, _dp]),
+    "ppm_tone_map": (C.c_int, [_dp, C.c_int64, C.c_double, C.POINTER(C.c_int32)]),
+    "ppm_write_exr": (C.c_int, [C.c_char_p, _dp, C.c_int32, C.c_int32, C.c_double]),
+    "ppm_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_uint64]),
+    "ppm_batch_destroy": (C.c_int, [_P]),
+    "ppm_batch_last_error": (C.c_char_p, [_P]),
+    "ppm_batch_render": (C.c_int, [_P, _P, C.c_int32, _dp]),
     "ppm_scene_parse": (C.c_int, [C.c_char_p, C.c_void_p, C.POINTER(C.c_int32), C.c_void_p, C.POINTER(C.c_int32),
                                   C.c_void_p, C.POINTER(C.c_int32)]),
     "ppm_camera_parse": (C.c_int, [C.c_char_p, C.c_void_p, C.POINTER(C.c_int64)]),

@@ -28,6 +28,11 @@ def _ptr(a: np.ndarray, ctype):
     return a.ctypes.data_as(C.POINTER(ctype)) if a is not None else None
 
 
+# RenderConfig.flags bits (include/ppm_api.h)
+RENDER_TUNE_CELLS = 1   # time cells per radius 1 and 2 before the render, keep the faster
+RENDER_CLASSIC = 2      # the classic ray tracer (trace_ray_classic) instead of photon mapping
+
+
 @dataclass
 class RenderConfig:
     nphoton: int = 200_000
@@ -263,5 +268,61 @@ class Context:
         return dict(photons_emitted=s.photons_emitted, photons_stored=s.photons_stored, hit_points=s.hit_points,
                     grid_cells=s.grid_cells, passes_done=s.passes_done, kernels_per_pass=s.kernels_per_pass,
                     r2=s.r2, candidates=s.candidates, in_radius=s.in_radius, gather_slots=s.gather_slots,
+                    cell_factor=s.cell_factor,
                     stage_ms={n: s.stage_ms[i] for i, n in enumerate(names)},
                     stage_calls={n: s.stage_calls[i] for i, n in enumerate(names)})
+
+
+class Batch:
+    """Many independent renders on one GPU (ppm_batch): one graph launch per
+    pass runs a pass of every job."""
+
+    def __init__(self, device: int = 0, seed: int = 1):
+        self.lib = load()
+        h = C.c_void_p()
+        st = self.lib.ppm_batch_create(C.byref(h), int(device), int(seed))
+        if st != 0:
+            raise PPMError(st, self.lib.ppm_last_error(None).decode())
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.ppm_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render(self, jobs):
+        """jobs: [(scene, camera, RenderConfig)]; returns ([images], device ms of the passes)."""
+        arr = (S.Job * max(1, len(jobs)))()
+        keep, images = [], []
+        for j, (sc, cam, cfg) in enumerate(jobs):
+            objs, no = sc.c_objects()
+            mats, nm = sc.c_materials()
+            lts, nl = sc.c_lights()
+            img = np.zeros((cam.yreso, cam.xreso, 3), np.float64)
+            cam_c = S.Camera.from_buffer_copy(cam)
+            keep += [objs, mats, lts, cam_c]
+            images.append(img)
+            jb = arr[j]
+            jb.objs, jb.n_objs = C.cast(objs, C.c_void_p), no
+            jb.mats, jb.n_mats = C.cast(mats, C.c_void_p), nm
+            jb.lights, jb.n_lights = C.cast(lts, C.c_void_p), nl
+            jb.cam = C.cast(C.pointer(cam_c), C.c_void_p)
+            jb.cfg = cfg.to_c()
+            jb.image_out = _ptr(img, C.c_double)
+        ms = C.c_double()
+        st = self.lib.ppm_batch_render(self.h, arr, len(jobs), C.byref(ms))
+        if st != 0:
+            raise PPMError(st, self.lib.ppm_batch_last_error(self.h).decode())
+        return images, ms.value

@@ -22,6 +22,7 @@ UNITS = {
     "k_grid.cu": [],
     "k_bvh.cu": [],
     "scene_file.cpp": [],
+    "output.cpp": [],
     "ppm_api.cu": [],
 }
 
@@ -35,7 +36,7 @@ def nvcc() -> str:
 
 def _sources_mtime() -> float:
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    files.append(os.path.join(HERE, "cli", "ppmpa.cpp"))
+    files += [os.path.join(HERE, "cli", f) for f in os.listdir(os.path.join(HERE, "cli"))]
     files.append(os.path.join(ROOT, "include", "ppm_api.h"))
     files.append(os.path.abspath(__file__))
     return max(os.path.getmtime(f) for f in files)
@@ -75,17 +76,22 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
 
 
 CLI = os.path.join(OUT, "ppmpa")
+TOOLS = ("ppmpa", "pm", "rt", "rtc")   # drop-ins for the reference's binaries
 
 
 def _build_cli() -> str:
-    """The `ppmpa` command-line program (same argv and output as the reference binary)."""
-    src = os.path.join(HERE, "cli", "ppmpa.cpp")
-    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), src,
-           "-o", CLI + ".tmp", "-L", OUT, "-lppmpa_gb300", "-Wl,-rpath,$ORIGIN"]
-    res = subprocess.run(cmd, capture_output=True, text=True)
-    if res.returncode != 0:
-        raise RuntimeError(f"ppmpa CLI build failed:\n{res.stderr}")
-    os.replace(CLI + ".tmp", CLI)
+    """The command-line programs (same argv and output as the reference's binaries)."""
+    def one(name):
+        src = os.path.join(HERE, "cli", name + ".cpp")
+        out = os.path.join(OUT, name)
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), src,
+               "-o", out + ".tmp", "-L", OUT, "-lppmpa_gb300", "-Wl,-rpath,$ORIGIN"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"{name} build failed:\n{res.stderr}")
+        os.replace(out + ".tmp", out)
+    with cf.ThreadPoolExecutor(max_workers=len(TOOLS)) as ex:
+        list(ex.map(one, TOOLS))
     return CLI
 
 

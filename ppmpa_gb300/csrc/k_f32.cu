@@ -31,11 +31,15 @@ void launch_scatter_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, co
 }
 void launch_eye_level_f(const SceneView<float> &sc, const DCamera<float> &cam, uint64_t seed, PassState *st, int uc,
                         int level, EyeQueue<float> in, EyeQueue<float> out, unsigned long long qcap,
-                        HitPoint<float> *hits, EyeOut<float> pix, int grid, cudaStream_t s) {
-    if (sc.bvh)
-        k_eye_level_bvh<float><<<grid, 128, 0, s>>>(with_bvh(sc), cam, seed, st, uc, level, in, out, qcap, hits, pix);
+                        HitPoint<float> *hits, EyeOut<float> pix, int grid, cudaStream_t s, bool classic) {
+    if (sc.bvh && classic)
+        k_eye_level_bvh<float, true><<<grid, 128, 0, s>>>(with_bvh(sc), cam, seed, st, uc, level, in, out, qcap, hits, pix);
+    else if (sc.bvh)
+        k_eye_level_bvh<float, false><<<grid, 128, 0, s>>>(with_bvh(sc), cam, seed, st, uc, level, in, out, qcap, hits, pix);
+    else if (classic)
+        k_eye_level<float, true><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
     else
-        k_eye_level<float><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
+        k_eye_level<float, false><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
 }
 void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
                      const uint32_t *start, double pw, const double *q_r2, int pfilter, int mode, GatherOutF out,

@@ -99,6 +99,7 @@ struct ppm_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     long long passes_done = 0;
     int kernels_per_pass = 0;
+    int cell_factor = 0;          // grid cells per radius of the current render
 
     // timing
     bool timing = false;
@@ -147,6 +148,13 @@ static void release(DevBuf &b) {
 }
 
 template <typename T> static T *as(DevBuf &b) { return static_cast<T *>(b.p); }
+
+#define CK_B(call)                                                                                 \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return batch_err(b, PPM_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));    \
+    } while (0)
 
 #define TRY(x)                          \
     do {                                \
@@ -286,6 +294,7 @@ static void conv_camera(const ppm_camera &c, DCamera<T> &d) {
         d.esy[a] = (T)c.esy[a];
         d.eex[a] = (T)c.eex[a];
         d.eey[a] = (T)c.eey[a];
+        d.ambient[a] = (T)c.ambient[a];
     }
     d.xreso = c.xreso;
     d.yreso = c.yreso;
@@ -959,6 +968,45 @@ extern "C" int ppm_estimate_noalloc(ppm_ctx *ctx, const double *pos, const doubl
     return PPM_OK;
 }
 
+// One eye pass over the FP64 photon map of ppm_photonmap_build: what the
+// reference's `rt` does with a map read from `pm` (src/bin/rt.rs:41-46):
+// trace_ray (tracer.rs:129-177) for every pixel's camera ray, with the map's
+// power and radius^2 in the estimate.  pass selects the random streams.
+extern "C" int ppm_eye_pass(ppm_ctx *ctx, int32_t use_classic, uint64_t seed, int32_t pass, double *image_out) {
+    if (!ctx || !image_out || pass < 0) return PPM_ERR_INVALID_ARG;
+    if (ctx->map_kind != 1) return set_err(ctx, PPM_ERR_NOT_READY, "no FP64 photon map built");
+    if (!ctx->have_scene || !ctx->have_cam) return set_err(ctx, PPM_ERR_NOT_READY, "scene and camera must be set");
+    cudaSetDevice(ctx->device);
+    drop_graph(ctx);
+    ctx->render_ready = false;
+    ctx->npx = (long long)ctx->cam.xreso * ctx->cam.yreso;
+    ctx->hit_cap = ctx->npx * HITS_PER_PIXEL;
+    TRY(ensure(ctx, ctx->hits_d, sizeof(HitPoint<double>) * ctx->hit_cap));
+    TRY(ensure_eye_queues(ctx, ctx->npx, sizeof(double4)));
+    TRY(ensure(ctx, ctx->pass_img, sizeof(double) * 3 * ctx->npx));
+    // the map's grid and radius stay; the eye needs the hit capacity and pass
+    const unsigned long long hcap = (unsigned long long)ctx->hit_cap;
+    CK(cudaMemcpyAsync(&ctx->st->hit_cap, &hcap, sizeof hcap, cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(&ctx->st->pass, &pass, sizeof pass, cudaMemcpyHostToDevice, ctx->s));
+    launch_pass_begin(ctx->st, ctx->s);
+    const int uc = use_classic ? 1 : 0;
+    enqueue_eye<double>(ctx, as<HitPoint<double>>(ctx->hits_d),
+        [&](int l, EyeQueue<double> in, EyeQueue<double> out, unsigned long long qcap, HitPoint<double> *h, int g,
+            cudaStream_t st) {
+            launch_eye_level_d(ctx->sv_d, ctx->cam_d, seed, ctx->st, uc, l, in, out, qcap, h,
+                               EyeOut<double>{as<double>(ctx->pass_img)}, g, st);
+        }, ctx->s);
+    GatherOutD go{as<double>(ctx->pass_img), nullptr, nullptr};
+    launch_gather_d(as<HitPoint<double>>(ctx->hits_d), ctx->st, -1, as<double4>(ctx->spos), as<double4>(ctx->sdir),
+                    as<uint32_t>(ctx->start), ctx->map_pw, ctx->cam.pfilter, 0, go, grid_blocks(ctx, 8), ctx->s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(image_out, ctx->pass_img.p, sizeof(double) * 3 * ctx->npx, cudaMemcpyDeviceToHost, ctx->s));
+    PassState h;
+    TRY(read_state(ctx, h));
+    if (h.overflow) return set_err(ctx, PPM_ERR_CAPACITY, "eye pass overflow (flags %u)", h.overflow);
+    return PPM_OK;
+}
+
 // ---------------------------------------------------------------------------
 // FP32 photon map (gather sweep)
 // ---------------------------------------------------------------------------
@@ -1227,6 +1275,38 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
     const int g8 = grid_blocks(ctx, 8), g4 = grid_blocks(ctx, 4);
     if (ev) CK(cudaEventRecord(ev[0], s));
     launch_pass_begin(ctx->st, s); kernels++;
+    if (ctx->cfg.flags & PPM_RENDER_CLASSIC) {
+        // classic tracer: eye rays only (no photons, no map, no gather); the
+        // stage events stay in order so the timing table reads zeros there
+        if (ev) CK(cudaEventRecord(ev[5], s));
+        if (mixed)
+            kernels += enqueue_eye<float>(ctx, as<HitPoint<float>>(ctx->hits_f),
+                [&](int l, EyeQueue<float> in, EyeQueue<float> out, unsigned long long qcap, HitPoint<float> *h, int g,
+                    cudaStream_t st) {
+                    launch_eye_level_f(ctx->sv_f, ctx->cam_f, ctx->cfg.seed, ctx->st, uc, l, in, out, qcap, h,
+                                       EyeOut<float>{as<float>(ctx->pass_direct32), as<float>(ctx->pass_gather32)}, g,
+                                       st, true);
+                }, s);
+        else
+            kernels += enqueue_eye<double>(ctx, as<HitPoint<double>>(ctx->hits_d),
+                [&](int l, EyeQueue<double> in, EyeQueue<double> out, unsigned long long qcap, HitPoint<double> *h,
+                    int g, cudaStream_t st) {
+                    launch_eye_level_d(ctx->sv_d, ctx->cam_d, ctx->cfg.seed, ctx->st, uc, l, in, out, qcap, h,
+                                       EyeOut<double>{as<double>(ctx->pass_img)}, g, st, true);
+                }, s);
+        if (ev) for (int k : {6, 1, 2, 7, 3}) CK(cudaEventRecord(ev[k], s));
+        if (mixed)
+            launch_accum_mixed(as<float>(ctx->pass_direct32), as<float>(ctx->pass_gather32), ctx->st, ctx->pw,
+                               as<double>(ctx->pass_img), as<double>(ctx->sum_img), 3 * ctx->npx, s);
+        else
+            launch_accum(as<double>(ctx->pass_img), as<double>(ctx->sum_img), 3 * ctx->npx, s);
+        launch_pass_end(ctx->st, s);
+        kernels += 2;
+        if (ev) CK(cudaEventRecord(ev[4], s));
+        CK(cudaGetLastError());
+        ctx->kernels_per_pass = kernels;
+        return PPM_OK;
+    }
     // the eye pass does not depend on the photon map: run it on the side stream
     CK(cudaEventRecord(ctx->ev_fork, s));
     CK(cudaStreamWaitEvent(s2, ctx->ev_fork, 0));
@@ -1304,12 +1384,47 @@ static double schedule_r2(const ppm_render_cfg &c, int upto) {
     return r;
 }
 
+// Grid cell autotuner of a render: one untimed and one timed eager pass with
+// 1 and with 2 cells per radius; the faster wins.  The trial passes write
+// only buffers that the caller's render then resets (state, pass and sum
+// images), so the image does not depend on the trial.
+static int tune_cells(ppm_ctx *ctx, const ppm_render_cfg &cfg, long long cap, int &best) {
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return set_err(ctx, PPM_ERR_CUDA, "event"); }
+    const bool timing = ctx->timing;
+    ctx->timing = false;
+    float best_ms = 1e30f;
+    int rc = PPM_OK;
+    for (int k = 1; k <= 2 && rc == PPM_OK; k++) {
+        for (int rep = 0; rep < 2 && rc == PPM_OK; rep++) {
+            rc = upload_state(ctx, schedule_r2(cfg, cfg.first_pass), cfg.first_pass, cfg.alpha, cfg.schedule_offset,
+                              (double)k, cap, ctx->hit_cap);
+            if (rc == PPM_OK && cudaEventRecord(e0, ctx->s) != cudaSuccess) rc = set_err(ctx, PPM_ERR_CUDA, "event");
+            if (rc == PPM_OK) rc = enqueue_pass(ctx, false);
+            if (rc == PPM_OK && cudaEventRecord(e1, ctx->s) != cudaSuccess) rc = set_err(ctx, PPM_ERR_CUDA, "event");
+            float ms = 0.0f;
+            if (rc == PPM_OK && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+                rc = set_err(ctx, PPM_ERR_CUDA, "cell tuner timing");
+            if (rc == PPM_OK && rep == 1 && ms < best_ms) { best_ms = ms; best = k; }
+        }
+    }
+    ctx->timing = timing;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != PPM_OK) return rc;
+    CK(cudaMemsetAsync(ctx->sum_img.p, 0, sizeof(double) * 3 * ctx->npx, ctx->s));
+    CK(cudaMemsetAsync(ctx->pass_img.p, 0, sizeof(double) * 3 * ctx->npx, ctx->s));
+    return PPM_OK;
+}
+
 extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
     if (!ctx || !cfg) return PPM_ERR_INVALID_ARG;
     if (!ctx->have_scene || !ctx->have_cam || ctx->lights.empty())
         return set_err(ctx, PPM_ERR_NOT_READY, "scene (with lights) and camera must be set first");
     if (cfg->nphoton <= 0 || cfg->passes < 0 || !(cfg->radius0 > 0.0) || cfg->precision < 0 || cfg->precision > 1 ||
-        cfg->cell_factor < 0 || cfg->cell_factor > 2 || cfg->first_pass < 0)
+        cfg->cell_factor < 0 || cfg->cell_factor > 2 || cfg->first_pass < 0 ||
+        (cfg->flags & ~(PPM_RENDER_TUNE_CELLS | PPM_RENDER_CLASSIC)))
         return set_err(ctx, PPM_ERR_INVALID_ARG, "bad render configuration");
     cudaSetDevice(ctx->device);
     drop_graph(ctx);
@@ -1320,15 +1435,16 @@ extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
     long long cap = std::max(1LL, nem * MAX_TRACE);
     ctx->npx = (long long)ctx->cam.xreso * ctx->cam.yreso;
     ctx->hit_cap = ctx->npx * HITS_PER_PIXEL;
+    const bool photons = !(cfg->flags & PPM_RENDER_CLASSIC);
     if (cfg->precision == PPM_PRECISION_MIXED) {
-        TRY(ensure_photons_f(ctx, cap, false));
+        if (photons) TRY(ensure_photons_f(ctx, cap, false));
         TRY(ensure(ctx, ctx->hits_f, sizeof(HitPoint<float>) * ctx->hit_cap));
-        TRY(ensure_ray_queues(ctx, nem, sizeof(float4)));
+        if (photons) TRY(ensure_ray_queues(ctx, nem, sizeof(float4)));
         TRY(ensure_eye_queues(ctx, ctx->npx, sizeof(float4)));
     } else {
-        TRY(ensure_photons_d(ctx, cap));
+        if (photons) TRY(ensure_photons_d(ctx, cap));
         TRY(ensure(ctx, ctx->hits_d, sizeof(HitPoint<double>) * ctx->hit_cap));
-        TRY(ensure_ray_queues(ctx, nem, sizeof(double4)));
+        if (photons) TRY(ensure_ray_queues(ctx, nem, sizeof(double4)));
         TRY(ensure_eye_queues(ctx, ctx->npx, sizeof(double4)));
     }
     TRY(ensure(ctx, ctx->pass_img, sizeof(double) * 3 * ctx->npx));
@@ -1340,9 +1456,11 @@ extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
     CK(cudaMemsetAsync(ctx->sum_img.p, 0, sizeof(double) * 3 * ctx->npx, ctx->s));
     CK(cudaMemsetAsync(ctx->pass_img.p, 0, sizeof(double) * 3 * ctx->npx, ctx->s));
     int cf = cfg->cell_factor ? cfg->cell_factor : 1;
+    if ((cfg->flags & PPM_RENDER_TUNE_CELLS) && !(cfg->flags & PPM_RENDER_CLASSIC)) TRY(tune_cells(ctx, *cfg, cap, cf));
     TRY(upload_state(ctx, schedule_r2(*cfg, cfg->first_pass), cfg->first_pass, cfg->alpha, cfg->schedule_offset, (double)cf,
                      cap, ctx->hit_cap));
     CK(cudaStreamSynchronize(ctx->s));
+    ctx->cell_factor = cf;
     ctx->passes_done = 0;
     ctx->map_kind = 0;
     for (int i = 0; i < 16; i++) { ctx->stage_ms[i] = 0.0; ctx->stage_calls[i] = 0; }
@@ -1429,6 +1547,7 @@ extern "C" int ppm_render_stats(ppm_ctx *ctx, ppm_stats *out) {
     out->candidates = (int64_t)h.candidates;
     out->in_radius = (int64_t)h.in_radius;
     out->gather_slots = (int64_t)h.slots;
+    out->cell_factor = ctx->cell_factor;
     return PPM_OK;
 }
 
@@ -1437,4 +1556,135 @@ extern "C" int ppm_render(ppm_ctx *ctx, const ppm_render_cfg *cfg, double *image
     TRY(ppm_render_begin(ctx, cfg));
     TRY(ppm_render_step(ctx, cfg->passes));
     return ppm_render_image(ctx, image_out);
+}
+
+// ---------------------------------------------------------------------------
+// Batched rendering.  One context per job (scene, camera, buffers, pass
+// graph); each pass of the whole batch is one launch of a parent graph whose
+// children are the jobs' pass graphs, with no edges between jobs, so the GPU
+// runs the jobs' kernels side by side.  Jobs with fewer passes drop out of
+// the parent graph when they are done.
+// ---------------------------------------------------------------------------
+struct ppm_batch {
+    int device = 0;
+    uint64_t seed = 0;
+    std::vector<ppm_ctx *> ctxs;
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    std::string err;
+};
+
+static int batch_err(ppm_batch *b, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    b->err = buf;
+    return code;
+}
+
+extern "C" int ppm_batch_create(ppm_batch **out, int device, uint64_t seed) {
+    if (!out) return PPM_ERR_INVALID_ARG;
+    *out = nullptr;
+    ppm_ctx *probe = nullptr;
+    int st = ppm_ctx_create(&probe, device, seed);
+    if (st != PPM_OK) return st;
+    ppm_batch *b = new ppm_batch;
+    b->device = device;
+    b->seed = seed;
+    b->ctxs.push_back(probe);
+    if (cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&b->e0) != cudaSuccess || cudaEventCreate(&b->e1) != cudaSuccess) {
+        ppm_batch_destroy(b);
+        return PPM_ERR_CUDA;
+    }
+    *out = b;
+    return PPM_OK;
+}
+
+extern "C" int ppm_batch_destroy(ppm_batch *b) {
+    if (!b) return PPM_OK;
+    cudaSetDevice(b->device);
+    if (b->s) cudaStreamSynchronize(b->s);
+    for (ppm_ctx *c : b->ctxs) ppm_ctx_destroy(c);
+    if (b->e0) cudaEventDestroy(b->e0);
+    if (b->e1) cudaEventDestroy(b->e1);
+    if (b->s) cudaStreamDestroy(b->s);
+    delete b;
+    return PPM_OK;
+}
+
+extern "C" const char *ppm_batch_last_error(const ppm_batch *b) { return b ? b->err.c_str() : ""; }
+
+extern "C" int ppm_batch_render(ppm_batch *b, const ppm_job *jobs, int32_t njobs, double *device_ms) {
+    if (!b || njobs < 0 || (njobs && !jobs)) return PPM_ERR_INVALID_ARG;
+    cudaSetDevice(b->device);
+    for (int j = 0; j < njobs; j++) {
+        const ppm_job &jb = jobs[j];
+        if (!jb.cam || !jb.image_out) return batch_err(b, PPM_ERR_INVALID_ARG, "job %d: camera and image are required", j);
+    }
+    while ((int)b->ctxs.size() < njobs) {
+        ppm_ctx *c = nullptr;
+        int st = ppm_ctx_create(&c, b->device, b->seed);
+        if (st != PPM_OK) return batch_err(b, st, "context for job %zu: %s", b->ctxs.size(), ppm_last_error(nullptr));
+        b->ctxs.push_back(c);
+    }
+    int max_passes = 0;
+    for (int j = 0; j < njobs; j++) {
+        const ppm_job &jb = jobs[j];
+        ppm_ctx *c = b->ctxs[j];
+        ppm_render_cfg cfg = jb.cfg;
+        cfg.use_graph = 1;
+        int st = ppm_scene_upload(c, jb.objs, jb.n_objs, jb.mats, jb.n_mats, jb.lights, jb.n_lights);
+        if (st == PPM_OK) st = ppm_camera_set(c, jb.cam);
+        if (st == PPM_OK) st = ppm_render_begin(c, &cfg);
+        if (st != PPM_OK) return batch_err(b, st, "job %d: %s", j, c->err.c_str());
+        max_passes = std::max(max_passes, cfg.passes);
+    }
+    // every job's set-up (uploads, tuning, capture) ran on its own stream
+    for (int j = 0; j < njobs; j++) CK_B(cudaStreamSynchronize(b->ctxs[j]->s));
+    CK_B(cudaEventRecord(b->e0, b->s));
+    int p = 0;
+    while (p < max_passes) {
+        // jobs still running, and the pass at which the next one finishes
+        cudaGraph_t parent = nullptr;
+        CK_B(cudaGraphCreate(&parent, 0));
+        int until = max_passes;
+        int rc = PPM_OK;
+        for (int j = 0; j < njobs && rc == PPM_OK; j++) {
+            const int pj = jobs[j].cfg.passes;
+            if (pj <= p) continue;
+            until = std::min(until, pj);
+            cudaGraphNode_t node;
+            cudaError_t e = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, b->ctxs[j]->graph);
+            if (e != cudaSuccess) rc = batch_err(b, PPM_ERR_CUDA, "job %d graph: %s", j, cudaGetErrorString(e));
+        }
+        cudaGraphExec_t exec = nullptr;
+        if (rc == PPM_OK) {
+            cudaError_t e = cudaGraphInstantiate(&exec, parent, 0);
+            if (e != cudaSuccess) rc = batch_err(b, PPM_ERR_CUDA, "batch graph: %s", cudaGetErrorString(e));
+        }
+        for (; rc == PPM_OK && p < until; p++) {
+            cudaError_t e = cudaGraphLaunch(exec, b->s);
+            if (e != cudaSuccess) rc = batch_err(b, PPM_ERR_CUDA, "batch pass %d: %s", p, cudaGetErrorString(e));
+        }
+        if (exec) cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(parent);
+        if (rc != PPM_OK) return rc;
+    }
+    CK_B(cudaEventRecord(b->e1, b->s));
+    CK_B(cudaStreamSynchronize(b->s));
+    if (device_ms) {
+        float ms = 0.0f;
+        CK_B(cudaEventElapsedTime(&ms, b->e0, b->e1));
+        *device_ms = ms;
+    }
+    for (int j = 0; j < njobs; j++) {
+        ppm_ctx *c = b->ctxs[j];
+        c->passes_done = jobs[j].cfg.passes;
+        int st = ppm_render_image(c, jobs[j].image_out);
+        if (st != PPM_OK) return batch_err(b, st, "job %d: %s", j, c->err.c_str());
+    }
+    return PPM_OK;
 }

@@ -310,6 +310,7 @@ struct DLight {
 template <typename T>
 struct DCamera {
     T eye[3], origin[3], esx[3], esy[3], eex[3], eey[3];
+    T ambient[3];   // added to the direct light by the classic tracer
     int32_t xreso, yreso, jitter_aa, blur;
 };
 

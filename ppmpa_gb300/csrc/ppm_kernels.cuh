@@ -414,7 +414,11 @@ template <> struct EyeOut<float> {
     }
 };
 
-template <typename T, bool B>
+// CLASSIC: trace_ray_classic (tracer.rs:221-259) instead of trace_ray:
+// direct light of every light plus the camera's ambient, no hit points, the
+// exact mirror direction, refraction about the normal with the child's
+// medium by the side the refracted ray leaves on, and the bsdf at cos1.
+template <typename T, bool B, bool CLASSIC = false>
 __device__ __forceinline__ void eye_level(const SceneView<T, B> &sc, const DCamera<T> &cam, uint64_t seed,
                                           PassState *st, int uc, int level, EyeQueue<T> in, EyeQueue<T> out,
                                           unsigned long long qcap, HitPoint<T> *hits, EyeOut<T> pix) {
@@ -480,18 +484,28 @@ __device__ __forceinline__ void eye_level(const SceneView<T, B> &sc, const DCame
             } else {
                 T cos2;
                 V3<T> rdir0 = specular_reflection(is.n, rd, cos1);
-                Rng rv;
-                rv.init(seed, p, pass, TAG_EYE | node);
-                rdir = reflection_glossy(rv, is.n, rdir0, sf_power_glossy(mate));
                 T eta = relative_ior_average(ior_of(sc, medium, air), mate.ior);
-                V3<T> hvec = is.n;
-                if (!normalize(rdir - rd, hvec)) hvec = is.n;
-                has_t = specular_refraction(hvec, rd, eta, td, cos2);
-                T cos = cos1 < cos2 ? cos1 : cos2;
-                cf = bsdf_coef(mate, cos);
+                if constexpr (CLASSIC) {
+                    rdir = rdir0;
+                    has_t = specular_refraction(is.n, rd, eta, td, cos2);
+                    cf = bsdf_coef(mate, cos1);
+                } else {
+                    Rng rv;
+                    rv.init(seed, p, pass, TAG_EYE | node);
+                    rdir = reflection_glossy(rv, is.n, rdir0, sf_power_glossy(mate));
+                    V3<T> hvec = is.n;
+                    if (!normalize(rdir - rd, hvec)) hvec = is.n;
+                    has_t = specular_refraction(hvec, rd, eta, td, cos2);
+                    T cos = cos1 < cos2 ? cos1 : cos2;
+                    cf = bsdf_coef(mate, cos);
+                }
             }
             const V3<T> W = hmul(w, cf.di);
-            if (any_nz(W)) {
+            if (CLASSIC && any_nz(W)) {
+                V3<T> di = ld3(cam.ambient);
+                for (int l = 0; l < sc.n_lights; l++) di = di + radiance_from_light(sc, is.pos, is.n, sc.lights[l]);
+                acc = acc + hmul(W, di);
+            } else if (any_nz(W)) {
                 if (uc) {
                     V3<T> di = mk3(T(0), T(0), T(0));
                     for (int l = 0; l < sc.n_lights; l++) di = di + radiance_from_light(sc, is.pos, is.n, sc.lights[l]);
@@ -526,7 +540,8 @@ __device__ __forceinline__ void eye_level(const SceneView<T, B> &sc, const DCame
                     unsigned long long o = agg_append(&st->eq[level + 1]);
                     if (o < qcap) {
                         out.a[o] = mk4(is.pos, p);
-                        out.b[o] = mk4(td, (2u * node + 1u) | ((uint32_t)((is.in ? mid : -1) + 1) << 16));
+                        const int m2 = CLASSIC ? (dot(td, is.n) < T(0) ? mid : -1) : (is.in ? mid : -1);
+                        out.b[o] = mk4(td, (2u * node + 1u) | ((uint32_t)(m2 + 1) << 16));
                         out.c[o] = mk4(wt, 0u);
                     } else {
                         atomicOr(&st->overflow, 4u);
@@ -542,17 +557,17 @@ __device__ __forceinline__ void eye_level(const SceneView<T, B> &sc, const DCame
 // Two entry points over the same body: without a hierarchy the compiler's
 // own register choice (no spills, more resident warps); with one, a cap of
 // 128 registers, under which the traversal stack does not spill.
-template <typename T>
+template <typename T, bool CLASSIC>
 __global__ void __launch_bounds__(128) k_eye_level(SceneView<T, false> sc, DCamera<T> cam, uint64_t seed,
                                                    PassState *st, int uc, int level, EyeQueue<T> in, EyeQueue<T> out,
                                                    unsigned long long qcap, HitPoint<T> *hits, EyeOut<T> pix) {
-    eye_level(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
+    eye_level<T, false, CLASSIC>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
 }
-template <typename T>
+template <typename T, bool CLASSIC>
 __global__ void __maxnreg__(128) k_eye_level_bvh(SceneView<T, true> sc, DCamera<T> cam, uint64_t seed, PassState *st,
                                                  int uc, int level, EyeQueue<T> in, EyeQueue<T> out,
                                                  unsigned long long qcap, HitPoint<T> *hits, EyeOut<T> pix) {
-    eye_level(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
+    eye_level<T, true, CLASSIC>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
 }
 
 // ---------------------------------------------------------------------------

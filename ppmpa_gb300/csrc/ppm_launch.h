@@ -20,7 +20,8 @@ void launch_scatter_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, c
                       const uint2 *keyrank, int grid, cudaStream_t s);
 void launch_eye_level_d(const SceneView<double> &sc, const DCamera<double> &cam, uint64_t seed, PassState *st, int uc,
                         int level, EyeQueue<double> in, EyeQueue<double> out, unsigned long long qcap,
-                        HitPoint<double> *hits, EyeOut<double> pix, int grid, cudaStream_t s);
+                        HitPoint<double> *hits, EyeOut<double> pix, int grid, cudaStream_t s,
+                        bool classic = false);
 void launch_gather_d(const HitPoint<double> *hits, PassState *st, long long n_fixed, const double4 *spos,
                      const double4 *sdir, const uint32_t *start, double pw, int pfilter, int mode, GatherOutD out,
                      int grid, cudaStream_t s);
@@ -44,7 +45,8 @@ void launch_scatter_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, co
                       const uint2 *keyrank, int grid, cudaStream_t s);
 void launch_eye_level_f(const SceneView<float> &sc, const DCamera<float> &cam, uint64_t seed, PassState *st, int uc,
                         int level, EyeQueue<float> in, EyeQueue<float> out, unsigned long long qcap,
-                        HitPoint<float> *hits, EyeOut<float> pix, int grid, cudaStream_t s);
+                        HitPoint<float> *hits, EyeOut<float> pix, int grid, cudaStream_t s,
+                        bool classic = false);
 void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
                      const uint32_t *start, double pw, const double *q_r2, int pfilter, int mode, GatherOutF out,
                      int grid, cudaStream_t s);

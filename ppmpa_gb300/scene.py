@@ -64,12 +64,19 @@ class RenderCfg(C.Structure):
                 ("seed", C.c_uint64), ("first_pass", C.c_int32), ("flags", C.c_int32)]
 
 
+class Job(C.Structure):
+    """ppm_job: one render of a batch (scene arrays, camera, config, output image)."""
+    _fields_ = [("objs", C.c_void_p), ("n_objs", C.c_int32), ("n_mats", C.c_int32), ("mats", C.c_void_p),
+                ("lights", C.c_void_p), ("n_lights", C.c_int32), ("pad_", C.c_int32), ("cam", C.c_void_p),
+                ("cfg", RenderCfg), ("image_out", C.POINTER(C.c_double))]
+
+
 class Stats(C.Structure):
     _fields_ = [("photons_emitted", C.c_int64), ("photons_stored", C.c_int64), ("hit_points", C.c_int64),
                 ("grid_cells", C.c_int64), ("passes_done", C.c_int64), ("kernels_per_pass", C.c_int32),
                 ("n_stages", C.c_int32), ("r2", C.c_double), ("stage_ms", C.c_double * 16),
                 ("stage_calls", C.c_int64 * 16), ("candidates", C.c_int64), ("in_radius", C.c_int64),
-                ("gather_slots", C.c_int64)]
+                ("gather_slots", C.c_int64), ("cell_factor", C.c_int32)]
 
 
 # ---------------------------------------------------------------------------
@@ -227,36 +234,59 @@ def sun_light(color, flux, pos, nvec, dir1, dir2, direction) -> Lgt:
 # ---------------------------------------------------------------------------
 # scene container
 # ---------------------------------------------------------------------------
+def _object_dtype():
+    """numpy view of ppm_object (120 bytes)."""
+    import numpy as np
+    return np.dtype({"names": ["shape", "material", "position", "nvec", "dir1", "dir2", "dist", "radius"],
+                     "formats": ["<i4", "<i4", ("<f8", 3), ("<f8", 3), ("<f8", 3), ("<f8", 3), "<f8", "<f8"],
+                     "offsets": [0, 4, 8, 32, 56, 80, 104, 112], "itemsize": C.sizeof(Object)})
+
+
 @dataclass
 class Scene:
     objects: List[tuple] = field(default_factory=list)   # (Shape, material index)
     materials: List[Mat] = field(default_factory=list)
     lights: List[Lgt] = field(default_factory=list)
-    # triangles added in bulk (numpy arrays), placed after `objects`
-    tri_p0: object = None
-    tri_d1: object = None
-    tri_d2: object = None
-    tri_n: object = None
-    tri_mat: object = None
+    # objects added in bulk (numpy rows of the ppm_object layout), after `objects`
+    bulk: list = field(default_factory=list)
 
-    def add_triangles(self, p0, p1, p2, mats):
-        """Triangles p0 p1 p2 (n x 3 each, counter-clockwise seen from the
-        normal's side) as Shape::new_polygon builds them (geometry.rs:93-103):
-        dir1 = p1 - p0, dir2 = p2 - p0, nvec = normalize(dir1 x dir2)."""
+    def _bulk_rows(self, n, shape, mats):
+        import numpy as np
+        rows = np.zeros(n, _object_dtype())
+        rows["shape"] = shape
+        rows["material"] = np.broadcast_to(np.asarray(mats, np.int32), (n,))
+        self.bulk.append(rows)
+        return rows
+
+    def _bulk_flat(self, shape, p0, p1, p2, mats):
         import numpy as np
         p0 = np.ascontiguousarray(p0, np.float64)
         d1 = np.ascontiguousarray(p1, np.float64) - p0
         d2 = np.ascontiguousarray(p2, np.float64) - p0
         n = np.cross(d1, d2)
         n /= np.linalg.norm(n, axis=1, keepdims=True)
-        mats = np.broadcast_to(np.asarray(mats, np.int32), (len(p0),))
-        cat = (lambda a, b: b if a is None else np.concatenate([a, b]))
-        self.tri_p0, self.tri_d1, self.tri_d2 = cat(self.tri_p0, p0), cat(self.tri_d1, d1), cat(self.tri_d2, d2)
-        self.tri_n, self.tri_mat = cat(self.tri_n, n), cat(self.tri_mat, np.array(mats))
+        r = self._bulk_rows(len(p0), shape, mats)
+        r["position"], r["nvec"], r["dir1"], r["dir2"] = p0, n, d1, d2
+
+    def add_triangles(self, p0, p1, p2, mats):
+        """Triangles p0 p1 p2 (n x 3 each, counter-clockwise seen from the
+        normal's side) as Shape::new_polygon builds them (geometry.rs:93-103):
+        dir1 = p1 - p0, dir2 = p2 - p0, nvec = normalize(dir1 x dir2)."""
+        self._bulk_flat(SHAPE_POLYGON, p0, p1, p2, mats)
+
+    def add_parallelograms(self, p0, p1, p2, mats):
+        """Shape::new_parallelogram (geometry.rs:105-115) for n x 3 corner arrays."""
+        self._bulk_flat(SHAPE_PARALLELOGRAM, p0, p1, p2, mats)
+
+    def add_spheres(self, centres, radii, mats):
+        import numpy as np
+        c = np.ascontiguousarray(centres, np.float64)
+        r = self._bulk_rows(len(c), SHAPE_SPHERE, mats)
+        r["position"], r["radius"] = c, np.broadcast_to(np.asarray(radii, np.float64), (len(c),))
 
     @property
     def n_objects(self) -> int:
-        return len(self.objects) + (0 if self.tri_p0 is None else len(self.tri_p0))
+        return len(self.objects) + sum(len(b) for b in self.bulk)
 
     def add_material(self, m: Mat) -> int:
         self.materials.append(m)
@@ -274,17 +304,13 @@ class Scene:
             o.shape, o.material = s.shape, m
             o.position[:], o.nvec[:], o.dir1[:], o.dir2[:] = s.position, s.nvec, s.dir1, s.dir2
             o.dist, o.radius = s.dist, s.radius
-        if self.tri_p0 is not None:
+        if self.bulk:
             import numpy as np
+            view = np.frombuffer(arr, dtype=_object_dtype())
             k = len(self.objects)
-            view = np.frombuffer(arr, dtype=np.dtype({
-                "names": ["shape", "material", "position", "nvec", "dir1", "dir2", "dist", "radius"],
-                "formats": ["<i4", "<i4", ("<f8", 3), ("<f8", 3), ("<f8", 3), ("<f8", 3), "<f8", "<f8"],
-                "offsets": [0, 4, 8, 32, 56, 80, 104, 112], "itemsize": C.sizeof(Object)}))
-            t = view[k:n]
-            t["shape"], t["material"] = SHAPE_POLYGON, self.tri_mat
-            t["position"], t["nvec"], t["dir1"], t["dir2"] = self.tri_p0, self.tri_n, self.tri_d1, self.tri_d2
-            t["dist"], t["radius"] = 0.0, 0.0
+            for b in self.bulk:
+                view[k:k + len(b)] = b
+                k += len(b)
         return arr, n
 
     def c_materials(self):

@@ -89,3 +89,70 @@ def oct_roundtrip(d):
     p = np.where((z < 0)[:, None], fold, p)
     v = np.column_stack([p, z]).astype(np.float64)
     return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+# ---------------------------------------------------------------------------
+# batch of uneven render jobs
+# ---------------------------------------------------------------------------
+def _log_uniform(rng, lo, hi):
+    return float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+
+
+def batch_scene(rng, n_prims: int):
+    """The closed box with n_prims spheres and quads (half each) inside,
+    materials drawn from diffuse / mirror / glass, one point or one
+    parallelogram light under the ceiling."""
+    from . import scene as S
+    sc = S.Scene()
+    white = sc.add_material(S.new_simple((0.75, 0.75, 0.75), (0.0, 0.0, 0.0), 1.0, 0.0, 0.0))
+    red = sc.add_material(S.new_simple((0.75, 0.0, 0.0), (0.0, 0.0, 0.0), 1.0, 0.0, 0.0))
+    green = sc.add_material(S.new_simple((0.0, 0.75, 0.0), (0.0, 0.0, 0.0), 1.0, 0.0, 0.0))
+    mirror = sc.add_material(S.new_simple((0.0, 0.0, 0.0), (0.78, 0.78, 0.78), 0.0, 1.0, 0.0))
+    glass = sc.add_material(S.new_ts((1.0, 1.0, 1.0), (0.05, 0.05, 0.05), 0.0, 0.0, 0.0, ior=(1.5, 1.5, 1.5)))
+    sc.add(S.parallelogram((-1.0, 0.0, 2.0), (1.0, 0.0, 2.0), (-1.0, 2.0, 2.0)), white)
+    sc.add(S.parallelogram((-1.0, 0.0, 0.0), (-1.0, 0.0, 2.0), (1.0, 0.0, 0.0)), white)
+    sc.add(S.parallelogram((-1.0, 2.0, 0.0), (1.0, 2.0, 0.0), (-1.0, 2.0, 2.0)), white)
+    sc.add(S.parallelogram((-1.0, 0.0, 0.0), (-1.0, 2.0, 0.0), (-1.0, 0.0, 2.0)), red)
+    sc.add(S.parallelogram((1.0, 0.0, 0.0), (1.0, 0.0, 2.0), (1.0, 2.0, 0.0)), green)
+    palette = np.array([white, white, red, green, mirror, glass], np.int32)
+    n_s = n_prims // 2
+    n_q = n_prims - n_s
+    size = 0.35 * (6.0 / max(1, n_prims)) ** (1.0 / 3.0)       # fills a fraction of the box
+    lo, hi = np.array([-0.9, 0.1, 0.1]), np.array([0.9, 1.8, 1.9])
+    if n_s:
+        c = rng.uniform(lo, hi, (n_s, 3))
+        sc.add_spheres(c, size * rng.uniform(0.5, 1.0, n_s), palette[rng.integers(0, len(palette), n_s)])
+    if n_q:
+        p0 = rng.uniform(lo, hi, (n_q, 3))
+        a = rng.normal(size=(n_q, 3))
+        b = rng.normal(size=(n_q, 3))
+        a *= size / np.linalg.norm(a, axis=1, keepdims=True)
+        b *= size / np.linalg.norm(b, axis=1, keepdims=True)
+        sc.add_parallelograms(p0, p0 + a, p0 + b, palette[rng.integers(0, len(palette), n_q)])
+    col = S.color_normalize((1.0, 1.0, 1.0))
+    if rng.random() < 0.5:
+        sc.lights.append(S.point_light(col, 100.0, (0.0, 1.95, 1.0)))
+    else:
+        sc.lights.append(S.parallelogram_light(col, 100.0, (-0.3, 1.99, 0.7), (0.0, -1.0, 0.0), (0.6, 0.0, 0.0),
+                                               (0.0, 0.0, 0.6)))
+    return sc
+
+
+def batch_jobs(n_jobs: int = 64, seed: int = 7, passes: int = 8, precision: int = 1, flags: int = 1):
+    """[(scene, camera, RenderConfig)]: primitive counts log-uniform over
+    10..200k, square images 64..512 pixels wide, photons per pass
+    log-uniform over 50k..2M, alpha uniform in [0.5, 0.9]."""
+    from . import scene as S
+    from .api import RenderConfig
+    rng = np.random.default_rng([seed, 404])
+    jobs = []
+    for j in range(n_jobs):
+        n_prims = int(round(_log_uniform(rng, 10, 200_000)))
+        reso = int(round(_log_uniform(rng, 64, 512)))
+        nphoton = int(round(_log_uniform(rng, 50_000, 2_000_000)))
+        alpha = float(rng.uniform(0.5, 0.9))
+        sc = batch_scene(rng, n_prims)
+        cfg = RenderConfig(nphoton=nphoton, passes=passes, radius0=0.05, alpha=alpha, precision=precision,
+                           seed=seed * 1000 + j, flags=flags)
+        jobs.append((sc, S.box_camera(reso), cfg))
+    return jobs

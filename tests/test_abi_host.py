@@ -117,3 +117,10 @@ def test_cli_usage_and_rust_number_format(built_lib):
     out = subprocess.run([cli, "--format-test", *vals], capture_output=True, text=True, check=True)
     got = [tuple(l.split()) for l in out.stdout.strip().split("\n")]
     assert got == want
+
+
+def test_batch_job_layout_matches_header(built_lib):
+    """ppm_job: pointer, 2 x int32, 3 pointers with an int32 pair, the render
+    config at 48 and the image pointer at 112 (120 bytes)."""
+    assert C.sizeof(S.Job) == 120 and S.Job.cfg.offset == 48 and S.Job.image_out.offset == 112
+    assert C.sizeof(S.RenderCfg) == 64

@@ -1,0 +1,52 @@
+"""Batched rendering (ppm_batch_render): every job's image equals the image
+ppm_render gives for that job alone (same seed and configuration), up to the
+order of floating-point atomic adds; jobs with fewer passes drop out at the
+right pass; the cell-size autotuner changes nothing but speed."""
+import numpy as np
+import pytest
+
+from ppmpa_gb300 import MIXED, PLAIN, Batch, Context, RenderConfig, mesh as M, scene as S, workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _jobs():
+    rng = np.random.default_rng(3)
+    return [
+        (S.box_scene("c1"), S.box_camera(64), RenderConfig(nphoton=30000, passes=4, radius0=0.08, seed=11)),
+        (S.box_scene("c2"), S.box_camera(96), RenderConfig(nphoton=50000, passes=2, radius0=0.06, alpha=0.5,
+                                                           precision=PLAIN, seed=12)),
+        (M.mesh_scene(3), S.box_camera(80), RenderConfig(nphoton=40000, passes=3, radius0=0.07, seed=13)),
+        (W.batch_scene(rng, 3000), S.box_camera(72), RenderConfig(nphoton=20000, passes=5, radius0=0.05, seed=14)),
+        (W.batch_scene(rng, 40), S.box_camera(64), RenderConfig(nphoton=60000, passes=1, radius0=0.09, seed=15,
+                                                               precision=PLAIN)),
+    ]
+
+
+def test_batch_images_equal_single_renders():
+    jobs = _jobs()
+    with Batch(0, seed=1) as b:
+        imgs, ms = b.render(jobs)
+    assert ms > 0
+    with Context(0, seed=1) as ctx:
+        for (sc, cam, cfg), img in zip(jobs, imgs):
+            ctx.upload_scene(sc)
+            ctx.set_camera(cam)
+            want = ctx.render(cfg)
+            tol = 1e-10 if cfg.precision == PLAIN else 1e-5
+            assert img.shape == want.shape
+            assert np.allclose(img, want, rtol=tol, atol=tol * want.max()), cfg
+            assert want.max() > 0
+
+
+def test_cell_tuning_changes_only_speed():
+    sc, cam = S.box_scene("c2"), S.box_camera(96)
+    with Context(0, seed=1) as ctx:
+        ctx.upload_scene(sc)
+        ctx.set_camera(cam)
+        base = dict(nphoton=50000, passes=3, radius0=0.06, seed=21, precision=MIXED)
+        imgs = {cf: ctx.render(RenderConfig(cell_factor=cf, **base)) for cf in (1, 2)}
+        tuned = ctx.render(RenderConfig(flags=1, **base))
+        cf = ctx.stats()["cell_factor"]
+        assert cf in (1, 2)
+        assert np.allclose(tuned, imgs[cf], rtol=1e-5, atol=1e-5 * tuned.max())
