@@ -251,6 +251,14 @@ def run_gpu(args, w):
     ctx = Context(local, seed=args.seed)
     ctx.upload_scene(sc)
     ctx.set_camera(cam)
+    leaf = None
+    if ctx.accel_info()["bvh_objects"]:
+        # BVH leaf size: timed on 256k random rays through the box
+        rng = np.random.default_rng(args.seed + 17)
+        p = rng.uniform((-0.95, 0.05, 0.05), (0.95, 1.95, 1.95), (262144, 3))
+        d = rng.normal(size=(262144, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        leaf, leaf_ms = ctx.tune_bvh_leaf(np.hstack([p, d]))
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
 
@@ -382,7 +390,7 @@ def run_gpu(args, w):
         "value": value, "unit": "Mphotons/s", "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 trace/gather, f64 radius/average", "data": "synthetic (seeded scene, seeded photon streams)",
-        "config": {"workload": args.workload, **w, "precision": "mixed", "cuda_graph": True,
+        "config": {"workload": args.workload, **w, "precision": "mixed", "cuda_graph": True, "bvh_leaf": leaf,
                    "l2": "flushed between timed passes (2x L2 write)", "parallelism": f"passes x{world}"},
         "plain_fp64": {"value": value_plain, "unit": "Mphotons/s", "ms_per_step": ms_plain / steps_plain,
                        "mixed_over_plain": value / value_plain},

@@ -194,6 +194,13 @@ const char *ppm_parse_error(void);
  * the hierarchy from 2 objects, PPM_ACCEL_NONE the loop; applies at once. */
 enum { PPM_ACCEL_AUTO = 0, PPM_ACCEL_BVH = 1, PPM_ACCEL_NONE = 2 };
 int  ppm_set_accel(ppm_ctx *ctx, int32_t mode);
+/* objects per BVH leaf (1..8, default 1; leaves are runs of the Morton-ordered
+ * objects); rebuilds the tree at once.  No reference counterpart. */
+int  ppm_set_bvh_leaf(ppm_ctx *ctx, int32_t leaf_max);
+/* Leaf-size autotuner: builds the tree with 1, 2, 4 and 8 objects per leaf,
+ * times the FP32 first-hit kernel over the given rays (n x 6) and keeps the
+ * fastest; returns it and its time.  No reference counterpart. */
+int  ppm_tune_bvh_leaf(ppm_ctx *ctx, const double *rays, int64_t n, int32_t *best_leaf, double *best_ms);
 /* objects in the hierarchy (0: none) and unbounded objects tested per ray */
 int  ppm_accel_info(ppm_ctx *ctx, int32_t *bvh_objects, int32_t *unbounded);
 /* Host helpers: camera.rs:150-175 and Surface::new_simple/new_ts (surface.rs:45-66). */

@@ -48,6 +48,8 @@ SIGNATURES = {
     "ppm_query_within_f32": (C.c_int, [_P, _fp, C.c_int64, _dp, _i64p, _i32p, C.c_int64, _i64p]),
     "ppm_estimate_f32": (C.c_int, [_P, _fp, _fp, C.c_int64, _dp, _dp]),
     "ppm_set_accel": (C.c_int, [_P, C.c_int32]),
+    "ppm_set_bvh_leaf": (C.c_int, [_P, C.c_int32]),
+    "ppm_tune_bvh_leaf": (C.c_int, [_P, _dp, C.c_int64, C.POINTER(C.c_int32), _dp]),
     "ppm_eye_pass": (C.c_int, [_P, C.c_int32, C.c_uint64, C.c_int32, _dp]),
     "ppm_tone_map": (C.c_int, [_dp, C.c_int64, C.c_double, C.POINTER(C.c_int32)]),
     "ppm_write_exr": (C.c_int, [C.c_char_p, _dp, C.c_int32, C.c_int32, C.c_double]),

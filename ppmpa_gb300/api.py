@@ -211,6 +211,17 @@ class Context:
         """0 automatic (BVH from 32 bounded objects), 1 BVH, 2 loop over the objects."""
         self._check(self.lib.ppm_set_accel(self.h, int(mode)))
 
+    def set_bvh_leaf(self, leaf_max: int):
+        self._check(self.lib.ppm_set_bvh_leaf(self.h, int(leaf_max)))
+
+    def tune_bvh_leaf(self, rays):
+        """Picks the BVH leaf size (1, 2, 4, 8) fastest for these rays (n x 6); returns (leaf, ms)."""
+        rays = np.ascontiguousarray(rays, np.float64).reshape(-1, 6)
+        leaf, ms = C.c_int32(), C.c_double()
+        self._check(self.lib.ppm_tune_bvh_leaf(self.h, _ptr(rays, C.c_double), rays.shape[0], C.byref(leaf),
+                                               C.byref(ms)))
+        return leaf.value, ms.value
+
     def accel_info(self) -> dict:
         m, u = C.c_int32(), C.c_int32()
         self._check(self.lib.ppm_accel_info(self.h, C.byref(m), C.byref(u)))

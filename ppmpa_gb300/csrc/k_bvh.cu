@@ -8,10 +8,11 @@
 //   5. hierarchy: Karras, "Maximizing parallelism in the construction of
 //      BVHs, octrees and k-d trees" (HPG 2012) -- node i finds its key range
 //      and split from the longest common prefixes of the sorted codes
-//      (ties between equal codes broken by position);
-//   6. refit bottom-up: each leaf climbs; of the two threads reaching a node
-//      the second (atomic counter) merges the children's boxes and carries
-//      on, so no thread ever waits.
+//      (ties between equal codes broken by position); a child whose range
+//      holds at most leaf_max (1..8) objects becomes a leaf run;
+//   6. refit bottom-up: of the two threads supplying a node's child boxes
+//      the second (atomic counter) merges them and carries on to the
+//      parent, so no thread ever waits.
 // Layout of the nodes: ppm_bvh.cuh.
 #include <algorithm>
 #include <utility>
@@ -229,8 +230,10 @@ __device__ __forceinline__ int delta(const uint32_t *code, int m, int i, int j) 
     return __clz(a ^ b);
 }
 
-__global__ void k_bvh_karras(const uint32_t *code, const uint32_t *pos, const int32_t *bounded, int m, BvhNode *nodes,
-                             int32_t *leaf_parent) {
+// Children whose key range holds at most leaf_max objects become leaves:
+// ~(first << 3 | (count - 1)), a run of the Morton-ordered object list.
+// Internal nodes inside such runs stay unreachable (parent -1).
+__global__ void k_bvh_karras(const uint32_t *code, const int32_t *order, int m, int leaf_max, BvhNode *nodes) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m - 1) return;
     const int d = delta(code, m, i, i + 1) > delta(code, m, i, i - 1) ? 1 : -1;
@@ -249,14 +252,25 @@ __global__ void k_bvh_karras(const uint32_t *code, const uint32_t *pos, const in
     } while (t > 1);
     const int g = i + s * d + min(d, 0);
     const int lo = min(i, j), hi = max(i, j);
+    const int nl = g - lo + 1, nr = hi - g;
     int left, right;
-    if (lo == g) { left = ~bounded[pos[g]]; leaf_parent[g] = i; }
-    else { left = g; nodes[g].d.z = i; }
-    if (hi == g + 1) { right = ~bounded[pos[g + 1]]; leaf_parent[g + 1] = i; }
-    else { right = g + 1; nodes[g + 1].d.z = i; }
+    // one object per leaf: the leaf is ~object itself (no indirection)
+    if (nl <= leaf_max) left = leaf_max == 1 ? ~order[lo] : ~((lo << 3) | (nl - 1));
+    else { left = g; nodes[g].d.z = i; nodes[g].d.w = 0; }
+    if (nr <= leaf_max) right = leaf_max == 1 ? ~order[g + 1] : ~(((g + 1) << 3) | (nr - 1));
+    else { right = g + 1; nodes[g + 1].d.z = i; nodes[g + 1].d.w = 1; }
     nodes[i].d.x = left;
     nodes[i].d.y = right;
-    if (i == 0) nodes[0].d.z = -1;
+    if (i == 0) { nodes[0].d.z = -1; nodes[0].d.w = 0; }
+}
+
+// order[k]: the object at sorted position k; inv_order[object]: its position
+__global__ void k_bvh_order(const uint32_t *pos, const int32_t *bounded, int m, int32_t *order, int32_t *inv_order) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < m) {
+        order[k] = bounded[pos[k]];
+        inv_order[bounded[pos[k]]] = k;
+    }
 }
 
 __device__ __forceinline__ void put_box(BvhNode &n, bool right, float4 lo, float4 hi) {
@@ -269,48 +283,71 @@ __device__ __forceinline__ void put_box(BvhNode &n, bool right, float4 lo, float
     }
 }
 
-// leaf k (sorted position) carries the box of bounded[pos[k]] up the tree
-__global__ void k_bvh_refit(const uint32_t *pos, const int32_t *bounded, const float4 *blo, const float4 *bhi, int m,
-                            BvhNode *nodes, const int32_t *leaf_parent, uint32_t *visits) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= m) return;
-    float4 lo = blo[pos[k]], hi = bhi[pos[k]];
-    int child = ~bounded[pos[k]];   // the child as its parent stores it
-    int p = leaf_parent[k];
-    while (p >= 0) {
-        const int4 dd = nodes[p].d;
-        put_box(nodes[p], dd.y == child, lo, hi);
-        __threadfence();
-        if (atomicAdd(&visits[p], 1u) == 0u) return;   // the sibling's thread finishes this node
+__device__ __forceinline__ void leaf_box(const uint32_t *pos, const float4 *blo, const float4 *bhi, int enc,
+                                         int leaf_max, const int32_t *inv_order, float4 &lo, float4 &hi) {
+    const int r = ~enc;
+    const int first = leaf_max == 1 ? inv_order[r] : r >> 3, n = leaf_max == 1 ? 1 : (r & 7) + 1;
+    lo = blo[pos[first]];
+    hi = bhi[pos[first]];
+    for (int k = 1; k < n; k++) {
+        const float4 a = blo[pos[first + k]], b = bhi[pos[first + k]];
+        lo = make_float4(fminf(lo.x, a.x), fminf(lo.y, a.y), fminf(lo.z, a.z), 0.0f);
+        hi = make_float4(fmaxf(hi.x, b.x), fmaxf(hi.y, b.y), fmaxf(hi.z, b.z), 0.0f);
+    }
+}
+
+// Bottom-up boxes.  Thread i writes the boxes of node i's leaf children;
+// whichever thread supplies a node's second child box completes it (union
+// of the two) and carries that box to the parent's slot (side d.w), so no
+// thread waits for another.
+__global__ void k_bvh_refit(const uint32_t *pos, const float4 *blo, const float4 *bhi, int m, int leaf_max,
+                            const int32_t *inv_order, BvhNode *nodes, uint32_t *visits) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m - 1) return;
+    const int4 d0 = nodes[i].d;
+    uint32_t r = 0;
+    float4 lo, hi;
+    if (d0.x < 0) { leaf_box(pos, blo, bhi, d0.x, leaf_max, inv_order, lo, hi); put_box(nodes[i], false, lo, hi); r++; }
+    if (d0.y < 0) { leaf_box(pos, blo, bhi, d0.y, leaf_max, inv_order, lo, hi); put_box(nodes[i], true, lo, hi); r++; }
+    if (r == 0) return;
+    __threadfence();
+    int p = i;
+    uint32_t add = r;
+    for (;;) {
+        if (atomicAdd(&visits[p], add) + add < 2u) return;   // the other child's thread completes p
         __threadfence();
         const float4 a = __ldcg(&nodes[p].a), b = __ldcg(&nodes[p].b), c = __ldcg(&nodes[p].c);
         lo = make_float4(fminf(a.x, b.x), fminf(a.z, b.z), fminf(c.x, c.z), 0.0f);
         hi = make_float4(fmaxf(a.y, b.y), fmaxf(a.w, b.w), fmaxf(c.y, c.w), 0.0f);
-        child = p;
-        p = dd.z;
+        const int4 dp = __ldcg(&nodes[p].d);
+        if (dp.z < 0) return;                                 // the root, or a node inside a leaf run
+        put_box(nodes[dp.z], dp.w != 0, lo, hi);
+        __threadfence();
+        p = dp.z;
+        add = 1;
     }
 }
 
 }  // namespace
 
-int bvh_scratch_words(int m) {
+int bvh_scratch_words(int m, int n_objs) {
     const int nb = (m + RADIX_TILE - 1) / RADIX_TILE;
-    // blo, bhi, centroid (4 words each), code x2, pos x2, hist, leaf_parent, visits, bounds
-    return 12 * m + 4 * m + 256 * nb + m + m + 8;
+    // blo, bhi, centroid (4 words each), code x2, pos x2, hist, visits, bounds;
+    // inv_order (one word per scene object, n_objs >= m) comes after
+    return 12 * m + 4 * m + 256 * nb + m + 8 + n_objs;
 }
 
-void launch_bvh_build(const DObject<double> *objs, const int32_t *bounded, int m, BvhNode *nodes, uint32_t *scratch,
-                      cudaStream_t s) {
-    if (m < 2) return;
+int launch_bvh_build(const DObject<double> *objs, const int32_t *bounded, int m, int n_objs, int leaf_max,
+                     BvhNode *nodes, int32_t *order, uint32_t *scratch, cudaStream_t s) {
     const int nb = (m + RADIX_TILE - 1) / RADIX_TILE;
     float4 *blo = (float4 *)scratch;
     float4 *bhi = blo + m;
     float4 *cen = bhi + m;
     uint32_t *code = (uint32_t *)(cen + m), *code2 = code + m, *pos = code2 + m, *pos2 = pos + m;
     uint32_t *hist = pos2 + m;
-    int32_t *leaf_parent = (int32_t *)(hist + 256 * nb);
-    uint32_t *visits = (uint32_t *)(leaf_parent + m);
+    uint32_t *visits = hist + 256 * nb;
     uint32_t *cb = visits + m;
+    int32_t *inv_order = (int32_t *)(cb + 8);   // n_objs words
     const int g = (m + 255) / 256;
     k_bvh_bounds<<<g, 256, 0, s>>>(objs, bounded, m, blo, bhi, cen);
     k_bvh_init_bounds<<<1, 32, 0, s>>>(cb);
@@ -323,9 +360,13 @@ void launch_bvh_build(const DObject<double> *objs, const int32_t *bounded, int m
         std::swap(code, code2);
         std::swap(pos, pos2);
     }
+    k_bvh_order<<<g, 256, 0, s>>>(pos, bounded, m, order, inv_order);
+    if (m <= leaf_max) return leaf_max == 1 ? ~bounded[0] : ~(m - 1);   // one leaf: the whole run
+    cudaMemsetAsync(nodes, 0xff, sizeof(BvhNode) * (size_t)(m - 1), s);   // parents -1 until linked
     cudaMemsetAsync(visits, 0, sizeof(uint32_t) * m, s);
-    k_bvh_karras<<<(m - 1 + 255) / 256, 256, 0, s>>>(code, pos, bounded, m, nodes, leaf_parent);
-    k_bvh_refit<<<g, 256, 0, s>>>(pos, bounded, blo, bhi, m, nodes, leaf_parent, visits);
+    k_bvh_karras<<<(m - 1 + 255) / 256, 256, 0, s>>>(code, order, m, leaf_max, nodes);
+    k_bvh_refit<<<(m - 1 + 255) / 256, 256, 0, s>>>(pos, blo, bhi, m, leaf_max, inv_order, nodes, visits);
+    return 0;
 }
 
 }  // namespace ppm

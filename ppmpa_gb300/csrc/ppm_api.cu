@@ -53,8 +53,9 @@ struct ppm_ctx {
     std::vector<ppm_material> mats;
     std::vector<ppm_light> lights;
     DevBuf objs_d, mats_d, lights_d, objs_f, mats_f, lights_f;
-    DevBuf bvh_nodes, bvh_bounded, bvh_unb;   // hierarchy over the bounded objects
+    DevBuf bvh_nodes, bvh_bounded, bvh_unb, bvh_order;   // hierarchy over the bounded objects
     int accel_mode = 0;                        // PPM_ACCEL_*
+    int bvh_leaf = 1;                          // objects per leaf (1..8)
     int bvh_m = 0;                             // objects in the hierarchy (0: none)
     SceneView<double> sv_d{};
     SceneView<float> sv_f{};
@@ -471,7 +472,7 @@ extern "C" int ppm_ctx_destroy(ppm_ctx *ctx) {
                       &ctx->raw_d, &ctx->spos, &ctx->sdir, &ctx->raw_f, &ctx->sorted_f, &ctx->sidx,
                       &ctx->keyrank, &ctx->count, &ctx->start, &ctx->block_sums, &ctx->hits_d, &ctx->hits_f,
                       &ctx->pass_img, &ctx->sum_img, &ctx->scratch, &ctx->pass_direct32, &ctx->pass_gather32,
-                      &ctx->qstart, &ctx->bvh_nodes, &ctx->bvh_bounded, &ctx->bvh_unb};
+                      &ctx->qstart, &ctx->bvh_nodes, &ctx->bvh_bounded, &ctx->bvh_unb, &ctx->bvh_order};
     for (DevBuf *b : bufs) release(*b);
     for (DevBuf &b : ctx->rq) release(b);
     for (DevBuf &b : ctx->eqb) release(b);
@@ -516,19 +517,23 @@ static int build_accel(ppm_ctx *ctx) {
     const int m = (int)bounded.size();
     const bool use = ctx->accel_mode == PPM_ACCEL_BVH ? m >= 2
                    : ctx->accel_mode == PPM_ACCEL_NONE ? false : m >= BVH_MIN_OBJECTS;
-    ctx->sv_d.bvh = nullptr; ctx->sv_d.unb = nullptr; ctx->sv_d.n_unb = 0; ctx->sv_d.bvh_root = 0; ctx->sv_d.bvh_steps = 0;
-    ctx->sv_f.bvh = nullptr; ctx->sv_f.unb = nullptr; ctx->sv_f.n_unb = 0; ctx->sv_f.bvh_root = 0; ctx->sv_f.bvh_steps = 0;
+    for (auto *v : {&ctx->sv_d}) { v->bvh = nullptr; v->bvh_order = nullptr; v->unb = nullptr; v->n_unb = 0; v->bvh_root = 0; v->bvh_steps = 0; }
+    for (auto *v : {&ctx->sv_f}) { v->bvh = nullptr; v->bvh_order = nullptr; v->unb = nullptr; v->n_unb = 0; v->bvh_root = 0; v->bvh_steps = 0; }
     ctx->bvh_m = 0;
     if (!use) return PPM_OK;
     if (m > (1 << 28)) return set_err(ctx, PPM_ERR_INVALID_ARG, "at most 2^28 bounded objects");
     TRY(upload_vec(ctx, ctx->bvh_bounded, bounded));
     if (!unb.empty()) TRY(upload_vec(ctx, ctx->bvh_unb, unb));
     TRY(ensure(ctx, ctx->bvh_nodes, sizeof(BvhNode) * (size_t)(m - 1)));
+    TRY(ensure(ctx, ctx->bvh_order, sizeof(int32_t) * (size_t)m));
     DevBuf scratch;
-    if (cudaMalloc(&scratch.p, sizeof(uint32_t) * (size_t)bvh_scratch_words(m)) != cudaSuccess)
+    const int n_objs = (int)ctx->objs.size();
+    if (cudaMalloc(&scratch.p, sizeof(uint32_t) * (size_t)bvh_scratch_words(m, n_objs)) != cudaSuccess)
         return set_err(ctx, PPM_ERR_OOM, "no device memory for the BVH build of %d objects", m);
-    launch_bvh_build(as<DObject<double>>(ctx->objs_d), as<int32_t>(ctx->bvh_bounded), m, as<BvhNode>(ctx->bvh_nodes),
-                     as<uint32_t>(scratch), ctx->s);
+    const int root = launch_bvh_build(as<DObject<double>>(ctx->objs_d), as<int32_t>(ctx->bvh_bounded), m, n_objs,
+                                      ctx->bvh_leaf,
+                                      as<BvhNode>(ctx->bvh_nodes), as<int32_t>(ctx->bvh_order), as<uint32_t>(scratch),
+                                      ctx->s);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->s);
     cudaFree(scratch.p);
@@ -536,8 +541,12 @@ static int build_accel(ppm_ctx *ctx) {
     const BvhNode *nodes = as<BvhNode>(ctx->bvh_nodes);
     const int32_t *u = unb.empty() ? nullptr : as<int32_t>(ctx->bvh_unb);
     const int32_t steps = 2 * m + 64;
+    const int32_t *order = as<int32_t>(ctx->bvh_order);
     ctx->sv_d.bvh = nodes; ctx->sv_d.unb = u; ctx->sv_d.n_unb = (int32_t)unb.size(); ctx->sv_d.bvh_steps = steps;
     ctx->sv_f.bvh = nodes; ctx->sv_f.unb = u; ctx->sv_f.n_unb = (int32_t)unb.size(); ctx->sv_f.bvh_steps = steps;
+    ctx->sv_d.bvh_order = order; ctx->sv_f.bvh_order = order;
+    ctx->sv_d.bvh_root = root; ctx->sv_f.bvh_root = root;
+    ctx->sv_d.bvh_runs = ctx->sv_f.bvh_runs = ctx->bvh_leaf > 1 ? 1 : 0;
     ctx->bvh_m = m;
     return PPM_OK;
 }
@@ -601,6 +610,63 @@ extern "C" int ppm_set_accel(ppm_ctx *ctx, int32_t mode) {
     ctx->render_ready = false;
     drop_graph(ctx);
     return build_accel(ctx);
+}
+
+extern "C" int ppm_set_bvh_leaf(ppm_ctx *ctx, int32_t leaf_max) {
+    if (!ctx || leaf_max < 1 || leaf_max > 8) return PPM_ERR_INVALID_ARG;
+    ctx->bvh_leaf = leaf_max;
+    if (!ctx->have_scene) return PPM_OK;
+    cudaSetDevice(ctx->device);
+    ctx->render_ready = false;
+    drop_graph(ctx);
+    return build_accel(ctx);
+}
+
+// Leaf-size autotuner: rebuilds the tree with 1, 2, 4 and 8 objects per leaf,
+// times the FP32 first-hit kernel over the caller's rays (best of two) and
+// keeps the fastest tree.
+extern "C" int ppm_tune_bvh_leaf(ppm_ctx *ctx, const double *rays, int64_t n, int32_t *best_leaf, double *best_ms) {
+    if (!ctx || !rays || n <= 0) return PPM_ERR_INVALID_ARG;
+    if (!ctx->have_scene) return set_err(ctx, PPM_ERR_NOT_READY, "no scene");
+    cudaSetDevice(ctx->device);
+    const size_t rb = sizeof(double) * 6 * n, tb = sizeof(double) * n, ob = sizeof(int32_t) * n;
+    TRY(ensure(ctx, ctx->scratch, rb + tb + ob + 64));
+    char *base = as<char>(ctx->scratch);
+    double *d_r = (double *)base, *d_t = (double *)(base + rb);
+    int32_t *d_o = (int32_t *)(base + rb + tb);
+    CK(cudaMemcpyAsync(d_r, rays, rb, cudaMemcpyHostToDevice, ctx->s));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return set_err(ctx, PPM_ERR_CUDA, "event"); }
+    int best = ctx->bvh_leaf, rc = PPM_OK;
+    float best_t = 1e30f;
+    for (int leaf : {1, 2, 4, 8}) {
+        ctx->bvh_leaf = leaf;
+        if ((rc = build_accel(ctx)) != PPM_OK) break;
+        float t = 1e30f;
+        for (int rep = 0; rep < 2 && rc == PPM_OK; rep++) {
+            float ms = 0.0f;
+            cudaError_t e = cudaEventRecord(e0, ctx->s);
+            if (e == cudaSuccess) launch_intersect_f(ctx->sv_f, d_r, n, d_t, d_o, ctx->s);
+            if (e == cudaSuccess) e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->s);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e != cudaSuccess) rc = set_err(ctx, PPM_ERR_CUDA, "leaf tuner: %s", cudaGetErrorString(e));
+            t = std::min(t, ms);
+        }
+        if (rc == PPM_OK && t < best_t) { best_t = t; best = leaf; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != PPM_OK) return rc;
+    ctx->bvh_leaf = best;
+    ctx->render_ready = false;
+    drop_graph(ctx);
+    TRY(build_accel(ctx));
+    if (best_leaf) *best_leaf = best;
+    if (best_ms) *best_ms = best_t;
+    return PPM_OK;
 }
 
 extern "C" int ppm_accel_info(ppm_ctx *ctx, int32_t *bvh_objects, int32_t *unbounded) {
@@ -1353,8 +1419,11 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
     if (ev) CK(cudaEventRecord(ev[7], s));
     if (mixed) {
         GatherOutF go{as<float>(ctx->pass_gather32), nullptr, ctx->count_gather ? &ctx->st->candidates : nullptr};
+        // above 2M photons per pass the stored map (1-3 photons of 16 B per
+        // emitted one) fills most of L2 or more: queries come from a counter
+        const bool dyn = ctx->cfg.nphoton > 2000000;
         launch_gather_f(as<HitPoint<float>>(ctx->hits_f), ctx->st, -1, as<float4>(ctx->sorted_f), as<uint32_t>(ctx->start),
-                        ctx->pw, nullptr, ctx->cam.pfilter, 0, go, g8, s);
+                        ctx->pw, nullptr, ctx->cam.pfilter, 0, go, g8, s, dyn);
     } else {
         GatherOutD go{as<double>(ctx->pass_img), nullptr, nullptr};
         launch_gather_d(as<HitPoint<double>>(ctx->hits_d), ctx->st, -1, as<double4>(ctx->spos), as<double4>(ctx->sdir),

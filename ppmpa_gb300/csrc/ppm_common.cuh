@@ -327,16 +327,19 @@ struct SceneView {
     int32_t n_objs, n_mats, n_lights;
     int32_t bvh_root;          // root node (>= 0), or ~object when one object is bounded
     const BvhNode *bvh;
+    const int32_t *bvh_order;  // objects in Morton order (leaves are runs of it)
     const int32_t *unb;
     int32_t n_unb;
     int32_t bvh_steps;         // bound on one walk: 2 * objects in the tree + 64
+    int32_t bvh_runs;          // leaves are runs of bvh_order (leaf size > 1)
+    int32_t pad;
 };
 
 // the same tables typed for the kernels that walk the hierarchy
 template <typename T>
 __host__ __device__ inline SceneView<T, true> with_bvh(const SceneView<T, false> &v) {
     return SceneView<T, true>{v.objs, v.mats, v.lights, v.n_objs, v.n_mats, v.n_lights, v.bvh_root,
-                              v.bvh, v.unb, v.n_unb, v.bvh_steps};
+                              v.bvh, v.bvh_order, v.unb, v.n_unb, v.bvh_steps, v.bvh_runs, 0};
 }
 
 // Emission bookkeeping (src/bin/ppmpa.rs:30-31): light l owns emission

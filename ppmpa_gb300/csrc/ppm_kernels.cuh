@@ -218,8 +218,13 @@ __global__ void __launch_bounds__(256) k_emit(SceneView<T> sc, EmitPlan plan, ui
 
 // one bounce level of trace_photon (tracer.rs:31-125) for every live ray;
 // continuing rays are compacted into the next level's queue
+// resident blocks of 256 threads asked of the bounce kernel: 4 in FP32 (fits
+// in 64 registers without spills), 2 in FP64 (as many as its registers allow)
+template <typename T> struct BounceBlocks { static constexpr int value = 2; };
+template <> struct BounceBlocks<float> { static constexpr int value = 4; };
+
 template <typename T, bool B>
-__global__ void __launch_bounds__(256) k_bounce(SceneView<T, B> sc, uint64_t seed, PassState *st, int uc, int level,
+__global__ void __launch_bounds__(256, BounceBlocks<T>::value) k_bounce(SceneView<T, B> sc, uint64_t seed, PassState *st, int uc, int level,
                                                 long long n_level0, RayQueue<T> in, RayQueue<T> out,
                                                 unsigned long long qcap, PhotonBuf<T> photons) {
     const uint32_t pass = (uint32_t)st->pass;
@@ -840,27 +845,35 @@ struct GatherOutF {
 #if defined(PPM_BUILD_F32)
 constexpr unsigned GATHER_CHUNK = 4;   // queries a warp takes per counter increment
 
-// PERQ: per-query radii (the estimate entry point); otherwise the pass radius
-template <bool COUNT, bool PERQ>
+// PERQ: per-query radii (the estimate entry point); otherwise the pass radius.
+// DYN: queries handed out by a counter (maps larger than L2), see below.
+template <bool COUNT, bool PERQ, bool DYN>
 __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed,
                                                   const float4 *smap, const uint32_t *start, double pw,
                                                   const double *q_r2, int pfilter, int mode, GatherOutF out) {
     const unsigned long long nq = n_hitpoints(st, n_fixed);
     const GridParams g = st->grid;
     const unsigned lane = lane_id();
-    // Warps take GATHER_CHUNK queries at a time from a counter, so the
-    // queries in flight stay a narrow window of the (cell-ordered) batch and
-    // their photons stay in L2; a fixed warp stride lets slow warps fall
-    // behind and spreads the window over the whole map.
-    unsigned long long qi = 0, qend = 0;
+    // Maps larger than L2 (DYN): warps take GATHER_CHUNK queries at a time
+    // from a counter, so the queries in flight stay a narrow window of the
+    // (spatially ordered) batch and their photons stay in L2; a fixed warp
+    // stride lets slow warps fall behind and spreads the window over the
+    // whole map.  When the map fits in L2 the fixed stride is cheaper.
+    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    unsigned long long qi = DYN ? 0ull : (((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    unsigned long long qend = DYN ? 0ull : nq;
     for (;;) {
-        if (qi == qend) {
-            unsigned long long c = 0;
-            if (lane == 0) c = atomicAdd(&st->gather_next, (unsigned long long)GATHER_CHUNK);
-            c = __shfl_sync(0xffffffffu, c, 0);
-            if (c >= nq) break;
-            qi = c;
-            qend = c + GATHER_CHUNK < nq ? c + GATHER_CHUNK : nq;
+        if constexpr (DYN) {
+            if (qi == qend) {
+                unsigned long long c = 0;
+                if (lane == 0) c = atomicAdd(&st->gather_next, (unsigned long long)GATHER_CHUNK);
+                c = __shfl_sync(0xffffffffu, c, 0);
+                if (c >= nq) break;
+                qi = c;
+                qend = c + GATHER_CHUNK < nq ? c + GATHER_CHUNK : nq;
+            }
+        } else {
+            if (qi >= nq) break;
         }
         const HitPoint<float> h = hits[qi];
         double r2;
@@ -935,7 +948,7 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
                 o[2] = (double)s2 * kk;
             }
         }
-        ++qi;
+        qi += DYN ? 1ull : nwarps;
     }
 }
 

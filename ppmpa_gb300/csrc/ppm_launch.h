@@ -47,9 +47,11 @@ void launch_eye_level_f(const SceneView<float> &sc, const DCamera<float> &cam, u
                         int level, EyeQueue<float> in, EyeQueue<float> out, unsigned long long qcap,
                         HitPoint<float> *hits, EyeOut<float> pix, int grid, cudaStream_t s,
                         bool classic = false);
+// per-query radii (q_r2) always take queries from the counter; otherwise dyn
+// chooses it (maps larger than L2)
 void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
                      const uint32_t *start, double pw, const double *q_r2, int pfilter, int mode, GatherOutF out,
-                     int grid, cudaStream_t s);
+                     int grid, cudaStream_t s, bool dyn = false);
 void launch_within_f(const float *q, long long nq, const double *q_r2, const PassState *st, const float4 *smap,
                      const uint32_t *start, const int32_t *sidx, unsigned long long *counts,
                      const unsigned long long *offsets, int32_t *idx_out, int grid, cudaStream_t s);
@@ -65,10 +67,12 @@ void launch_pack_photons_f(const float *pos, const float *dir, const uint8_t *wl
 
 // ---- BVH over the bounded objects (k_bvh.cu) --------------------------------------
 // 32-bit words of device scratch launch_bvh_build needs for m objects
-int bvh_scratch_words(int m);
-// builds the m - 1 internal nodes over objs[bounded[0..m)] (m >= 2)
-void launch_bvh_build(const DObject<double> *objs, const int32_t *bounded, int m, BvhNode *nodes, uint32_t *scratch,
-                      cudaStream_t s);
+int bvh_scratch_words(int m, int n_objs);
+// builds the internal nodes (at most m - 1) over objs[bounded[0..m)] with
+// leaves of at most leaf_max (1..8) objects and the Morton-ordered object
+// list `order`; returns the root (0, or a leaf when m <= leaf_max)
+int launch_bvh_build(const DObject<double> *objs, const int32_t *bounded, int m, int n_objs, int leaf_max,
+                     BvhNode *nodes, int32_t *order, uint32_t *scratch, cudaStream_t s);
 
 // ---- grid / scan / pass bookkeeping ------------------------------------------------
 constexpr int SCAN_TILE = 4096;

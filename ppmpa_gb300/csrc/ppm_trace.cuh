@@ -126,7 +126,7 @@ __device__ __forceinline__ bool intersect(const SceneView<T, B> &sc, V3<T> rp, V
             }
         };
         for (int k = 0; k < sc.n_unb; k++) test(sc.unb[k]);
-        bvh_walk<T>(sc.bvh, sc.bvh_root, sc.bvh_steps, rp, rd, test,
+        bvh_walk<T>(sc.bvh, sc.bvh_order, sc.bvh_runs != 0, sc.bvh_root, sc.bvh_steps, rp, rd, test,
                     [&]() { return bi < 0 ? Cst<T>::inf() : best; });
     }
     if (bi < 0) return false;

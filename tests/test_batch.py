@@ -50,3 +50,24 @@ def test_cell_tuning_changes_only_speed():
         cf = ctx.stats()["cell_factor"]
         assert cf in (1, 2)
         assert np.allclose(tuned, imgs[cf], rtol=1e-5, atol=1e-5 * tuned.max())
+
+
+@pytest.mark.parametrize("precision,tol", [(PLAIN, 1e-12), (MIXED, 1e-6)])
+def test_pass_shards_reassemble_the_full_render(precision, tol):
+    """Passes rendered in blocks (first_pass) and averaged give the image of
+    one render of all passes: the pass-sharded multi-GPU path, run as two
+    shards one after another on one GPU."""
+    from ppmpa_gb300.shard import context_renderer, render_sharded
+    sc, cam = S.box_scene("c2"), S.box_camera(64)
+    cfg = RenderConfig(nphoton=30000, passes=6, radius0=0.08, precision=precision, seed=31)
+    with Context(0, seed=1) as ctx:
+        ctx.upload_scene(sc)
+        ctx.set_camera(cam)
+        full = ctx.render(cfg)
+        run = context_renderer(ctx, cfg)
+        parts = [render_sharded(run, 6, r, 2, reduce_sum=lambda a: a) for r in range(2)]
+        # rank 0's block plus rank 1's block, as the reduction would add them
+        from ppmpa_gb300.shard import shard_passes
+        total = sum(run(*shard_passes(6, r, 2)) for r in range(2)) / 6.0
+    assert np.allclose(total, full, rtol=tol, atol=tol * full.max())
+    assert parts[1] is None

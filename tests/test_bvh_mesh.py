@@ -34,9 +34,11 @@ def _rays(rng, n):
     return np.hstack([p, d])
 
 
-@pytest.mark.parametrize("level,nrays", [(1, 20000), (4, 20000), (6, 4000)])
-def test_bvh_first_hits_match_oracle_loop(ctx, level, nrays):
+@pytest.mark.parametrize("level,nrays,leaf", [(1, 20000, 1), (4, 20000, 1), (6, 4000, 1), (4, 20000, 2),
+                                              (4, 20000, 4), (6, 4000, 8), (1, 2000, 8)])
+def test_bvh_first_hits_match_oracle_loop(ctx, level, nrays, leaf):
     sc = M.mesh_scene(level)
+    ctx.set_bvh_leaf(leaf)
     ctx.upload_scene(sc)
     ctx.set_accel(BVH)
     assert ctx.accel_info()["bvh_objects"] == sc.n_objects
@@ -97,3 +99,17 @@ def test_full_mesh_builds_and_renders(ctx):
     for img in imgs:
         assert np.isfinite(img).all() and img.mean() > 0
     assert abs(imgs[1].mean() / imgs[0].mean() - 1) < 0.1
+
+
+def test_leaf_tuner_keeps_answers(ctx):
+    sc = M.mesh_scene(5)
+    ctx.set_bvh_leaf(1)
+    ctx.upload_scene(sc)
+    ctx.set_accel(0)
+    rays = _rays(np.random.default_rng(21), 30000)
+    want = ctx.intersect(rays)
+    leaf, ms = ctx.tune_bvh_leaf(rays)
+    assert leaf in (1, 2, 4, 8) and ms > 0
+    got = ctx.intersect(rays)
+    assert all(np.array_equal(a, b) for a, b in zip(got, want))
+    ctx.set_bvh_leaf(1)

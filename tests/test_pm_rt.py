@@ -68,8 +68,16 @@ def test_classic_tracer_matches_oracle(built_lib):
             want = Oracle(sc, cam).classic_pass(seed=9, pass_index=0)
             assert want.max() > 0
             assert np.allclose(got, want, rtol=1e-9, atol=1e-12 * want.max())
-            mixed = ctx.render(RenderConfig(nphoton=1, passes=1, precision=MIXED, seed=9, flags=RENDER_CLASSIC))
-            assert abs(mixed.mean() / want.mean() - 1) < 1e-3
+    # FP32 draws its camera jitter from 32-bit words (another sample), so
+    # the precisions are compared on a camera without jitter or lens blur
+    sc = S.reference_scene()
+    cam = S.make_camera(48, 40, antialias=False, blur=False)
+    with Context(0, seed=9) as ctx:
+        ctx.upload_scene(sc)
+        ctx.set_camera(cam)
+        plain = ctx.render(RenderConfig(nphoton=1, passes=1, precision=PLAIN, seed=9, flags=RENDER_CLASSIC))
+        mixed = ctx.render(RenderConfig(nphoton=1, passes=1, precision=MIXED, seed=9, flags=RENDER_CLASSIC))
+        assert abs(mixed.mean() / plain.mean() - 1) < 1e-3
     out = subprocess.run([f"{TOOLS}/rtc", "cam.scr", "scene.scene", "--seed", "9"], capture_output=True, text=True,
                          check=True, timeout=120)
     lines = out.stdout.split("\n")
