@@ -75,7 +75,7 @@ def parse():
     p.add_argument("--profile", type=int, default=0,
                    help="only run this many mixed passes (one warm-up) and exit: the profiler's command")
     p.add_argument("--precision", default="mixed", choices=["mixed", "plain"])
-    p.add_argument("--cell-factor", type=int, default=0, help="grid cells per radius (0: library default)")
+    p.add_argument("--cell-factor", type=int, default=0, help="grid cells per radius (0: tuned per render)")
     p.add_argument("--nphoton", type=int, default=0, help="photons per pass (0: the workload's); for profiling")
     return p.parse_args()
 
@@ -270,7 +270,8 @@ def run_gpu(args, w):
     def cfg(precision, passes, first=0, graph=True, seed=None):
         return RenderConfig(nphoton=w["nphoton"], passes=passes, use_classic=True, radius0=w["r0"],
                             alpha=w["alpha"], schedule_offset=1, precision=precision, use_graph=graph,
-                            seed=args.seed if seed is None else seed, first_pass=first, cell_factor=args.cell_factor)
+                            seed=args.seed if seed is None else seed, first_pass=first, cell_factor=args.cell_factor,
+                            flags=1 if args.cell_factor == 0 else 0)   # 1: cell-size autotuner
 
     def timed_passes(precision, steps, warmup, seed):
         ctx.render_begin(cfg(precision, steps + warmup, seed=seed))
@@ -304,6 +305,7 @@ def run_gpu(args, w):
     clocks = Clocks(local)
     clocks.start()
     ms = timed_passes(MIXED, args.steps, max(3, args.warmup), seed_rank)
+    cells = ctx.stats()["cell_factor"]
     clk = clocks.stop()
     st = ctx.stats()
     value = world * args.steps * w["nphoton"] / (ms / 1e3) / 1e6
@@ -365,7 +367,9 @@ def run_gpu(args, w):
     for k in range(e2e_steps):
         ctx.upload_scene(sc)
         ctx.set_camera(cam)
-        img = ctx.render(cfg(MIXED, w["passes"], seed=seed_rank + 3 + k))
+        c = cfg(MIXED, w["passes"], seed=seed_rank + 3 + k)
+        c.cell_factor, c.flags = cells, 0          # the cell size tuned above, as a repeat caller passes it
+        img = ctx.render(c)
     t_e2e = time.perf_counter() - t0
     e2e_value = world * e2e_steps * w["passes"] * w["nphoton"] / t_e2e / 1e6
     import ctypes
@@ -391,12 +395,14 @@ def run_gpu(args, w):
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 trace/gather, f64 radius/average", "data": "synthetic (seeded scene, seeded photon streams)",
         "config": {"workload": args.workload, **w, "precision": "mixed", "cuda_graph": True, "bvh_leaf": leaf,
+                   "cells_per_radius": cells,
                    "l2": "flushed between timed passes (2x L2 write)", "parallelism": f"passes x{world}"},
         "plain_fp64": {"value": value_plain, "unit": "Mphotons/s", "ms_per_step": ms_plain / steps_plain,
                        "mixed_over_plain": value / value_plain},
         "rmse": out_rmse,
         "e2e": {"value": e2e_value, "unit": "Mphotons/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "step": f"ppm_scene_upload + ppm_camera_set + ppm_render({w['passes']} passes) + image download"},
+                "step": f"ppm_scene_upload + ppm_camera_set + ppm_render({w['passes']} passes, cell size {cells} "
+                        f"as tuned above) + image download"},
         "gpu_launches": kernels_per_pass * args.steps,
         "kernels_per_pass": kernels_per_pass,
         "stages_ms_per_pass": {k: round(v, 4) for k, v in stage_avg.items()},

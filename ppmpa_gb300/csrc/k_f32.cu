@@ -6,17 +6,12 @@
 
 namespace ppm {
 
-void launch_emit_f(const SceneView<float> &sc, const EmitPlan &plan, uint64_t seed, const PassState *st,
-                   RayQueue<float> q, int grid, cudaStream_t s) {
-    k_emit<float><<<grid, 256, 0, s>>>(sc, plan, seed, st, q);
-}
-void launch_bounce_f(const SceneView<float> &sc, uint64_t seed, PassState *st, int uc, int level, long long n_level0,
-                     RayQueue<float> in, RayQueue<float> out, unsigned long long qcap, PhotonBuf<float> photons,
-                     int grid, cudaStream_t s) {
+void launch_trace_f(const SceneView<float> &sc, const EmitPlan &plan, uint64_t seed, PassState *st, int uc,
+                    PhotonBuf<float> photons, int grid, cudaStream_t s) {
     if (sc.bvh)
-        k_bounce<float, true><<<grid, 256, 0, s>>>(with_bvh(sc), seed, st, uc, level, n_level0, in, out, qcap, photons);
+        k_trace<float, true><<<grid, 256, 0, s>>>(with_bvh(sc), plan, seed, st, uc, photons);
     else
-        k_bounce<float, false><<<grid, 256, 0, s>>>(sc, seed, st, uc, level, n_level0, in, out, qcap, photons);
+        k_trace<float, false><<<grid, 256, 0, s>>>(sc, plan, seed, st, uc, photons);
 }
 void launch_bbox_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s) {
     k_bbox<float><<<grid, 256, 0, s>>>(buf, st, n_fixed);

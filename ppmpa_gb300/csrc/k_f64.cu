@@ -6,17 +6,12 @@
 
 namespace ppm {
 
-void launch_emit_d(const SceneView<double> &sc, const EmitPlan &plan, uint64_t seed, const PassState *st,
-                   RayQueue<double> q, int grid, cudaStream_t s) {
-    k_emit<double><<<grid, 256, 0, s>>>(sc, plan, seed, st, q);
-}
-void launch_bounce_d(const SceneView<double> &sc, uint64_t seed, PassState *st, int uc, int level, long long n_level0,
-                     RayQueue<double> in, RayQueue<double> out, unsigned long long qcap, PhotonBuf<double> photons,
-                     int grid, cudaStream_t s) {
+void launch_trace_d(const SceneView<double> &sc, const EmitPlan &plan, uint64_t seed, PassState *st, int uc,
+                    PhotonBuf<double> photons, int grid, cudaStream_t s) {
     if (sc.bvh)
-        k_bounce<double, true><<<grid, 256, 0, s>>>(with_bvh(sc), seed, st, uc, level, n_level0, in, out, qcap, photons);
+        k_trace<double, true><<<grid, 256, 0, s>>>(with_bvh(sc), plan, seed, st, uc, photons);
     else
-        k_bounce<double, false><<<grid, 256, 0, s>>>(sc, seed, st, uc, level, n_level0, in, out, qcap, photons);
+        k_trace<double, false><<<grid, 256, 0, s>>>(sc, plan, seed, st, uc, photons);
 }
 void launch_bbox_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s) {
     k_bbox<double><<<grid, 256, 0, s>>>(buf, st, n_fixed);

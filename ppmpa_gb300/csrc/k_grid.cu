@@ -17,6 +17,7 @@ __global__ void k_pass_begin(PassState *st) {
     st->slots = 0;
     st->rows = 0;
     st->gather_next = 0;
+    st->emit_next = 0;
     for (int l = 0; l < MAX_TRACE + 2; l++) {
         st->qn[l] = 0;
         st->eq[l] = 0;

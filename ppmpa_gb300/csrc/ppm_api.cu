@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -71,8 +72,6 @@ struct ppm_ctx {
     PassState *st = nullptr;
     DevBuf raw_d, spos, sdir, raw_f, sorted_f, sidx, keyrank, count, start, block_sums;
     long long photon_cap_d = 0, photon_cap_f = 0;
-    DevBuf rq[4];                 // photon ray queues: level ping-pong A(a, b), B(a, b)
-    long long rq_cap = 0;         // entries per queue
     DevBuf eqb[6];                // eye queues: A(a, b, c), B(a, b, c)
     long long eq_cap = 0;
     DevBuf hits_d, hits_f;
@@ -365,12 +364,6 @@ static int grid_blocks(ppm_ctx *ctx, int per_sm) { return ctx->sm_count * per_sm
 
 constexpr int EYE_QUEUE_PER_PIXEL = 2;   // eye-tree vertices per pixel a level may hold
 
-static int ensure_ray_queues(ppm_ctx *ctx, long long n, size_t vec_bytes) {
-    for (DevBuf &b : ctx->rq) TRY(ensure(ctx, b, vec_bytes * (size_t)std::max(1LL, n)));
-    ctx->rq_cap = std::max(1LL, n);
-    return PPM_OK;
-}
-
 static int ensure_eye_queues(ppm_ctx *ctx, long long npx, size_t vec_bytes) {
     long long cap = std::max(1LL, npx * EYE_QUEUE_PER_PIXEL);
     for (DevBuf &b : ctx->eqb) TRY(ensure(ctx, b, vec_bytes * (size_t)cap));
@@ -379,19 +372,21 @@ static int ensure_eye_queues(ppm_ctx *ctx, long long npx, size_t vec_bytes) {
 }
 
 // emission + MAX_TRACE bounce levels over ping-pong ray queues; returns kernels launched
-template <typename T, typename Emit, typename Bounce>
+static void launch_trace(ppm_ctx *ctx, const EmitPlan &plan, uint64_t seed, int uc, PhotonBuf<double> pb, int g,
+                         cudaStream_t s) {
+    launch_trace_d(ctx->sv_d, plan, seed, ctx->st, uc, pb, g, s);
+}
+static void launch_trace(ppm_ctx *ctx, const EmitPlan &plan, uint64_t seed, int uc, PhotonBuf<float> pb, int g,
+                         cudaStream_t s) {
+    launch_trace_f(ctx->sv_f, plan, seed, ctx->st, uc, pb, g, s);
+}
+
+// one persistent launch with as many blocks as stay resident (TraceBlocks)
+template <typename T>
 static int enqueue_photon_trace(ppm_ctx *ctx, const EmitPlan &plan, uint64_t seed, int uc, PhotonBuf<T> pb,
-                                Emit emit, Bounce bounce, cudaStream_t s) {
-    using V = vec4_t<T>;
-    RayQueue<T> qa{as<V>(ctx->rq[0]), as<V>(ctx->rq[1])}, qb{as<V>(ctx->rq[2]), as<V>(ctx->rq[3])};
-    const long long n_emit = plan.first[plan.n_lights];
-    const long long blocks = (n_emit + 255) / 256;
-    const int g_emit = (int)std::max(1LL, std::min<long long>(blocks, (long long)ctx->sm_count * 8));
-    emit(ctx->sv_of(T()), plan, seed, ctx->st, qa, g_emit, s);
-    for (int l = 0; l < MAX_TRACE; l++)
-        bounce(ctx->sv_of(T()), seed, ctx->st, uc, l, n_emit, (l & 1) ? qb : qa, (l & 1) ? qa : qb,
-               (unsigned long long)ctx->rq_cap, pb, grid_blocks(ctx, 8), s);
-    return 1 + MAX_TRACE;
+                                cudaStream_t s) {
+    launch_trace(ctx, plan, seed, uc, pb, grid_blocks(ctx, TraceBlocks<T>::value), s);
+    return 1;
 }
 
 template <typename T, typename Level>
@@ -425,6 +420,14 @@ extern "C" const char *ppm_status_string(int s) {
     }
 }
 
+// The eye pass runs on a side stream beside the photon trace; it gets the
+// higher priority, so its blocks are scheduled first when both wait.
+static int eye_priority() {
+    int lo = 0, hi = 0;
+    if (cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess) return 0;
+    return hi;
+}
+
 extern "C" int ppm_ctx_create(ppm_ctx **out, int device, uint64_t seed) {
     if (!out) return PPM_ERR_INVALID_ARG;
     *out = nullptr;
@@ -443,7 +446,7 @@ extern "C" int ppm_ctx_create(ppm_ctx **out, int device, uint64_t seed) {
     }
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (cudaStreamCreateWithFlags(&ctx->s, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&ctx->s2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&ctx->s2, cudaStreamNonBlocking, eye_priority()) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaMalloc(&ctx->st, sizeof(PassState)) != cudaSuccess) {
@@ -474,7 +477,6 @@ extern "C" int ppm_ctx_destroy(ppm_ctx *ctx) {
                       &ctx->pass_img, &ctx->sum_img, &ctx->scratch, &ctx->pass_direct32, &ctx->pass_gather32,
                       &ctx->qstart, &ctx->bvh_nodes, &ctx->bvh_bounded, &ctx->bvh_unb, &ctx->bvh_order};
     for (DevBuf *b : bufs) release(*b);
-    for (DevBuf &b : ctx->rq) release(b);
     for (DevBuf &b : ctx->eqb) release(b);
     if (ctx->st) cudaFree(ctx->st);
     if (ctx->tev_made) {
@@ -762,11 +764,10 @@ extern "C" int ppm_trace_photons(ppm_ctx *ctx, int64_t nphoton, int32_t use_clas
     if (nem > 0x7fffffffLL) return set_err(ctx, PPM_ERR_INVALID_ARG, "too many photons");
     long long cap = std::max(1LL, nem * MAX_TRACE);
     TRY(ensure_photons_d(ctx, cap));
-    TRY(ensure_ray_queues(ctx, nem, sizeof(double4)));
     TRY(upload_state(ctx, 0.0, (int)pass, 0.0, 1, 1.0, cap, 0));
     launch_pass_begin(ctx->st, ctx->s);
     PhotonBuf<double> pb{as<PhotonD>(ctx->raw_d), as<double4>(ctx->spos), as<double4>(ctx->sdir)};
-    enqueue_photon_trace<double>(ctx, plan, ctx->seed, use_classic ? 1 : 0, pb, launch_emit_d, launch_bounce_d, ctx->s);
+    enqueue_photon_trace<double>(ctx, plan, ctx->seed, use_classic ? 1 : 0, pb, ctx->s);
     CK(cudaGetLastError());
     PassState h;
     TRY(read_state(ctx, h));
@@ -1396,7 +1397,7 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
     // photons
     if (mixed) {
         PhotonBuf<float> pb{as<float4>(ctx->raw_f), as<float4>(ctx->sorted_f), nullptr};
-        kernels += enqueue_photon_trace<float>(ctx, ctx->plan, ctx->cfg.seed, uc, pb, launch_emit_f, launch_bounce_f, s);
+        kernels += enqueue_photon_trace<float>(ctx, ctx->plan, ctx->cfg.seed, uc, pb, s);
         launch_bbox_f(pb, ctx->st, -1, g4, s);
         if (ev) CK(cudaEventRecord(ev[1], s));
         launch_grid_setup(ctx->st, -1.0, s);
@@ -1405,7 +1406,7 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
         launch_scatter_f(pb, ctx->st, -1, as<uint32_t>(ctx->start), as<uint2>(ctx->keyrank), g8, s);
     } else {
         PhotonBuf<double> pb{as<PhotonD>(ctx->raw_d), as<double4>(ctx->spos), as<double4>(ctx->sdir)};
-        kernels += enqueue_photon_trace<double>(ctx, ctx->plan, ctx->cfg.seed, uc, pb, launch_emit_d, launch_bounce_d, s);
+        kernels += enqueue_photon_trace<double>(ctx, ctx->plan, ctx->cfg.seed, uc, pb, s);
         launch_bbox_d(pb, ctx->st, -1, g4, s);
         if (ev) CK(cudaEventRecord(ev[1], s));
         launch_grid_setup(ctx->st, -1.0, s);
@@ -1453,8 +1454,10 @@ static double schedule_r2(const ppm_render_cfg &c, int upto) {
     return r;
 }
 
-// Grid cell autotuner of a render: one untimed and one timed eager pass with
-// 1 and with 2 cells per radius; the faster wins.  The trial passes write
+// Grid cell autotuner of a render: one untimed and two timed passes with 1
+// and with 2 cells per radius at the render's middle pass (the captured pass
+// graph, which reads the cell factor from the device state, or eager passes
+// without a graph); the faster wins.  The trial passes write
 // only buffers that the caller's render then resets (state, pass and sum
 // images), so the image does not depend on the trial.
 static int tune_cells(ppm_ctx *ctx, const ppm_render_cfg &cfg, long long cap, int &best) {
@@ -1463,20 +1466,31 @@ static int tune_cells(ppm_ctx *ctx, const ppm_render_cfg &cfg, long long cap, in
     if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return set_err(ctx, PPM_ERR_CUDA, "event"); }
     const bool timing = ctx->timing;
     ctx->timing = false;
+    // trials at the middle pass: its radius is typical of the render (the
+    // first pass has the largest radius, where finer cells pay off most)
+    const int trial = cfg.first_pass + cfg.passes / 2;
     float best_ms = 1e30f;
     int rc = PPM_OK;
     for (int k = 1; k <= 2 && rc == PPM_OK; k++) {
-        for (int rep = 0; rep < 2 && rc == PPM_OK; rep++) {
-            rc = upload_state(ctx, schedule_r2(cfg, cfg.first_pass), cfg.first_pass, cfg.alpha, cfg.schedule_offset,
-                              (double)k, cap, ctx->hit_cap);
+        float total = 0.0f;
+        for (int rep = 0; rep < 3 && rc == PPM_OK; rep++) {   // one warm-up, two timed passes
+            rc = upload_state(ctx, schedule_r2(cfg, trial), trial, cfg.alpha, cfg.schedule_offset, (double)k, cap,
+                              ctx->hit_cap);
             if (rc == PPM_OK && cudaEventRecord(e0, ctx->s) != cudaSuccess) rc = set_err(ctx, PPM_ERR_CUDA, "event");
-            if (rc == PPM_OK) rc = enqueue_pass(ctx, false);
+            if (rc == PPM_OK) {
+                if (ctx->graph_exec) {   // time the pass the render will replay
+                    if (cudaGraphLaunch(ctx->graph_exec, ctx->s) != cudaSuccess) rc = set_err(ctx, PPM_ERR_CUDA, "graph");
+                } else {
+                    rc = enqueue_pass(ctx, false);
+                }
+            }
             if (rc == PPM_OK && cudaEventRecord(e1, ctx->s) != cudaSuccess) rc = set_err(ctx, PPM_ERR_CUDA, "event");
             float ms = 0.0f;
             if (rc == PPM_OK && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
                 rc = set_err(ctx, PPM_ERR_CUDA, "cell tuner timing");
-            if (rc == PPM_OK && rep == 1 && ms < best_ms) { best_ms = ms; best = k; }
+            if (rep > 0) total += ms;
         }
+        if (rc == PPM_OK && total < best_ms) { best_ms = total; best = k; }
     }
     ctx->timing = timing;
     cudaEventDestroy(e0);
@@ -1508,12 +1522,10 @@ extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
     if (cfg->precision == PPM_PRECISION_MIXED) {
         if (photons) TRY(ensure_photons_f(ctx, cap, false));
         TRY(ensure(ctx, ctx->hits_f, sizeof(HitPoint<float>) * ctx->hit_cap));
-        if (photons) TRY(ensure_ray_queues(ctx, nem, sizeof(float4)));
         TRY(ensure_eye_queues(ctx, ctx->npx, sizeof(float4)));
     } else {
         if (photons) TRY(ensure_photons_d(ctx, cap));
         TRY(ensure(ctx, ctx->hits_d, sizeof(HitPoint<double>) * ctx->hit_cap));
-        if (photons) TRY(ensure_ray_queues(ctx, nem, sizeof(double4)));
         TRY(ensure_eye_queues(ctx, ctx->npx, sizeof(double4)));
     }
     TRY(ensure(ctx, ctx->pass_img, sizeof(double) * 3 * ctx->npx));
@@ -1525,7 +1537,6 @@ extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
     CK(cudaMemsetAsync(ctx->sum_img.p, 0, sizeof(double) * 3 * ctx->npx, ctx->s));
     CK(cudaMemsetAsync(ctx->pass_img.p, 0, sizeof(double) * 3 * ctx->npx, ctx->s));
     int cf = cfg->cell_factor ? cfg->cell_factor : 1;
-    if ((cfg->flags & PPM_RENDER_TUNE_CELLS) && !(cfg->flags & PPM_RENDER_CLASSIC)) TRY(tune_cells(ctx, *cfg, cap, cf));
     TRY(upload_state(ctx, schedule_r2(*cfg, cfg->first_pass), cfg->first_pass, cfg->alpha, cfg->schedule_offset, (double)cf,
                      cap, ctx->hit_cap));
     CK(cudaStreamSynchronize(ctx->s));
@@ -1543,6 +1554,13 @@ extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
         if (e != cudaSuccess) return set_err(ctx, PPM_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
         ctx->graph = g;
         CK(cudaGraphInstantiate(&ctx->graph_exec, g, 0));
+    }
+    if ((cfg->flags & PPM_RENDER_TUNE_CELLS) && !(cfg->flags & PPM_RENDER_CLASSIC)) {
+        TRY(tune_cells(ctx, *cfg, cap, cf));
+        TRY(upload_state(ctx, schedule_r2(*cfg, cfg->first_pass), cfg->first_pass, cfg->alpha, cfg->schedule_offset,
+                         (double)cf, cap, ctx->hit_cap));
+        CK(cudaStreamSynchronize(ctx->s));
+        ctx->cell_factor = cf;
     }
     ctx->render_ready = true;
     return PPM_OK;

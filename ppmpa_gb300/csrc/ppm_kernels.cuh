@@ -50,6 +50,7 @@ struct PassState {
     unsigned long long candidates, in_radius;   // gather counters (valid candidates, hits)
     unsigned long long slots, rows;             // lane slots issued, non-empty rows visited
     unsigned long long gather_next;             // next query chunk of the FP32 gather
+    unsigned long long emit_next;               // next emission index of the persistent photon trace
     double cell_factor;
     int64_t cell_cap;
     unsigned long long photon_cap;   // buffers hold at most this many photons
@@ -190,80 +191,70 @@ __device__ __forceinline__ uint32_t tag(float4 v) { return __float_as_uint(v.w);
 __device__ __forceinline__ uint32_t tag(double4 v) { return (uint32_t)__double_as_longlong(v.w); }
 
 // photon ray queue: a = (pos, emission index), b = (dir, wl | (medium+1) << 8)
-template <typename T>
-struct RayQueue {
-    vec4_t<T> *a;
-    vec4_t<T> *b;
-};
-
-// ---------------------------------------------------------------------------
-// photon emission (light.rs:67-91; per-light counts of ppmpa.rs:30-31)
-// ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(256) k_emit(SceneView<T> sc, EmitPlan plan, uint64_t seed, const PassState *st,
-                                              RayQueue<T> q) {
-    const uint32_t pass = (uint32_t)st->pass;
-    const int64_t n_emit = plan.first[plan.n_lights];
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_emit; i += (int64_t)gridDim.x * blockDim.x) {
-        int li = 0;
-        while (li < plan.n_lights - 1 && i >= plan.first[li + 1]) li++;
-        PhotonPath<T> ph;
-        Rng rg;
-        rg.init(seed, (uint32_t)i, pass, TAG_EMIT);
-        generate_photon(sc.lights[li], rg, ph);
-        q.a[i] = mk4(ph.pos, (uint32_t)i);
-        q.b[i] = mk4(ph.dir, (uint32_t)ph.wl);
-    }
-}
-
-// one bounce level of trace_photon (tracer.rs:31-125) for every live ray;
-// continuing rays are compacted into the next level's queue
-// resident blocks of 256 threads asked of the bounce kernel: 4 in FP32 (fits
-// in 64 registers without spills), 2 in FP64 (as many as its registers allow)
-template <typename T> struct BounceBlocks { static constexpr int value = 2; };
-template <> struct BounceBlocks<float> { static constexpr int value = 4; };
-
-template <typename T, bool B>
-__global__ void __launch_bounds__(256, BounceBlocks<T>::value) k_bounce(SceneView<T, B> sc, uint64_t seed, PassState *st, int uc, int level,
-                                                long long n_level0, RayQueue<T> in, RayQueue<T> out,
-                                                unsigned long long qcap, PhotonBuf<T> photons) {
-    const uint32_t pass = (uint32_t)st->pass;
-    unsigned long long n = level == 0 ? (unsigned long long)n_level0 : st->qn[level];
-    if (n > qcap) n = qcap;
-    const unsigned long long pcap = st->photon_cap;
-    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
-        const vec4_t<T> a = in.a[i], b = in.b[i];
-        PhotonPath<T> ph;
-        ph.pos = xyz(a);
-        ph.dir = xyz(b);
-        ph.item = tag(a);
-        const uint32_t meta = tag(b);
-        ph.wl = (int)(meta & 3u);
-        ph.medium = (int)(meta >> 8) - 1;
-        ph.level = level;
-        const PhotonPath<T> cur = ph;
-        bool store;
-        V3<T> spos;
-        const bool alive = photon_event(sc, seed, pass, uc != 0, ph, store, spos);
-        if (store) {
-            unsigned long long slot = agg_append(&st->n_stored);
-            if (slot < pcap) photons.write(slot, cur, spos);
-            else atomicOr(&st->overflow, 1u);
-        }
-        if (alive) {
-            unsigned long long o = agg_append(&st->qn[level + 1]);
-            if (o < qcap) {
-                out.a[o] = mk4(ph.pos, ph.item);
-                out.b[o] = mk4(ph.dir, (uint32_t)ph.wl | ((uint32_t)(ph.medium + 1) << 8));
-            } else {
-                atomicOr(&st->overflow, 1u);
-            }
-        }
-    }
-}
 
 // bounds of n photons (block reduction, then one atomic per block and axis)
+// resident blocks of 256 threads asked of the persistent photon trace: 4 in
+// FP32 (fits in 64 registers without spills), 2 in FP64
+template <typename T> struct TraceBlocks { static constexpr int value = 2; };
+template <> struct TraceBlocks<float> { static constexpr int value = 4; };
+
+// Persistent photon tracing: one launch per pass (measured faster than an
+// emission kernel plus MAX_TRACE bounce kernels with ray queues between them,
+// on the glass box and on the 1.3M-triangle mesh).  Each lane
+// carries one photon through one event per iteration; a lane whose photon
+// ended takes the next emission index (one atomic per warp for all its idle
+// lanes), so lanes stay busy until the emission list runs out, and no ray
+// goes through memory between bounces.  Random streams are keyed by
+// (emission index, pass, level) as in the wavefront form, so the stored
+// photons are the same set (their order in the buffer differs).
+template <typename T, bool B>
+__global__ void __launch_bounds__(256, TraceBlocks<T>::value) k_trace(SceneView<T, B> sc, EmitPlan plan, uint64_t seed,
+                                                                       PassState *st, int uc, PhotonBuf<T> photons) {
+    const uint32_t pass = (uint32_t)st->pass;
+    const unsigned long long n_emit = (unsigned long long)plan.first[plan.n_lights];
+    const unsigned long long pcap = st->photon_cap;
+    const unsigned lane = lane_id();
+    PhotonPath<T> ph;
+    ph.level = 0;
+    bool active = false, exhausted = false;
+    for (;;) {
+        const unsigned need = __ballot_sync(0xffffffffu, !active) & (exhausted ? 0u : 0xffffffffu);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0;
+            if ((int)lane == leader) base = atomicAdd(&st->emit_next, (unsigned long long)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (base + __popc(need) >= n_emit) exhausted = true;
+            if (!active) {
+                const unsigned long long i = base + __popc(need & ((1u << lane) - 1u));
+                if (i < n_emit) {
+                    int li = 0;
+                    while (li < plan.n_lights - 1 && (int64_t)i >= plan.first[li + 1]) li++;
+                    Rng rg;
+                    rg.init(seed, (uint32_t)i, pass, TAG_EMIT);
+                    generate_photon(sc.lights[li], rg, ph);
+                    ph.item = (uint32_t)i;
+                    active = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (active) {
+            const PhotonPath<T> cur = ph;
+            bool store;
+            V3<T> spos;
+            const bool alive = photon_event(sc, seed, pass, uc != 0, ph, store, spos);
+            if (store) {
+                unsigned long long slot = agg_append(&st->n_stored);
+                if (slot < pcap) photons.write(slot, cur, spos);
+                else atomicOr(&st->overflow, 1u);
+            }
+            ph.level = cur.level + 1;
+            active = alive && ph.level < MAX_TRACE;
+        }
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_bbox(PhotonBuf<T> buf, PassState *st, long long n_fixed) {
     unsigned long long n = n_photons(st, n_fixed);

@@ -8,11 +8,9 @@
 namespace ppm {
 
 // ---- FP64 path -------------------------------------------------------------
-void launch_emit_d(const SceneView<double> &sc, const EmitPlan &plan, uint64_t seed, const PassState *st,
-                   RayQueue<double> q, int grid, cudaStream_t s);
-void launch_bounce_d(const SceneView<double> &sc, uint64_t seed, PassState *st, int uc, int level, long long n_level0,
-                     RayQueue<double> in, RayQueue<double> out, unsigned long long qcap, PhotonBuf<double> photons,
-                     int grid, cudaStream_t s);
+// persistent photon tracing: every emitted photon through all its bounces
+void launch_trace_d(const SceneView<double> &sc, const EmitPlan &plan, uint64_t seed, PassState *st, int uc,
+                    PhotonBuf<double> photons, int grid, cudaStream_t s);
 void launch_bbox_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s);
 void launch_hist_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, uint32_t *count, uint2 *keyrank, int grid,
                    cudaStream_t s);
@@ -33,11 +31,9 @@ void launch_intersect_d(const SceneView<double> &sc, const double *rays, long lo
                         double *nrm, cudaStream_t s);
 
 // ---- FP32 mixed path ---------------------------------------------------------
-void launch_emit_f(const SceneView<float> &sc, const EmitPlan &plan, uint64_t seed, const PassState *st,
-                   RayQueue<float> q, int grid, cudaStream_t s);
-void launch_bounce_f(const SceneView<float> &sc, uint64_t seed, PassState *st, int uc, int level, long long n_level0,
-                     RayQueue<float> in, RayQueue<float> out, unsigned long long qcap, PhotonBuf<float> photons,
-                     int grid, cudaStream_t s);
+// persistent photon tracing: every emitted photon through all its bounces
+void launch_trace_f(const SceneView<float> &sc, const EmitPlan &plan, uint64_t seed, PassState *st, int uc,
+                    PhotonBuf<float> photons, int grid, cudaStream_t s);
 void launch_bbox_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s);
 void launch_hist_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, uint32_t *count, uint2 *keyrank, int grid,
                    cudaStream_t s);
