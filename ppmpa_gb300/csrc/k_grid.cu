@@ -28,9 +28,10 @@ __global__ void k_pass_begin(PassState *st) {
     }
 }
 
-// Grid over the photon bounds with cells of r/k * (1 + 1/128) (k = cells per
-// radius).  The margin keeps |p - q| <= r  =>  |cell(p) - cell(q)| <= ext per
-// axis under FP32 rounding of the cell coordinate (<= 3 ulp of <= 8192 cells).
+// Grid over the photon bounds with cells of c = r/k * (1 + 1/128) in y and z
+// (k = cells per radius) and c / sx in x.  The margin keeps |p - q| <= r  =>
+// |cell(p) - cell(q)| <= ext (extx in x) under FP32 rounding of the cell
+// coordinate (<= 3 ulp of <= 8192 cells per axis).
 __global__ void k_grid_setup(PassState *st, double r2_override) {
     if (threadIdx.x != 0) return;
     double r2 = r2_override > 0.0 ? r2_override : st->r2;
@@ -46,6 +47,7 @@ __global__ void k_grid_setup(PassState *st, double r2_override) {
         if (!(hi[a] - lo[a] >= 0.0 && hi[a] - lo[a] < 1e30)) empty = true;
     if (empty) for (int a = 0; a < 3; a++) { lo[a] = 0.0; hi[a] = 0.0; }
     double k = st->cell_factor > 0.0 ? st->cell_factor : 1.0;
+    const int sx = st->cell_sx >= 1 ? st->cell_sx : 1;
     double c = r / k * (1.0 + 1.0 / 128.0);
     if (!(c > 0.0 && c < 1e30)) c = 1.0;
     long long dim[3] = {1, 1, 1};
@@ -53,7 +55,8 @@ __global__ void k_grid_setup(PassState *st, double r2_override) {
         bool ok = true;
         long long tot = 1;
         for (int a = 0; a < 3; a++) {
-            double f = floor((hi[a] - lo[a]) / c);
+            const double ca = a == 0 ? c / sx : c;
+            double f = floor((hi[a] - lo[a]) / ca);
             if (!(f >= 0.0 && f < 8192.0)) { ok = false; dim[a] = 8193; }
             else dim[a] = (long long)f + 1;
             tot *= dim[a];
@@ -68,12 +71,17 @@ __global__ void k_grid_setup(PassState *st, double r2_override) {
         g.orgf[a] = (float)lo[a];
         g.dim[a] = (int32_t)dim[a];
     }
+    const double cx = c / sx;
     g.cell = c;
     g.inv = 1.0 / c;
     g.invf = (float)(1.0 / c);
+    g.invx = 1.0 / cx;
+    g.invxf = (float)(1.0 / cx);
     double ef = ceil(r / c + 3e-3);
     int ext = ef >= 1.0 && ef <= 8.0 ? (int)ef : (ef > 8.0 ? 8 : 1);
     g.ext = ext < 1 ? 1 : (ext > 8 ? 8 : ext);
+    double efx = ceil(r / cx + 3e-3);
+    g.extx = efx >= 1.0 && efx <= 64.0 ? (int)efx : (efx > 64.0 ? 64 : 1);
     g.ncell = dim[0] * dim[1] * dim[2];
     g.nkeys = 3 * g.ncell;
     g.r2f = (float)r2;

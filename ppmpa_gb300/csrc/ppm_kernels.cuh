@@ -23,13 +23,18 @@ namespace ppm {
 // Photons are counting-sorted by key = 3 * cell + wavelength: the photons of
 // a cell row are contiguous, and inside each cell they are grouped by
 // wavelength (so a warp's flux updates mostly go to one channel).
+// Cells are c wide in y and z and c / sx wide in x: a cell row (fixed y, z)
+// is contiguous in the sorted map, and the finer x cells let a query's x
+// range follow its sphere's chord closely while the number of rows stays
+// (2 ext + 1)^2.
 struct GridParams {
     double org[3];
-    double cell, inv;
+    double cell, inv;         // y/z cell size c and 1/c
+    double invx;              // 1 / (c / sx)
     float orgf[3];
-    float invf;
+    float invf, invxf;
     int32_t dim[3];
-    int32_t ext;
+    int32_t ext, extx;        // cells a radius can span: y/z, x
     int64_t ncell;
     int64_t nkeys;            // 3 * ncell
     float r2f, r2_lo, r2_hi;  // pass radius^2 in FP32 and its rounding band
@@ -52,6 +57,8 @@ struct PassState {
     unsigned long long gather_next;             // next query chunk of the FP32 gather
     unsigned long long emit_next;               // next emission index of the persistent photon trace
     double cell_factor;
+    int32_t cell_sx;           // x cells per y/z cell (>= 1)
+    int32_t pad2;
     int64_t cell_cap;
     unsigned long long photon_cap;   // buffers hold at most this many photons
     unsigned long long hit_cap;      // and this many hit points
@@ -301,14 +308,14 @@ __global__ void __launch_bounds__(256) k_bbox(PhotonBuf<T> buf, PassState *st, l
 template <typename T> struct CellMath;
 template <> struct CellMath<double> {
     __device__ static __forceinline__ int coord(const GridParams &g, double p, int a) {
-        double f = floor((p - g.org[a]) * g.inv);
+        double f = floor((p - g.org[a]) * (a == 0 ? g.invx : g.inv));
         f = fmin(fmax(f, 0.0), (double)(g.dim[a] - 1));
         return (int)f;
     }
 };
 template <> struct CellMath<float> {
     __device__ static __forceinline__ int coord(const GridParams &g, float p, int a) {
-        float f = floorf((p - g.orgf[a]) * g.invf);
+        float f = floorf((p - g.orgf[a]) * (a == 0 ? g.invxf : g.invf));
         f = fminf(fmaxf(f, 0.0f), (float)(g.dim[a] - 1));
         return (int)f;
     }
@@ -574,14 +581,16 @@ __global__ void __maxnreg__(128) k_eye_level_bvh(SceneView<T, true> sc, DCamera<
 // search.
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ __forceinline__ void query_cells(const GridParams &g, V3<T> q, int ext, int c[3], int lo[3], int hi[3]) {
+__device__ __forceinline__ void query_cells(const GridParams &g, V3<T> q, int ext, int extx, int c[3], int lo[3],
+                                            int hi[3]) {
     c[0] = CellMath<T>::coord(g, q.x, 0);
     c[1] = CellMath<T>::coord(g, q.y, 1);
     c[2] = CellMath<T>::coord(g, q.z, 2);
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        lo[a] = max(c[a] - ext, 0);
-        hi[a] = min(c[a] + ext, g.dim[a] - 1);
+        const int e = a == 0 ? extx : ext;
+        lo[a] = max(c[a] - e, 0);
+        hi[a] = min(c[a] + e, g.dim[a] - 1);
     }
 }
 
@@ -607,8 +616,8 @@ template <> struct RowCull<float> {
         const float rem = r2 * 1.00002f - dy * dy - dz * dz;
         if (rem < 0.0f) return false;
         const float rx = sqrtf(rem) * 1.00001f;
-        const float fx0 = floorf((q.x - rx - g.orgf[0]) * g.invf - 4e-3f);
-        const float fx1 = floorf((q.x + rx - g.orgf[0]) * g.invf + 4e-3f);
+        const float fx0 = floorf((q.x - rx - g.orgf[0]) * g.invxf - 4e-3f);
+        const float fx1 = floorf((q.x + rx - g.orgf[0]) * g.invxf + 4e-3f);
         x0 = max(lo_x, (int)fmaxf(fx0, -1.0f));
         x1 = min(hi_x, (int)fminf(fx1, (float)g.dim[0]));
         return x0 <= x1;
@@ -624,8 +633,8 @@ template <> struct RowCull<double> {
         const double rem = r2 * (1.0 + 1e-12) - dy * dy - dz * dz;
         if (rem < 0.0) return false;
         const double rx = sqrt(rem) * (1.0 + 1e-12);
-        const double fx0 = floor((q.x - rx - g.org[0]) * g.inv - 1e-6);
-        const double fx1 = floor((q.x + rx - g.org[0]) * g.inv + 1e-6);
+        const double fx0 = floor((q.x - rx - g.org[0]) * g.invx - 1e-6);
+        const double fx1 = floor((q.x + rx - g.org[0]) * g.invx + 1e-6);
         x0 = max(lo_x, (int)fmax(fx0, -1.0));
         x1 = min(hi_x, (int)fmin(fx1, (double)g.dim[0]));
         return x0 <= x1;
@@ -726,7 +735,7 @@ __global__ void __launch_bounds__(256) k_gather_d(const HitPoint<double> *hits, 
         const HitPoint<double> h = hits[qi];
         V3<double> q = ld3(h.pos), n = ld3(h.nrm);
         int c[3], lo[3], hi[3];
-        query_cells(g, q, g.ext, c, lo, hi);
+        query_cells(g, q, g.ext, g.extx, c, lo, hi);
         double s0 = 0.0, s1 = 0.0, s2 = 0.0;
         for_each_candidate(g, start, q, r2, lo, hi, [&](uint32_t idx, bool valid) {
             if (!valid) return;
@@ -869,13 +878,14 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
         const HitPoint<float> h = hits[qi];
         double r2;
         float r2_lo, r2_hi, r2f;
-        int ext = g.ext;
+        int ext = g.ext, extx = g.extx;
         if constexpr (PERQ) {
             r2 = q_r2[qi];
             r2_lo = __double2float_rd(r2 * (1.0 - 1e-6));
             r2_hi = __double2float_ru(r2 * (1.0 + 1e-6));
             r2f = (float)r2;
             ext = min(g.ext, max(1, (int)ceil(sqrt(r2) * g.inv + 3e-3)));
+            extx = min(g.extx, max(1, (int)ceil(sqrt(r2) * g.invx + 3e-3)));
         } else {
             r2 = st->r2;
             r2_lo = g.r2_lo;
@@ -884,7 +894,7 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
         }
         V3<float> q = ld3(h.pos), n = ld3(h.nrm);
         int c[3], lo[3], hi[3];
-        query_cells(g, q, ext, c, lo, hi);
+        query_cells(g, q, ext, extx, c, lo, hi);
         Kahan k0 = {0.f, 0.f}, k1 = {0.f, 0.f}, k2 = {0.f, 0.f};
         unsigned long long c_slots = 0, c_valid = 0, c_hits = 0;
         for_each_candidate(g, start, q, r2f, lo, hi, [&](uint32_t idx, bool valid) {
@@ -991,8 +1001,9 @@ __global__ void __launch_bounds__(256) k_within(const T *q, long long nq, const 
         const float r2_lo = __double2float_rd(r2 * (1.0 - 1e-6));
         const float r2_hi = __double2float_ru(r2 * (1.0 + 1e-6));
         int ext = min(g.ext, max(1, (int)ceil(sqrt(r2) * g.inv + 3e-3)));
+        int extx = min(g.extx, max(1, (int)ceil(sqrt(r2) * g.invx + 3e-3)));
         int c[3], lo[3], hi[3];
-        query_cells(g, qq, ext, c, lo, hi);
+        query_cells(g, qq, ext, extx, c, lo, hi);
         unsigned long long found = 0;
         unsigned long long wbase = offsets ? offsets[qi] : 0;
         for_each_candidate(g, start, qq, (T)r2, lo, hi, [&](uint32_t idx, bool valid) {

@@ -113,3 +113,21 @@ def test_leaf_tuner_keeps_answers(ctx):
     got = ctx.intersect(rays)
     assert all(np.array_equal(a, b) for a, b in zip(got, want))
     ctx.set_bvh_leaf(1)
+
+
+@pytest.mark.parametrize("n_prims,leaf", [(3000, 1), (3000, 4), (200, 2)])
+def test_bvh_on_spheres_and_quads_matches_oracle(ctx, n_prims, leaf):
+    """Batch-workload scenes: spheres and parallelograms in random positions
+    and orientations (sphere roots, parallelogram bounds, ties between
+    overlapping objects) through the hierarchy, against the oracle's loop."""
+    from ppmpa_gb300 import workloads as W
+    sc = W.batch_scene(np.random.default_rng(n_prims + leaf), n_prims)
+    ctx.set_bvh_leaf(leaf)
+    ctx.upload_scene(sc)
+    ctx.set_accel(BVH)
+    rays = _rays(np.random.default_rng(77), 20000)
+    t, obj, nrm = ctx.intersect(rays)
+    ot, oobj, onrm, _ = Oracle(sc).intersect(rays)
+    assert np.array_equal(obj, oobj) and np.array_equal(t, ot) and np.array_equal(nrm, onrm)
+    assert (obj >= 5).mean() > 0.05
+    ctx.set_bvh_leaf(1)
