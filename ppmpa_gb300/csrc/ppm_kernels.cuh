@@ -689,6 +689,35 @@ __device__ __forceinline__ void for_each_candidate(const GridParams &g, const ui
     }
 }
 
+// The same walk for the FP32 gather, two candidates per lane per step: both
+// photons are loaded before either is used (two loads in flight per lane,
+// half the loop overhead).  use(photon, valid) must not contain warp-collective
+// operations (the second call is skipped when no lane has a second photon).
+template <typename T, typename U>
+__device__ __forceinline__ void for_each_candidate_pair(const GridParams &g, const uint32_t *start, V3<T> q, T r2,
+                                                        const int lo[3], const int hi[3], const float4 *smap,
+                                                        U &&use) {
+    const int nrows = (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+    for (int row0 = 0; row0 < nrows; row0 += 32) {
+        RowSet rs = make_rows(g, start, q, r2, lo, hi, row0);
+        unsigned m = rs.nonempty;
+        while (m) {
+            int r = __ffs(m) - 1;
+            m &= m - 1;
+            const uint32_t b = __shfl_sync(0xffffffffu, rs.begin, r);
+            const uint32_t n = __shfl_sync(0xffffffffu, rs.len, r);
+            for (uint32_t base = 0; base < n; base += 64) {
+                const uint32_t o0 = base + lane_id(), o1 = o0 + 32;
+                const bool v0 = o0 < n, v1 = o1 < n;
+                const float4 p0 = __ldg(&smap[v0 ? b + o0 : b]);
+                const float4 p1 = __ldg(&smap[v1 ? b + o1 : b]);
+                use(p0, v0);
+                if (base + 32 < n) use(p1, v1);
+            }
+        }
+    }
+}
+
 __device__ __forceinline__ double filter_wt(int pfilter, double d, double r2) {
     if (pfilter == PF_CONE) {   // tracer.rs:201-204
         double d2 = sqrt(d / r2) / 1.1;
@@ -897,13 +926,12 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
         query_cells(g, q, ext, extx, c, lo, hi);
         Kahan k0 = {0.f, 0.f}, k1 = {0.f, 0.f}, k2 = {0.f, 0.f};
         unsigned long long c_slots = 0, c_valid = 0, c_hits = 0;
-        for_each_candidate(g, start, q, r2f, lo, hi, [&](uint32_t idx, bool valid) {
+        for_each_candidate_pair(g, start, q, r2f, lo, hi, smap, [&](float4 pp, bool valid) {
             if (COUNT) {
                 c_slots += 1;
                 c_valid += valid;
             }
             if (!valid) return;
-            float4 pp = smap[idx];
             float d2f;
             if (in_radius_f32(q.x, q.y, q.z, pp, r2_lo, r2_hi, r2, d2f)) {
                 uint32_t m = __float_as_uint(pp.w);

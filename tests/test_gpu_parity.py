@@ -329,3 +329,20 @@ def test_cli_renders_one_pass_in_reference_format(built_lib):
     assert len(px) == 65536 and all(len(p) == 3 for p in px)
     vals = np.array([[float(v) for v in p] for p in px])
     assert np.isfinite(vals).all() and vals.max() > 0
+
+
+def test_c1_full_configuration_render_matches_oracle(ctx):
+    """The diffuse-sphere box at its full configuration (256x256, 200k
+    photons per pass, r0 0.05, alpha 0.7, 10 passes), plain FP64 with the
+    pass graph: the averaged image equals the oracle's progressive render
+    (photon traces, radius schedule, eye passes, average) within 1e-9."""
+    sc, cam = S.box_scene("c1"), S.box_camera(256)
+    ctx.upload_scene(sc)
+    ctx.set_camera(cam)
+    cfg = RenderConfig(nphoton=200_000, passes=10, radius0=0.05, alpha=0.7, precision=PLAIN, seed=1234)
+    got = ctx.render(cfg)
+    want = Oracle(sc, cam).render(200_000, 10, 0.05, 0.7, schedule_offset=1, use_classic=True, seed=1234)
+    assert want.max() > 0
+    assert np.allclose(got, want, rtol=1e-9, atol=1e-12 * want.max())
+    mixed = ctx.render(RenderConfig(nphoton=200_000, passes=10, radius0=0.05, alpha=0.7, precision=MIXED, seed=1234))
+    assert abs(mixed.mean() / want.mean() - 1) < 0.02
