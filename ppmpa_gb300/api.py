@@ -243,6 +243,8 @@ class Context:
 
     # -- progressive render ------------------------------------------------------------
     def _image_shape(self):
+        if self.camera is None:
+            raise PPMError(6, "no camera set (set_camera before rendering)")
         return (self.camera.yreso, self.camera.xreso, 3)
 
     def render(self, cfg: RenderConfig) -> np.ndarray:

@@ -376,7 +376,7 @@ static int ensure_eye_queues(ppm_ctx *ctx, long long npx, size_t vec_bytes) {
     return PPM_OK;
 }
 
-// emission + MAX_TRACE bounce levels over ping-pong ray queues; returns kernels launched
+// the persistent photon trace of one pass, in the precision of the photon buffer
 static void launch_trace(ppm_ctx *ctx, const EmitPlan &plan, uint64_t seed, int uc, PhotonBuf<double> pb, int g,
                          cudaStream_t s) {
     launch_trace_d(ctx->sv_d, plan, seed, ctx->st, uc, pb, g, s);

@@ -346,3 +346,46 @@ def test_c1_full_configuration_render_matches_oracle(ctx):
     assert np.allclose(got, want, rtol=1e-9, atol=1e-12 * want.max())
     mixed = ctx.render(RenderConfig(nphoton=200_000, passes=10, radius0=0.05, alpha=0.7, precision=MIXED, seed=1234))
     assert abs(mixed.mean() / want.mean() - 1) < 0.02
+
+
+def test_not_ready_and_capacity_errors():
+    """Render calls out of order report NOT_READY; a caller index buffer too
+    small reports CAPACITY; an eye tree wider than its per-level queues
+    is reported as CAPACITY instead of a silently truncated image: both
+    children of every front hit on the inner ball reach glass again, four
+    vertices per pixel at the second level against room for two."""
+    import ctypes as C
+    from ppmpa_gb300 import _lib
+    with Context(0, seed=3) as fresh:
+        with pytest.raises(PPMError) as e:
+            fresh.render(RenderConfig(nphoton=1000, passes=1))
+        assert e.value.status == 6
+        with pytest.raises(PPMError) as e:
+            fresh.render_step(1)
+        assert e.value.status == 6
+        rng = np.random.default_rng(8)
+        pos, d, wl = _photon_cloud(rng, 2000)
+        fresh.build_photonmap(pos, d, wl, 1.0, 0.2 ** 2)
+        q = np.array([[0.5, 0.5, 0.5]])
+        r2 = np.array([0.2 ** 2])
+        off = np.zeros(2, np.int64)
+        idx = np.zeros(1, np.int32)
+        tot = C.c_int64()
+        lib = _lib.load()
+        st = lib.ppm_query_within(fresh.h, q.ctypes.data_as(C.POINTER(C.c_double)), 1,
+                                  r2.ctypes.data_as(C.POINTER(C.c_double)), off.ctypes.data_as(C.POINTER(C.c_int64)),
+                                  idx.ctypes.data_as(C.POINTER(C.c_int32)), 1, C.byref(tot))
+        assert st == 3 and tot.value > 1
+
+        sc = S.Scene()
+        white = sc.add_material(S.new_simple((0.75, 0.75, 0.75), (0.0, 0.0, 0.0), 1.0, 0.0, 0.0))
+        glass = sc.add_material(S.new_ts((1.0, 1.0, 1.0), (0.05, 0.05, 0.05), 0.0, 0.0, 0.0, ior=(1.5, 1.5, 1.5)))
+        sc.add(S.sphere((0.0, 1.0, 1.0), 5.0), glass)          # the camera sits inside this glass shell
+        sc.add(S.sphere((0.0, 1.0, 1.0), 2.0), glass)          # and looks at a second glass ball filling the view
+        sc.add(S.parallelogram((-9.0, -9.0, 9.0), (9.0, -9.0, 9.0), (-9.0, 9.0, 9.0)), white)
+        sc.lights.append(S.point_light(S.color_normalize((1, 1, 1)), 100.0, (0.0, 1.0, 3.0)))
+        fresh.upload_scene(sc)
+        fresh.set_camera(S.box_camera(32))
+        with pytest.raises(PPMError) as e:
+            fresh.render(RenderConfig(nphoton=2000, passes=1, radius0=0.1, precision=PLAIN, seed=3))
+        assert e.value.status == 3 and "overflow" in str(e.value)
