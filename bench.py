@@ -334,6 +334,41 @@ def run_gpu(args, w):
     if os.path.exists(prof_sum):
         traffic = json.load(open(prof_sum)).get(dominant)
 
+    # throughput of each stage: rays, photon tests and compulsory bytes per second
+    stage_roof = {}
+    for k, t in stage_avg.items():
+        b = algorithmic_bytes(k, st_t, npx)
+        if t > 0 and b > 0:
+            gbs = b / (t / 1e3) / 1e9
+            stage_roof[k] = {"ms": round(t, 4), "algorithmic_bytes": b, "achieved_gbs": round(gbs, 1),
+                             "frac": round(gbs / peak, 4)}
+    mid = w["passes"] // 2                         # one pass from the middle of the render, timed, then counted
+    one = cfg(MIXED, 1, first=mid, graph=False, seed=seed_rank + 4)
+    one.cell_factor, one.flags = cells, 0
+    ctx.render_begin(one)
+    before = ctx.stats()["stage_ms"]["gather"]
+    ctx.set_stage_timing(1)
+    ctx.render_step(1)
+    ctx.sync()
+    g_ms = ctx.stats()["stage_ms"]["gather"] - before
+    ctx.render_begin(one)
+    ctx.set_stage_timing(2)
+    ctx.render_step(1)
+    ctx.sync()
+    cnt = ctx.stats()
+    ctx.set_stage_timing(False)
+    rates = {
+        "photon_rays_per_s": st_t["photon_rays"] / (stage_avg["photon_trace"] / 1e3),
+        "eye_rays_per_s": st_t["eye_rays"] / (stage_avg["eye_trace"] / 1e3),
+        "photon_rays_per_pass": st_t["photon_rays"], "eye_rays_per_pass": st_t["eye_rays"],
+        "photon_tests_per_s": cnt["candidates"] / (g_ms / 1e3), "in_radius_per_s": cnt["in_radius"] / (g_ms / 1e3),
+        "candidates": cnt["candidates"], "in_radius": cnt["in_radius"], "gather_ms": round(g_ms, 4),
+        "pass": mid + 1,
+        "note": ("ray rates: last pass of the stage-timed run over its stage's mean time (eye rays: primary "
+                 "and reflected/refracted children, shadow rays not counted); photon tests: one pass from the "
+                 "middle of the render, timed, then replayed with the gather counters on"),
+    }
+
     # plain FP64 path on the same workload
     steps_plain = max(3, min(args.steps, 10))
     ms_plain = timed_passes(PLAIN, steps_plain, 3, seed_rank + 2)
@@ -409,6 +444,8 @@ def run_gpu(args, w):
         "roofline": {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                      "algorithmic_bytes": ab},
+        "stage_rooflines": stage_roof,
+        "rates": rates,
         "pass_stats": {"photons_stored": st["photons_stored"], "hit_points": st["hit_points"],
                        "grid_cells": st["grid_cells"]},
         "cpu_baseline": cpu,

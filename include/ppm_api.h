@@ -153,6 +153,9 @@ typedef struct ppm_stats {
     int64_t in_radius;         /* photons found in radius (last pass, stage timing level 2) */
     int64_t gather_slots;      /* lane slots the gather issued (last pass, stage timing level 2) */
     int32_t cell_factor;       /* grid cells per radius the render uses (tuned or given) */
+    int64_t photon_rays;       /* photon ray segments traced (emission + bounces), last pass */
+    int64_t eye_rays;          /* eye-tree rays traced (primary + reflected/refracted children;
+                                  shadow rays not counted), last pass */
 } ppm_stats;
 
 typedef struct ppm_ctx ppm_ctx;

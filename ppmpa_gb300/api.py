@@ -281,7 +281,7 @@ class Context:
         return dict(photons_emitted=s.photons_emitted, photons_stored=s.photons_stored, hit_points=s.hit_points,
                     grid_cells=s.grid_cells, passes_done=s.passes_done, kernels_per_pass=s.kernels_per_pass,
                     r2=s.r2, candidates=s.candidates, in_radius=s.in_radius, gather_slots=s.gather_slots,
-                    cell_factor=s.cell_factor,
+                    cell_factor=s.cell_factor, photon_rays=s.photon_rays, eye_rays=s.eye_rays,
                     stage_ms={n: s.stage_ms[i] for i, n in enumerate(names)},
                     stage_calls={n: s.stage_calls[i] for i, n in enumerate(names)})
 

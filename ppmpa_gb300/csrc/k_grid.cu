@@ -18,10 +18,8 @@ __global__ void k_pass_begin(PassState *st) {
     st->rows = 0;
     st->gather_next = 0;
     st->emit_next = 0;
-    for (int l = 0; l < MAX_TRACE + 2; l++) {
-        st->qn[l] = 0;
-        st->eq[l] = 0;
-    }
+    st->photon_rays = 0;
+    for (int l = 0; l < MAX_TRACE + 2; l++) st->eq[l] = 0;
     for (int a = 0; a < 3; a++) {
         st->bb_lo[a] = ord_enc(1e300);
         st->bb_hi[a] = ord_enc(-1e300);

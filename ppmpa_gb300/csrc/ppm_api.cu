@@ -1640,6 +1640,12 @@ extern "C" int ppm_render_stats(ppm_ctx *ctx, ppm_stats *out) {
     out->in_radius = (int64_t)h.in_radius;
     out->gather_slots = (int64_t)h.slots;
     out->cell_factor = ctx->cell_factor;
+    out->photon_rays = (int64_t)h.photon_rays;
+    if (ctx->render_ready) {
+        int64_t eye = (int64_t)ctx->cam.xreso * ctx->cam.yreso;
+        for (int l = 1; l < MAX_TRACE + 2; l++) eye += (int64_t)h.eq[l];
+        out->eye_rays = eye;
+    }
     return PPM_OK;
 }
 

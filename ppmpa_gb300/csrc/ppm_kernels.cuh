@@ -62,7 +62,7 @@ struct PassState {
     int64_t cell_cap;
     unsigned long long photon_cap;   // buffers hold at most this many photons
     unsigned long long hit_cap;      // and this many hit points
-    unsigned long long qn[MAX_TRACE + 2];   // photon rays alive at each bounce level
+    unsigned long long photon_rays;         // photon ray segments traced this pass (one per event)
     unsigned long long eq[MAX_TRACE + 2];   // eye-tree vertices at each depth
 };
 
@@ -224,6 +224,7 @@ __global__ void __launch_bounds__(256, TraceBlocks<T>::value) k_trace(SceneView<
     PhotonPath<T> ph;
     ph.level = 0;
     bool active = false, exhausted = false;
+    unsigned rays = 0;
     for (;;) {
         const unsigned need = __ballot_sync(0xffffffffu, !active) & (exhausted ? 0u : 0xffffffffu);
         if (need) {
@@ -247,6 +248,7 @@ __global__ void __launch_bounds__(256, TraceBlocks<T>::value) k_trace(SceneView<
         }
         if (!__any_sync(0xffffffffu, active)) break;
         if (active) {
+            rays++;
             const PhotonPath<T> cur = ph;
             bool store;
             V3<T> spos;
@@ -260,6 +262,9 @@ __global__ void __launch_bounds__(256, TraceBlocks<T>::value) k_trace(SceneView<
             active = alive && ph.level < MAX_TRACE;
         }
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rays += __shfl_xor_sync(0xffffffffu, rays, o);
+    if (lane == 0 && rays) atomicAdd(&st->photon_rays, (unsigned long long)rays);
 }
 
 template <typename T>

@@ -76,7 +76,8 @@ class Stats(C.Structure):
                 ("grid_cells", C.c_int64), ("passes_done", C.c_int64), ("kernels_per_pass", C.c_int32),
                 ("n_stages", C.c_int32), ("r2", C.c_double), ("stage_ms", C.c_double * 16),
                 ("stage_calls", C.c_int64 * 16), ("candidates", C.c_int64), ("in_radius", C.c_int64),
-                ("gather_slots", C.c_int64), ("cell_factor", C.c_int32)]
+                ("gather_slots", C.c_int64), ("cell_factor", C.c_int32), ("photon_rays", C.c_int64),
+                ("eye_rays", C.c_int64)]
 
 
 # ---------------------------------------------------------------------------

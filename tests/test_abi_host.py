@@ -124,3 +124,4 @@ def test_batch_job_layout_matches_header(built_lib):
     config at 48 and the image pointer at 112 (120 bytes)."""
     assert C.sizeof(S.Job) == 120 and S.Job.cfg.offset == 48 and S.Job.image_out.offset == 112
     assert C.sizeof(S.RenderCfg) == 64
+    assert C.sizeof(S.Stats) == 360 and S.Stats.photon_rays.offset == 344

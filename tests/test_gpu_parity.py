@@ -159,66 +159,6 @@ _oct_roundtrip = W.oct_roundtrip
 
 
 @pytest.mark.parametrize("clustered", [False, True])
-def test_within_fp64_sets_equal(ctx, clustered):
-    rng = np.random.default_rng(5)
-    pos, d, wl = _photon_cloud(rng, 60000, clustered)
-    R2 = 0.03 ** 2
-    ctx.build_photonmap(pos, d, wl, 0.01, R2)
-    q = np.vstack([rng.random((3000, 3)), pos[rng.integers(0, len(pos), 1000)]])
-    r2 = np.concatenate([np.full(2000, R2), rng.uniform(0, R2, len(q) - 2000)])
-    off, idx = ctx.query_within(q, r2)
-    ooff, oidx = Oracle(S.Scene()).within(pos, q, r2)
-    assert np.array_equal(off, ooff)
-    assert np.array_equal(idx, oidx)
-    assert len(idx) > 10000
-
-
-def test_within_fp64_boundary_equality(ctx):
-    # photons placed exactly at distance^2 == r2 (in f64) are inside (<=)
-    pos = np.array([[0.5, 0.5, 0.5], [0.75, 0.5, 0.5], [0.5, 0.25, 0.5], [0.5, 0.5, 0.8]])
-    d = np.tile([0.0, 0.0, -1.0], (4, 1))
-    wl = np.zeros(4, np.uint8)
-    ctx.build_photonmap(pos, d, wl, 1.0, 0.0625)
-    off, idx = ctx.query_within(np.array([[0.5, 0.5, 0.5]]), 0.0625)
-    assert sorted(idx.tolist()) == [0, 1, 2]
-
-
-def test_estimate_fp64(ctx):
-    rng = np.random.default_rng(6)
-    pos, d, wl = _photon_cloud(rng, 50000)
-    R2 = 0.04 ** 2
-    ctx.build_photonmap(pos, d, wl, 0.002, R2)
-    q = rng.random((4000, 3))
-    n = rng.normal(size=(4000, 3))
-    n /= np.linalg.norm(n, axis=1, keepdims=True)
-    orc = Oracle(S.Scene())
-    for pf in (S.FILTER_NONE, S.FILTER_CONE, S.FILTER_GAUSS):
-        g = ctx.estimate(q, n, pf)
-        o = orc.estimate(pos, d, wl, q, n, R2, 0.002, pf)
-        assert np.allclose(g, o, rtol=1e-9, atol=1e-12), pf
-        assert (o > 0).mean() > 0.3
-
-
-def _oct_roundtrip(d):
-    """FP32 octahedral 15+15-bit encode/decode as the FP32 map stores directions."""
-    d = d.astype(np.float32)
-    s = np.abs(d).sum(1, dtype=np.float32)
-    p = d[:, :2] / s[:, None]
-    neg = d[:, 2] < 0
-    sg = np.where(p >= 0, np.float32(1), np.float32(-1))
-    fold = (np.float32(1) - np.abs(p[:, ::-1])) * sg
-    p = np.where(neg[:, None], fold, p)
-    qv = np.clip(np.rint((p * np.float32(0.5) + np.float32(0.5)) * np.float32(32767)), 0, 32767)
-    p = qv.astype(np.float32) * np.float32(2.0 / 32767.0) - np.float32(1)
-    z = np.float32(1) - np.abs(p[:, 0]) - np.abs(p[:, 1])
-    sg = np.where(p >= 0, np.float32(1), np.float32(-1))
-    fold = (np.float32(1) - np.abs(p[:, ::-1])) * sg
-    p = np.where((z < 0)[:, None], fold, p)
-    v = np.column_stack([p, z]).astype(np.float64)
-    return v / np.linalg.norm(v, axis=1, keepdims=True)
-
-
-@pytest.mark.parametrize("clustered", [False, True])
 def test_fp32_map_sets_and_estimates(ctx, clustered):
     rng = np.random.default_rng(7)
     pos, d, wl = _photon_cloud(rng, 80000, clustered)
@@ -266,6 +206,23 @@ def test_render_graph_equals_eager(ctx):
             imgs.append(ctx.render(cfg))
     assert np.allclose(imgs[0], imgs[2], rtol=1e-9, atol=1e-14)
     assert np.allclose(imgs[1], imgs[3], rtol=1e-5, atol=1e-12)
+
+
+def test_ray_counters(ctx):
+    """photon_rays counts one segment per photon event, eye_rays the eye-tree
+    rays; both are per pass and reproducible for a fixed seed."""
+    sc, cam, orc = _setup(ctx, "box_c1")
+    npx = cam.xreso * cam.yreso
+    seen = []
+    for g in (False, True):
+        cfg = RenderConfig(nphoton=20000, passes=2, radius0=0.08, precision=PLAIN, use_graph=g, seed=11)
+        ctx.render(cfg)
+        st = ctx.stats()
+        assert st["photons_emitted"] <= st["photon_rays"] <= 10 * st["photons_emitted"]
+        assert st["photons_stored"] <= st["photon_rays"]
+        assert npx < st["eye_rays"] < 10 * npx          # the mirror sphere spawns children
+        seen.append((st["photon_rays"], st["eye_rays"]))
+    assert seen[0] == seen[1]
 
 
 def test_mixed_matches_plain_statistically(ctx):
