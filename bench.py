@@ -362,7 +362,8 @@ def run_gpu(args, w):
         "eye_rays_per_s": st_t["eye_rays"] / (stage_avg["eye_trace"] / 1e3),
         "photon_rays_per_pass": st_t["photon_rays"], "eye_rays_per_pass": st_t["eye_rays"],
         "photon_tests_per_s": cnt["candidates"] / (g_ms / 1e3), "in_radius_per_s": cnt["in_radius"] / (g_ms / 1e3),
-        "candidates": cnt["candidates"], "in_radius": cnt["in_radius"], "gather_ms": round(g_ms, 4),
+        "candidates": cnt["candidates"], "in_radius": cnt["in_radius"], "lane_slots": cnt["gather_slots"],
+        "gather_ms": round(g_ms, 4),
         "pass": mid + 1,
         "note": ("ray rates: last pass of the stage-timed run over its stage's mean time (eye rays: primary "
                  "and reflected/refracted children, shadow rays not counted); photon tests: one pass from the "
