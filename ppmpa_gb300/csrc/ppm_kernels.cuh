@@ -723,6 +723,34 @@ __device__ __forceinline__ void for_each_candidate_pair(const GridParams &g, con
     }
 }
 
+// The render gather's walk: the same steps as for_each_candidate_pair, with
+// a lane's two candidates handed to one call, use(p0, valid0, p1, valid1),
+// so that their radius tests and direction decodes form two independent
+// instruction chains in one block (one branch per step instead of two).
+template <typename U>
+__device__ __forceinline__ void for_each_candidate_two(const GridParams &g, const uint32_t *start, V3<float> q,
+                                                       float r2, const int lo[3], const int hi[3],
+                                                       const float4 *smap, U &&use) {
+    const int nrows = (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+    for (int row0 = 0; row0 < nrows; row0 += 32) {
+        RowSet rs = make_rows(g, start, q, r2, lo, hi, row0);
+        unsigned m = rs.nonempty;
+        while (m) {
+            int r = __ffs(m) - 1;
+            m &= m - 1;
+            const uint32_t b = __shfl_sync(0xffffffffu, rs.begin, r);
+            const uint32_t n = __shfl_sync(0xffffffffu, rs.len, r);
+            for (uint32_t base = 0; base < n; base += 64) {
+                const uint32_t o0 = base + lane_id(), o1 = o0 + 32;
+                const bool v0 = o0 < n, v1 = o1 < n;
+                const float4 p0 = __ldg(&smap[v0 ? b + o0 : b]);
+                const float4 p1 = __ldg(&smap[v1 ? b + o1 : b]);
+                use(p0, v0, p1, v1);
+            }
+        }
+    }
+}
+
 __device__ __forceinline__ double filter_wt(int pfilter, double d, double r2) {
     if (pfilter == PF_CONE) {   // tracer.rs:201-204
         double d2 = sqrt(d / r2) / 1.1;
@@ -929,39 +957,71 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
         V3<float> q = ld3(h.pos), n = ld3(h.nrm);
         int c[3], lo[3], hi[3];
         query_cells(g, q, ext, extx, c, lo, hi);
-        // Per-lane sums: compensated (Kahan) for the estimate entry point,
-        // whose queries can gather thousands of photons per lane; plain for
-        // the render, where a lane adds a few dozen terms (relative error
-        // < 1e-6) and the three sums take the photon's value or zero without
-        // a branch on its wavelength.
+        // Per-lane sums: compensated (Kahan) for the estimate entry point
+        // (PERQ), whose queries can gather thousands of photons per lane;
+        // plain for the render, where a lane adds a few dozen terms (relative
+        // error < 1e-6) and the three sums take the photon's value or zero
+        // without a branch on its wavelength.
         Kahan k0 = {0.f, 0.f}, k1 = {0.f, 0.f}, k2 = {0.f, 0.f};
         unsigned long long c_slots = 0, c_valid = 0, c_hits = 0;
-        for_each_candidate_pair(g, start, q, r2f, lo, hi, smap, [&](float4 pp, bool valid) {
-            if (COUNT) {
-                c_slots += 1;
-                c_valid += valid;
-            }
-            if (!valid) return;
-            float d2f;
-            if (in_radius_f32(q.x, q.y, q.z, pp, r2_lo, r2_hi, r2, d2f)) {
-                uint32_t m = __float_as_uint(pp.w);
-                V3<float> pd = oct_unpack(m);
-                float cos0 = dot(n, pd);
-                float val = cos0 < 0.0f ? -cos0 : 0.0f;
-                if (pfilter != PF_NONE) val *= filter_wt_f(pfilter, d2f, r2f);
-                const uint32_t wl = m >> 30;
-                if constexpr (PERQ) {
+        if constexpr (!PERQ) {
+            for_each_candidate_two(g, start, q, r2f, lo, hi, smap, [&](float4 p0, bool v0, float4 p1, bool v1) {
+                if (COUNT) {
+                    c_slots += 2;   // both halves of the step are evaluated
+                    c_valid += (int)v0 + (int)v1;
+                }
+                float dx = q.x - p0.x, dy = q.y - p0.y, dz = q.z - p0.z;
+                const float d0 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                dx = q.x - p1.x;
+                dy = q.y - p1.y;
+                dz = q.z - p1.z;
+                const float d1 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                // in_radius_f32 on both: below r2_lo in, above r2_hi out, between in FP64
+                bool in0 = v0 && d0 < r2_lo, in1 = v1 && d1 < r2_lo;
+                const bool b0 = v0 && !in0 && d0 <= r2_hi, b1 = v1 && !in1 && d1 <= r2_hi;
+                if (b0 || b1) {
+                    const double qx = q.x, qy = q.y, qz = q.z;
+                    if (b0) in0 = sq_euclid(qx, qy, qz, (double)p0.x, (double)p0.y, (double)p0.z) <= r2;
+                    if (b1) in1 = sq_euclid(qx, qy, qz, (double)p1.x, (double)p1.y, (double)p1.z) <= r2;
+                }
+                if (in0 || in1) {
+                    const uint32_t m0 = __float_as_uint(p0.w), m1 = __float_as_uint(p1.w);
+                    const V3<float> e0 = oct_unpack(m0), e1 = oct_unpack(m1);
+                    const float c0 = dot(n, e0), c1 = dot(n, e1);
+                    float w0 = (in0 && c0 < 0.0f) ? -c0 : 0.0f, w1 = (in1 && c1 < 0.0f) ? -c1 : 0.0f;
+                    if (pfilter != PF_NONE) {
+                        w0 *= filter_wt_f(pfilter, d0, r2f);
+                        w1 *= filter_wt_f(pfilter, d1, r2f);
+                    }
+                    const uint32_t l0 = m0 >> 30, l1 = m1 >> 30;
+                    k0.s += (l0 == 0u ? w0 : 0.0f) + (l1 == 0u ? w1 : 0.0f);
+                    k1.s += (l0 == 1u ? w0 : 0.0f) + (l1 == 1u ? w1 : 0.0f);
+                    k2.s += (l0 >= 2u ? w0 : 0.0f) + (l1 >= 2u ? w1 : 0.0f);
+                    if (COUNT) c_hits += (int)in0 + (int)in1;
+                }
+            });
+        } else {
+            for_each_candidate_pair(g, start, q, r2f, lo, hi, smap, [&](float4 pp, bool valid) {
+                if (COUNT) {
+                    c_slots += 1;
+                    c_valid += valid;
+                }
+                if (!valid) return;
+                float d2f;
+                if (in_radius_f32(q.x, q.y, q.z, pp, r2_lo, r2_hi, r2, d2f)) {
+                    uint32_t m = __float_as_uint(pp.w);
+                    V3<float> pd = oct_unpack(m);
+                    float cos0 = dot(n, pd);
+                    float val = cos0 < 0.0f ? -cos0 : 0.0f;
+                    if (pfilter != PF_NONE) val *= filter_wt_f(pfilter, d2f, r2f);
+                    const uint32_t wl = m >> 30;
                     if (wl == 0u) k0.add(val);
                     else if (wl == 1u) k1.add(val);
                     else k2.add(val);
-                } else {
-                    k0.s += wl == 0u ? val : 0.0f;
-                    k1.s += wl == 1u ? val : 0.0f;
-                    k2.s += wl >= 2u ? val : 0.0f;
+                    if (COUNT) c_hits += 1;
                 }
-                if (COUNT) c_hits += 1;
-            }
-        });
+            });
+        }
         float s0 = warp_sum(k0.s - k0.c), s1 = warp_sum(k1.s - k1.c), s2 = warp_sum(k2.s - k2.c);
         if (COUNT) {
             for (int o = 16; o > 0; o >>= 1) {
