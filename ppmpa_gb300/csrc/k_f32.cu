@@ -62,7 +62,7 @@ void launch_query_sort_f(const float *pos, const float *nrm, const double *r2, l
                          HitPoint<float> *hits, double *r2_sorted, int grid, cudaStream_t s) {
     if (n <= 0) return;
     k_query_hist<<<grid, 256, 0, s>>>(pos, n, st, count, keyrank);
-    launch_scan(count, st, block_sums, qstart, cell_cap, s);
+    launch_scan(count, st, block_sums, qstart, cell_cap, s, grid);
     k_query_place<<<grid, 256, 0, s>>>(pos, nrm, r2, n, qstart, keyrank, hits, r2_sorted);
 }
 void launch_intersect_f(const SceneView<float> &sc, const double *rays, long long n, double *t, int32_t *obj,

@@ -91,24 +91,46 @@ __global__ void k_grid_setup(PassState *st, double r2_override) {
 
 // exclusive scan of count[0, ncell) into start[0, ncell], zeroing count
 // (reduce -> scan of tile sums -> downsweep; no inter-block waiting)
+// Exclusive scan of the per-key counts into start[] (the photon map's cell
+// starts) in tiles of SCAN_TILE keys: per-tile sums, a one-block scan of the
+// tile sums, then each tile scanned from its offset.  The tile kernels loop
+// over the tiles the pass's grid has (nkeys varies per pass; the launch is
+// sized once for the capacity), read and write 16 bytes per thread per
+// round, and clear the counts for the next pass.
+constexpr int SCAN_ROUND = 256 * 4;   // keys per round: 256 threads x one uint4
+
+__device__ __forceinline__ uint4 load_counts(const uint32_t *count, long long i, long long n) {
+    if (i + 3 < n) return *reinterpret_cast<const uint4 *>(count + i);
+    uint4 v;
+    v.x = i < n ? count[i] : 0u;
+    v.y = i + 1 < n ? count[i + 1] : 0u;
+    v.z = i + 2 < n ? count[i + 2] : 0u;
+    v.w = i + 3 < n ? count[i + 3] : 0u;
+    return v;
+}
+
 __global__ void __launch_bounds__(256) k_scan_reduce(const uint32_t *count, const PassState *st, uint32_t *block_sums) {
     const long long n = st->grid.nkeys;
-    const long long base = (long long)blockIdx.x * SCAN_TILE;
-    if (base >= n) return;
-    uint32_t s = 0;
-    for (int j = threadIdx.x; j < SCAN_TILE; j += 256) {
-        long long i = base + j;
-        if (i < n) s += count[i];
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    const long long ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     __shared__ uint32_t ws[8];
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t t = 0;
-        for (int w = 0; w < 8; w++) t += ws[w];
-        block_sums[blockIdx.x] = t;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long long base = tile * SCAN_TILE;
+        uint32_t s = 0;
+#pragma unroll
+        for (int k = 0; k < SCAN_TILE / SCAN_ROUND; k++) {
+            const uint4 v = load_counts(count, base + (long long)k * SCAN_ROUND + 4 * threadIdx.x, n);
+            s += (v.x + v.y) + (v.z + v.w);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+            for (int w = 0; w < 8; w++) t += ws[w];
+            block_sums[tile] = t;
+        }
+        __syncthreads();
     }
 }
 
@@ -142,40 +164,53 @@ __global__ void __launch_bounds__(1024) k_scan_top(uint32_t *block_sums, const P
 __global__ void __launch_bounds__(256) k_scan_down(uint32_t *count, const PassState *st, const uint32_t *block_sums,
                                                    uint32_t *start) {
     const long long n = st->grid.nkeys;
-    const long long base = (long long)blockIdx.x * SCAN_TILE;
-    if (base >= n) return;
-    constexpr int PER = SCAN_TILE / 256;   // 16 consecutive cells per thread
-    uint32_t v[PER], t = 0;
-    const long long my = base + (long long)threadIdx.x * PER;
-#pragma unroll
-    for (int j = 0; j < PER; j++) {
-        long long i = my + j;
-        v[j] = i < n ? count[i] : 0u;
-        t += v[j];
-    }
-    // block exclusive scan of t
-    uint32_t incl = t;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
-        if ((threadIdx.x & 31) >= (unsigned)o) incl += u;
-    }
+    const long long ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ uint32_t ws[8];
-    if ((threadIdx.x & 31) == 31) ws[threadIdx.x >> 5] = incl;
-    __syncthreads();
-    uint32_t woff = 0;
-    for (int w = 0; w < (int)(threadIdx.x >> 5); w++) woff += ws[w];
-    uint32_t run = block_sums[blockIdx.x] + woff + incl - t;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long long base = tile * SCAN_TILE;
+        uint32_t run = block_sums[tile];   // keys before this tile
+#pragma unroll 1
+        for (int k = 0; k < SCAN_TILE / SCAN_ROUND; k++) {
+            const long long i = base + (long long)k * SCAN_ROUND + 4 * threadIdx.x;
+            const uint4 v = load_counts(count, i, n);
+            const uint32_t t = (v.x + v.y) + (v.z + v.w);
+            uint32_t incl = t;
 #pragma unroll
-    for (int j = 0; j < PER; j++) {
-        long long i = my + j;
-        if (i < n) {
-            start[i] = run;
-            count[i] = 0u;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= (unsigned)o) incl += u;
+            }
+            if (lane == 31) ws[warp] = incl;
+            __syncthreads();
+            uint32_t woff = 0, total = 0;
+#pragma unroll
+            for (int w = 0; w < 8; w++) {
+                const uint32_t x = ws[w];
+                woff += (unsigned)w < warp ? x : 0u;
+                total += x;
+            }
+            uint4 o;
+            o.x = run + woff + incl - t;
+            o.y = o.x + v.x;
+            o.z = o.y + v.y;
+            o.w = o.z + v.z;
+            if (i + 3 < n) {
+                *reinterpret_cast<uint4 *>(start + i) = o;
+                *reinterpret_cast<uint4 *>(count + i) = make_uint4(0u, 0u, 0u, 0u);
+            } else {
+                const uint32_t ov[4] = {o.x, o.y, o.z, o.w};
+                for (int j = 0; j < 4; j++)
+                    if (i + j < n) {
+                        start[i + j] = ov[j];
+                        count[i + j] = 0u;
+                    }
+            }
+            run += total;
+            __syncthreads();   // ws is rewritten by the next round
         }
-        run += v[j];
+        if (threadIdx.x == 0 && base + SCAN_TILE >= n) start[n] = run;   // the tile holding the last key
     }
-    if (my < n && my + PER >= n) start[n] = run;   // the thread holding the last cell
 }
 
 __global__ void k_accum(const double *pass_img, double *sum, long long n) {
@@ -193,8 +228,9 @@ __global__ void k_pass_end(PassState *st) {
 void launch_pass_begin(PassState *st, cudaStream_t s) { k_pass_begin<<<1, 32, 0, s>>>(st); }
 void launch_grid_setup(PassState *st, double r2_override, cudaStream_t s) { k_grid_setup<<<1, 32, 0, s>>>(st, r2_override); }
 void launch_scan(uint32_t *count, const PassState *st, uint32_t *block_sums, uint32_t *start, long long cell_cap,
-                 cudaStream_t s) {
-    int nb = (int)((cell_cap + SCAN_TILE - 1) / SCAN_TILE);
+                 cudaStream_t s, int grid) {
+    const long long tiles = (cell_cap + SCAN_TILE - 1) / SCAN_TILE;
+    const int nb = (int)(tiles < grid ? tiles : grid);
     k_scan_reduce<<<nb, 256, 0, s>>>(count, st, block_sums);
     k_scan_top<<<1, 1024, 0, s>>>(block_sums, st);
     k_scan_down<<<nb, 256, 0, s>>>(count, st, block_sums, start);

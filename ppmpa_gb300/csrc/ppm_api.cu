@@ -399,10 +399,12 @@ static int enqueue_eye(ppm_ctx *ctx, HitPoint<T> *hits, Level level_fn, cudaStre
     using V = vec4_t<T>;
     EyeQueue<T> qa{as<V>(ctx->eqb[0]), as<V>(ctx->eqb[1]), as<V>(ctx->eqb[2])};
     EyeQueue<T> qb{as<V>(ctx->eqb[3]), as<V>(ctx->eqb[4]), as<V>(ctx->eqb[5])};
+    // Level 0 has one thread per pixel.  The deeper levels' sizes are only
+    // known on the device; their grids stride over the queue.
     const int g0 = (int)std::max(1LL, std::min<long long>((ctx->npx + 127) / 128, (long long)ctx->sm_count * 16));
     for (int l = 0; l < MAX_TRACE; l++)
         level_fn(l, (l & 1) ? qb : qa, (l & 1) ? qa : qb, (unsigned long long)ctx->eq_cap, hits,
-                 l == 0 ? g0 : grid_blocks(ctx, 16), s);
+                 l == 0 ? g0 : grid_blocks(ctx, 4), s);
     return MAX_TRACE;
 }
 
@@ -819,7 +821,7 @@ static int build_map_d(ppm_ctx *ctx, long long n, double r2, double pw) {
     launch_grid_setup(ctx->st, r2, ctx->s);
     launch_hist_d(pb, ctx->st, n, as<uint32_t>(ctx->count), as<uint2>(ctx->keyrank), g, ctx->s);
     launch_scan(as<uint32_t>(ctx->count), ctx->st, as<uint32_t>(ctx->block_sums), as<uint32_t>(ctx->start), CELL_CAP,
-                ctx->s);
+                ctx->s, grid_blocks(ctx, 8));
     launch_scatter_d(pb, ctx->st, n, as<uint32_t>(ctx->start), as<uint2>(ctx->keyrank), g, ctx->s);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(ctx->s));
@@ -1094,7 +1096,7 @@ static int grid_map_f32(ppm_ctx *ctx, long long n, double r2max, double k) {
     launch_grid_setup(ctx->st, r2max, ctx->s);
     launch_hist_f(pb, ctx->st, n, as<uint32_t>(ctx->count), as<uint2>(ctx->keyrank), g, ctx->s);
     launch_scan(as<uint32_t>(ctx->count), ctx->st, as<uint32_t>(ctx->block_sums), as<uint32_t>(ctx->start), CELL_CAP,
-                ctx->s);
+                ctx->s, grid_blocks(ctx, 8));
     launch_scatter_f(pb, ctx->st, n, as<uint32_t>(ctx->start), as<uint2>(ctx->keyrank), g, ctx->s);
     CK(cudaGetLastError());
     return PPM_OK;
@@ -1407,7 +1409,8 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
         if (ev) CK(cudaEventRecord(ev[1], s));
         launch_grid_setup(ctx->st, -1.0, s);
         launch_hist_f(pb, ctx->st, -1, as<uint32_t>(ctx->count), as<uint2>(ctx->keyrank), g8, s);
-        launch_scan(as<uint32_t>(ctx->count), ctx->st, as<uint32_t>(ctx->block_sums), as<uint32_t>(ctx->start), CELL_CAP, s);
+        launch_scan(as<uint32_t>(ctx->count), ctx->st, as<uint32_t>(ctx->block_sums), as<uint32_t>(ctx->start), CELL_CAP, s,
+                    grid_blocks(ctx, 8));
         launch_scatter_f(pb, ctx->st, -1, as<uint32_t>(ctx->start), as<uint2>(ctx->keyrank), g8, s);
     } else {
         PhotonBuf<double> pb{as<PhotonD>(ctx->raw_d), as<double4>(ctx->spos), as<double4>(ctx->sdir)};
@@ -1416,7 +1419,8 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
         if (ev) CK(cudaEventRecord(ev[1], s));
         launch_grid_setup(ctx->st, -1.0, s);
         launch_hist_d(pb, ctx->st, -1, as<uint32_t>(ctx->count), as<uint2>(ctx->keyrank), g8, s);
-        launch_scan(as<uint32_t>(ctx->count), ctx->st, as<uint32_t>(ctx->block_sums), as<uint32_t>(ctx->start), CELL_CAP, s);
+        launch_scan(as<uint32_t>(ctx->count), ctx->st, as<uint32_t>(ctx->block_sums), as<uint32_t>(ctx->start), CELL_CAP, s,
+                    grid_blocks(ctx, 8));
         launch_scatter_d(pb, ctx->st, -1, as<uint32_t>(ctx->start), as<uint2>(ctx->keyrank), g8, s);
     }
     kernels += 4 + kernels_per_scan();

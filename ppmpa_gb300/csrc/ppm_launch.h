@@ -74,8 +74,9 @@ int launch_bvh_build(const DObject<double> *objs, const int32_t *bounded, int m,
 constexpr int SCAN_TILE = 4096;
 void launch_pass_begin(PassState *st, cudaStream_t s);
 void launch_grid_setup(PassState *st, double r2_override, cudaStream_t s);
+// grid: blocks of the two tile kernels (each loops over the pass's tiles)
 void launch_scan(uint32_t *count, const PassState *st, uint32_t *block_sums, uint32_t *start, long long cell_cap,
-                 cudaStream_t s);
+                 cudaStream_t s, int grid);
 void launch_accum(const double *pass_img, double *sum, long long n, cudaStream_t s);
 void launch_accum_mixed(const float *direct, const float *gathered, const PassState *st, double pw, double *pass_img,
                         double *sum, long long n, cudaStream_t s);
