@@ -20,6 +20,7 @@ __global__ void k_pass_begin(PassState *st) {
     st->emit_next = 0;
     st->photon_rays = 0;
     for (int l = 0; l < MAX_TRACE + 2; l++) st->eq[l] = 0;
+    st->inv_pi_r2 = ONE_PI_D / st->r2;
     for (int a = 0; a < 3; a++) {
         st->bb_lo[a] = ord_enc(1e300);
         st->bb_hi[a] = ord_enc(-1e300);
@@ -243,9 +244,13 @@ void launch_pass_end(PassState *st, cudaStream_t s) { k_pass_end<<<1, 32, 0, s>>
 
 // FP32 path: pass image = direct + gathered * pw / (pi r2) in FP64 (the flux
 // normalisation by the emitted photon count), added to the FP64 running sum
+// (FP64 is a narrow pipe on this GPU: the per-pass constant comes from the
+// pass state, computed once at pass begin, and each thread takes several
+// elements, so the FP64 work per element is the two conversions, one fused
+// multiply-add and the running-sum add.)
 __global__ void k_accum_mixed(const float *direct, const float *gathered, const PassState *st, double pw,
                               double *pass_img, double *sum, long long n) {
-    const double kk = pw * (ONE_PI_D / st->r2);
+    const double kk = pw * st->inv_pi_r2;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         double v = (double)direct[i] + (double)gathered[i] * kk;
         pass_img[i] = v;
@@ -254,7 +259,7 @@ __global__ void k_accum_mixed(const float *direct, const float *gathered, const 
 }
 void launch_accum_mixed(const float *direct, const float *gathered, const PassState *st, double pw, double *pass_img,
                         double *sum, long long n, cudaStream_t s) {
-    k_accum_mixed<<<(unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096), 256, 0, s>>>(direct, gathered, st, pw,
+    k_accum_mixed<<<(unsigned)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024), 256, 0, s>>>(direct, gathered, st, pw,
                                                                                              pass_img, sum, n);
 }
 

@@ -57,6 +57,7 @@ struct PassState {
     unsigned long long gather_next;             // next query chunk of the FP32 gather
     unsigned long long emit_next;               // next emission index of the persistent photon trace
     double cell_factor;
+    double inv_pi_r2;          // 1 / (pi r2) of the current pass, set at pass begin
     int32_t cell_sx;           // x cells per y/z cell (>= 1)
     int32_t pad2;
     int64_t cell_cap;
