@@ -697,8 +697,9 @@ __device__ __forceinline__ void for_each_candidate(const GridParams &g, const ui
 
 // The same walk for the FP32 gather, two candidates per lane per step: both
 // photons are loaded before either is used (two loads in flight per lane,
-// half the loop overhead).  use(photon, valid) must not contain warp-collective
-// operations (the second call is skipped when no lane has a second photon).
+// half the loop overhead).  Every lane makes every use(photon, valid) call
+// (the second call of a step is skipped by the whole warp when no lane has a
+// second photon), so use() may hold warp votes.
 template <typename T, typename U>
 __device__ __forceinline__ void for_each_candidate_pair(const GridParams &g, const uint32_t *start, V3<T> q, T r2,
                                                         const int lo[3], const int hi[3], const float4 *smap,
@@ -728,6 +729,7 @@ __device__ __forceinline__ void for_each_candidate_pair(const GridParams &g, con
 // a lane's two candidates handed to one call, use(p0, valid0, p1, valid1),
 // so that their radius tests and direction decodes form two independent
 // instruction chains in one block (one branch per step instead of two).
+// Every lane makes every call, so use() may hold warp votes.
 template <typename U>
 __device__ __forceinline__ void for_each_candidate_two(const GridParams &g, const uint32_t *start, V3<float> q,
                                                        float r2, const int lo[3], const int hi[3],
@@ -977,10 +979,13 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
                 dy = q.y - p1.y;
                 dz = q.z - p1.z;
                 const float d1 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                // in_radius_f32 on both: below r2_lo in, above r2_hi out, between in FP64
+                // in_radius_f32 on both: below r2_lo in, above r2_hi out, between in FP64.
+                // The vote keeps the FP64 recheck a branch that warps almost never
+                // take; left to the compiler it was predicated into every step,
+                // which costs issue slots on this GPU's narrow FP64 pipe.
                 bool in0 = v0 && d0 < r2_lo, in1 = v1 && d1 < r2_lo;
                 const bool b0 = v0 && !in0 && d0 <= r2_hi, b1 = v1 && !in1 && d1 <= r2_hi;
-                if (b0 || b1) {
+                if (__any_sync(0xffffffffu, b0 || b1)) {
                     const double qx = q.x, qy = q.y, qz = q.z;
                     if (b0) in0 = sq_euclid(qx, qy, qz, (double)p0.x, (double)p0.y, (double)p0.z) <= r2;
                     if (b1) in1 = sq_euclid(qx, qy, qz, (double)p1.x, (double)p1.y, (double)p1.z) <= r2;
@@ -1007,9 +1012,15 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
                     c_slots += 1;
                     c_valid += valid;
                 }
-                if (!valid) return;
-                float d2f;
-                if (in_radius_f32(q.x, q.y, q.z, pp, r2_lo, r2_hi, r2, d2f)) {
+                // in_radius_f32, with the FP64 recheck behind a warp vote (see the render walk)
+                const float dx = q.x - pp.x, dy = q.y - pp.y, dz = q.z - pp.z;
+                const float d2f = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                bool in = valid && d2f < r2_lo;
+                const bool band = valid && !in && d2f <= r2_hi;
+                if (__any_sync(0xffffffffu, band))
+                    if (band) in = sq_euclid((double)q.x, (double)q.y, (double)q.z, (double)pp.x, (double)pp.y,
+                                             (double)pp.z) <= r2;
+                if (in) {
                     uint32_t m = __float_as_uint(pp.w);
                     V3<float> pd = oct_unpack(m);
                     float cos0 = dot(n, pd);
