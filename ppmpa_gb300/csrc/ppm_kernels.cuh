@@ -121,17 +121,20 @@ __device__ __forceinline__ uint32_t oct_pack(float x, float y, float z, int wl) 
     qx = min(qx, 32767u); qy = min(qy, 32767u);
     return qx | (qy << 15) | ((uint32_t)wl << 30);
 }
-__device__ __forceinline__ V3<float> oct_unpack(uint32_t m) {
+// cos(n, d) for the packed direction d.  Decode: p = q * 2/32767 - 1 per
+// component, z = 1 - |px| - |py|; below the equator (z < 0) the octahedron's
+// fold maps (px, py) to ((1 - |py|) sign px, (1 - |px|) sign py), written here
+// as px - copysign(-z, px) (equal in exact arithmetic, no branch).  The
+// normalisation is applied to the dot product.
+__device__ __forceinline__ float oct_dot(uint32_t m, V3<float> n) {
     float px = (float)(m & 32767u) * (2.0f / 32767.0f) - 1.0f;
     float py = (float)((m >> 15) & 32767u) * (2.0f / 32767.0f) - 1.0f;
-    float pz = 1.0f - fabsf(px) - fabsf(py);
-    if (pz < 0.0f) {
-        float ox = (1.0f - fabsf(py)) * (px >= 0.0f ? 1.0f : -1.0f);
-        float oy = (1.0f - fabsf(px)) * (py >= 0.0f ? 1.0f : -1.0f);
-        px = ox; py = oy;
-    }
-    float inv = rsqrtf(px * px + py * py + pz * pz);
-    return mk3(px * inv, py * inv, pz * inv);
+    const float pz = 1.0f - fabsf(px) - fabsf(py);
+    const float t = fmaxf(-pz, 0.0f);
+    px -= copysignf(t, px);
+    py -= copysignf(t, py);
+    const float len2 = __fmaf_rn(pz, pz, __fmaf_rn(py, py, px * px));
+    return (n.x * px + n.y * py + n.z * pz) * rsqrtf(len2);
 }
 
 // unsorted photon record of the FP64 path (also the parity download format)
@@ -992,8 +995,7 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
                 }
                 if (in0 || in1) {
                     const uint32_t m0 = __float_as_uint(p0.w), m1 = __float_as_uint(p1.w);
-                    const V3<float> e0 = oct_unpack(m0), e1 = oct_unpack(m1);
-                    const float c0 = dot(n, e0), c1 = dot(n, e1);
+                    const float c0 = oct_dot(m0, n), c1 = oct_dot(m1, n);
                     float w0 = (in0 && c0 < 0.0f) ? -c0 : 0.0f, w1 = (in1 && c1 < 0.0f) ? -c1 : 0.0f;
                     if (pfilter != PF_NONE) {
                         w0 *= filter_wt_f(pfilter, d0, r2f);
@@ -1022,8 +1024,7 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
                                              (double)pp.z) <= r2;
                 if (in) {
                     uint32_t m = __float_as_uint(pp.w);
-                    V3<float> pd = oct_unpack(m);
-                    float cos0 = dot(n, pd);
+                    float cos0 = oct_dot(m, n);
                     float val = cos0 < 0.0f ? -cos0 : 0.0f;
                     if (pfilter != PF_NONE) val *= filter_wt_f(pfilter, d2f, r2f);
                     const uint32_t wl = m >> 30;
