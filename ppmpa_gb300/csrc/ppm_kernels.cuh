@@ -13,6 +13,7 @@
 //             photon_to_radiance over the exact in-radius set (tracer.rs:179-195)
 //   accum   : FP64 running sum of pass images (util/averager.rb:66-69)
 #pragma once
+#include <type_traits>
 #include "ppm_trace.cuh"
 
 namespace ppm {
@@ -729,10 +730,13 @@ __device__ __forceinline__ void for_each_candidate_pair(const GridParams &g, con
 }
 
 // The render gather's walk: the same steps as for_each_candidate_pair, with
-// a lane's two candidates handed to one call, use(p0, valid0, p1, valid1),
-// so that their radius tests and direction decodes form two independent
-// instruction chains in one block (one branch per step instead of two).
-// Every lane makes every call, so use() may hold warp votes.
+// a lane's two candidates handed to one call, use(two, p0, valid0, p1,
+// valid1), so that their radius tests and direction decodes form two
+// independent instruction chains in one block (one branch per step instead
+// of two).  A step over a row's last 32 or fewer candidates passes
+// two = std::false_type and no second photon, so that the body compiled for
+// it does one candidate's work.  Every lane makes every call, so use() may
+// hold warp votes.
 template <typename U>
 __device__ __forceinline__ void for_each_candidate_two(const GridParams &g, const uint32_t *start, V3<float> q,
                                                        float r2, const int lo[3], const int hi[3],
@@ -750,8 +754,12 @@ __device__ __forceinline__ void for_each_candidate_two(const GridParams &g, cons
                 const uint32_t o0 = base + lane_id(), o1 = o0 + 32;
                 const bool v0 = o0 < n, v1 = o1 < n;
                 const float4 p0 = __ldg(&smap[v0 ? b + o0 : b]);
-                const float4 p1 = __ldg(&smap[v1 ? b + o1 : b]);
-                use(p0, v0, p1, v1);
+                if (base + 32 < n) {
+                    const float4 p1 = __ldg(&smap[v1 ? b + o1 : b]);
+                    use(std::true_type{}, p0, v0, p1, v1);
+                } else {
+                    use(std::false_type{}, p0, v0, p0, false);   // the row's last 32 or fewer
+                }
             }
         }
     }
@@ -971,23 +979,28 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
         Kahan k0 = {0.f, 0.f}, k1 = {0.f, 0.f}, k2 = {0.f, 0.f};
         unsigned long long c_slots = 0, c_valid = 0, c_hits = 0;
         if constexpr (!PERQ) {
-            for_each_candidate_two(g, start, q, r2f, lo, hi, smap, [&](float4 p0, bool v0, float4 p1, bool v1) {
+            for_each_candidate_two(g, start, q, r2f, lo, hi, smap,
+                                   [&](auto two, float4 p0, bool v0, float4 p1, bool v1) {
+                constexpr bool TWO = decltype(two)::value;
                 if (COUNT) {
-                    c_slots += 2;   // both halves of the step are evaluated
+                    c_slots += TWO ? 2 : 1;
                     c_valid += (int)v0 + (int)v1;
                 }
                 float dx = q.x - p0.x, dy = q.y - p0.y, dz = q.z - p0.z;
                 const float d0 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                dx = q.x - p1.x;
-                dy = q.y - p1.y;
-                dz = q.z - p1.z;
-                const float d1 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                float d1 = 0.0f;
+                if constexpr (TWO) {
+                    dx = q.x - p1.x;
+                    dy = q.y - p1.y;
+                    dz = q.z - p1.z;
+                    d1 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                }
                 // in_radius_f32 on both: below r2_lo in, above r2_hi out, between in FP64.
                 // The vote keeps the FP64 recheck a branch that warps almost never
                 // take; left to the compiler it was predicated into every step,
                 // which costs issue slots on this GPU's narrow FP64 pipe.
-                bool in0 = v0 && d0 < r2_lo, in1 = v1 && d1 < r2_lo;
-                const bool b0 = v0 && !in0 && d0 <= r2_hi, b1 = v1 && !in1 && d1 <= r2_hi;
+                bool in0 = v0 && d0 < r2_lo, in1 = TWO && v1 && d1 < r2_lo;
+                const bool b0 = v0 && !in0 && d0 <= r2_hi, b1 = TWO && v1 && !in1 && d1 <= r2_hi;
                 if (__any_sync(0xffffffffu, b0 || b1)) {
                     const double qx = q.x, qy = q.y, qz = q.z;
                     if (b0) in0 = sq_euclid(qx, qy, qz, (double)p0.x, (double)p0.y, (double)p0.z) <= r2;
@@ -995,16 +1008,23 @@ __global__ void __launch_bounds__(256) k_gather_f(const HitPoint<float> *hits, P
                 }
                 if (in0 || in1) {
                     const uint32_t m0 = __float_as_uint(p0.w), m1 = __float_as_uint(p1.w);
-                    const float c0 = oct_dot(m0, n), c1 = oct_dot(m1, n);
+                    const float c0 = oct_dot(m0, n);
+                    const float c1 = TWO ? oct_dot(m1, n) : 0.0f;
                     float w0 = (in0 && c0 < 0.0f) ? -c0 : 0.0f, w1 = (in1 && c1 < 0.0f) ? -c1 : 0.0f;
                     if (pfilter != PF_NONE) {
                         w0 *= filter_wt_f(pfilter, d0, r2f);
-                        w1 *= filter_wt_f(pfilter, d1, r2f);
+                        if (TWO) w1 *= filter_wt_f(pfilter, d1, r2f);
                     }
                     const uint32_t l0 = m0 >> 30, l1 = m1 >> 30;
-                    k0.s += (l0 == 0u ? w0 : 0.0f) + (l1 == 0u ? w1 : 0.0f);
-                    k1.s += (l0 == 1u ? w0 : 0.0f) + (l1 == 1u ? w1 : 0.0f);
-                    k2.s += (l0 >= 2u ? w0 : 0.0f) + (l1 >= 2u ? w1 : 0.0f);
+                    if constexpr (TWO) {
+                        k0.s += (l0 == 0u ? w0 : 0.0f) + (l1 == 0u ? w1 : 0.0f);
+                        k1.s += (l0 == 1u ? w0 : 0.0f) + (l1 == 1u ? w1 : 0.0f);
+                        k2.s += (l0 >= 2u ? w0 : 0.0f) + (l1 >= 2u ? w1 : 0.0f);
+                    } else {
+                        k0.s += l0 == 0u ? w0 : 0.0f;
+                        k1.s += l0 == 1u ? w0 : 0.0f;
+                        k2.s += l0 >= 2u ? w0 : 0.0f;
+                    }
                     if (COUNT) c_hits += (int)in0 + (int)in1;
                 }
             });
