@@ -49,6 +49,11 @@ __device__ __forceinline__ void slab(T o, T inv, float lo, float hi, T &t0, T &t
     t0 = a < b ? a : b;
     t1 = a < b ? b : a;
 }
+__device__ __forceinline__ void slab(float o, float inv, float lo, float hi, float &t0, float &t1) {
+    const float a = (lo - o) * inv, b = (hi - o) * inv;   // finite: inv is clamped by safe_inv
+    t0 = fminf(a, b);
+    t1 = fmaxf(a, b);
+}
 
 template <typename T>
 __device__ __forceinline__ bool box_hit(V3<T> o, V3<T> inv, float lx, float hx, float ly, float hy, float lz, float hz,
@@ -57,10 +62,16 @@ __device__ __forceinline__ bool box_hit(V3<T> o, V3<T> inv, float lx, float hx, 
     slab(o.x, inv.x, lx, hx, x0, x1);
     slab(o.y, inv.y, ly, hy, y0, y1);
     slab(o.z, inv.z, lz, hz, z0, z1);
-    T tn = x0 > y0 ? x0 : y0;
-    tn = tn > z0 ? tn : z0;
-    T tf = x1 < y1 ? x1 : y1;
-    tf = tf < z1 ? tf : z1;
+    T tn, tf;
+    if constexpr (sizeof(T) == 4) {
+        tn = fmaxf(fmaxf(x0, y0), z0);
+        tf = fminf(fminf(x1, y1), z1);
+    } else {
+        tn = x0 > y0 ? x0 : y0;
+        tn = tn > z0 ? tn : z0;
+        tf = x1 < y1 ? x1 : y1;
+        tf = tf < z1 ? tf : z1;
+    }
     tnear = tn;
     return tn <= tf && tf >= Cst<T>::nearly0() && tn <= tmax;
 }

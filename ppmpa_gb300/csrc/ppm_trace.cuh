@@ -225,9 +225,22 @@ __device__ __forceinline__ V3<T> diffuse_reflection(Rng &rg, V3<T> n) {
     return dot(n, d) > T(0) ? d : -d;
 }
 
-// generate_random_dir (cube rejection, 3 draws per trial, at most 256 trials)
+// generate_random_dir (cube rejection, 3 draws per trial, at most 256 trials).
+// The FP32 path draws the same uniform distribution on the sphere directly
+// (z = 1 - 2u, phi = 2 pi v: Archimedes' hat-box theorem), two draws and no
+// loop: the rejection loop's trial count differs between the lanes of a
+// warp, and the warp waits for its slowest lane.  The FP64 path keeps the
+// reference's draws, which its parity with the oracle checks one by one.
 template <typename T>
 __device__ __forceinline__ V3<T> random_dir(Rng &rg) {
+    if constexpr (sizeof(T) == 4) {
+        const T z = gen_range<T>(rg, T(-1), T(1));
+        const T phi = gen_range<T>(rg, T(0), T(2.0 * PI_D));
+        const T r = dsqrt(fmaxf(T(1) - z * z, T(0)));
+        T sn, cs;
+        Math<T>::sincos_(phi, sn, cs);
+        return mk3(r * cs, r * sn, z);
+    }
     for (int it = 0; it < 256; it++) {
         T x = gen_range<T>(rg, T(-1), T(1));
         T y = gen_range<T>(rg, T(-1), T(1));
