@@ -38,14 +38,12 @@ void launch_eye_level_f(const SceneView<float> &sc, const DCamera<float> &cam, u
 }
 void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
                      const uint32_t *start, double pw, const double *q_r2, int pfilter, int mode, GatherOutF out,
-                     int grid, cudaStream_t s, bool dyn) {
-#define PPM_GATHER(C, P, D) k_gather_f<C, P, D><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pw, q_r2, pfilter, mode, out)
-    if (q_r2 && out.count) PPM_GATHER(true, true, true);
-    else if (q_r2) PPM_GATHER(false, true, true);
-    else if (out.count && dyn) PPM_GATHER(true, false, true);
-    else if (out.count) PPM_GATHER(true, false, false);
-    else if (dyn) PPM_GATHER(false, false, true);
-    else PPM_GATHER(false, false, false);
+                     int grid, cudaStream_t s) {
+#define PPM_GATHER(C, P) k_gather_f<C, P><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pw, q_r2, pfilter, mode, out)
+    if (q_r2 && out.count) PPM_GATHER(true, true);
+    else if (q_r2) PPM_GATHER(false, true);
+    else if (out.count) PPM_GATHER(true, false);
+    else PPM_GATHER(false, false);
 #undef PPM_GATHER
 }
 void launch_within_f(const float *q, long long nq, const double *q_r2, const PassState *st, const float4 *smap,

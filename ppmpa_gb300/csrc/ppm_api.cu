@@ -1429,11 +1429,8 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
     if (ev) CK(cudaEventRecord(ev[7], s));
     if (mixed) {
         GatherOutF go{as<float>(ctx->pass_gather32), nullptr, ctx->count_gather ? &ctx->st->candidates : nullptr};
-        // above 2M photons per pass the stored map (1-3 photons of 16 B per
-        // emitted one) fills most of L2 or more: queries come from a counter
-        const bool dyn = ctx->cfg.nphoton > 2000000;
         launch_gather_f(as<HitPoint<float>>(ctx->hits_f), ctx->st, -1, as<float4>(ctx->sorted_f), as<uint32_t>(ctx->start),
-                        ctx->pw, nullptr, ctx->cam.pfilter, 0, go, g8, s, dyn);
+                        ctx->pw, nullptr, ctx->cam.pfilter, 0, go, g8, s);
     } else {
         GatherOutD go{as<double>(ctx->pass_img), nullptr, nullptr};
         launch_gather_d(as<HitPoint<double>>(ctx->hits_d), ctx->st, -1, as<double4>(ctx->spos), as<double4>(ctx->sdir),

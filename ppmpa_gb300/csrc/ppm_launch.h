@@ -47,7 +47,7 @@ void launch_eye_level_f(const SceneView<float> &sc, const DCamera<float> &cam, u
 // chooses it (maps larger than L2)
 void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
                      const uint32_t *start, double pw, const double *q_r2, int pfilter, int mode, GatherOutF out,
-                     int grid, cudaStream_t s, bool dyn = false);
+                     int grid, cudaStream_t s);
 void launch_within_f(const float *q, long long nq, const double *q_r2, const PassState *st, const float4 *smap,
                      const uint32_t *start, const int32_t *sidx, unsigned long long *counts,
                      const unsigned long long *offsets, int32_t *idx_out, int grid, cudaStream_t s);
