@@ -1215,7 +1215,7 @@ static int run_estimate_f32(ppm_ctx *ctx, const EstBatch &b, int64_t nq, bool co
     CK(cudaMemsetAsync(&ctx->st->gather_next, 0, sizeof(unsigned long long), ctx->s));
     if (e1) CK(cudaEventRecord(e1, ctx->s));
     launch_gather_f(b.h, ctx->st, nq, as<float4>(ctx->sorted_f), as<uint32_t>(ctx->start), ctx->map_pw, b.r2s, PF_NONE,
-                    1, go, grid_blocks(ctx, 8), ctx->s);
+                    go, grid_blocks(ctx, 8), ctx->s);
     CK(cudaGetLastError());
     if (e2) CK(cudaEventRecord(e2, ctx->s));
     return PPM_OK;
@@ -1430,7 +1430,7 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
     if (mixed) {
         GatherOutF go{as<float>(ctx->pass_gather32), nullptr, ctx->count_gather ? &ctx->st->candidates : nullptr};
         launch_gather_f(as<HitPoint<float>>(ctx->hits_f), ctx->st, -1, as<float4>(ctx->sorted_f), as<uint32_t>(ctx->start),
-                        ctx->pw, nullptr, ctx->cam.pfilter, 0, go, g8, s);
+                        ctx->pw, nullptr, ctx->cam.pfilter, go, g8, s);
     } else {
         GatherOutD go{as<double>(ctx->pass_img), nullptr, nullptr};
         launch_gather_d(as<HitPoint<double>>(ctx->hits_d), ctx->st, -1, as<double4>(ctx->spos), as<double4>(ctx->sdir),

@@ -890,13 +890,23 @@ __device__ __forceinline__ float warp_sum_comp(Kahan k) {
     return s + c;
 }
 
+// float -> double that the compiler cannot hoist out of a branch (an inline
+// cvt marked volatile): the gathers' FP64 rechecks of the query position sit
+// in branches almost never taken, and hoisted to once per query the
+// conversions cost FP64 issue slots on every query.
+__device__ __forceinline__ double f2d_here(float x) {
+    double d;
+    asm volatile("cvt.f64.f32 %0, %1;" : "=d"(d) : "f"(x));
+    return d;
+}
+
 __device__ __forceinline__ bool in_radius_f32(float qx, float qy, float qz, float4 pp, float r2_lo, float r2_hi,
                                               double r2, float &d2f) {
     float dx = qx - pp.x, dy = qy - pp.y, dz = qz - pp.z;
     d2f = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
     if (d2f < r2_lo) return true;
     if (d2f > r2_hi) return false;
-    return sq_euclid((double)qx, (double)qy, (double)qz, (double)pp.x, (double)pp.y, (double)pp.z) <= r2;
+    return sq_euclid(f2d_here(qx), f2d_here(qy), f2d_here(qz), (double)pp.x, (double)pp.y, (double)pp.z) <= r2;
 }
 
 __device__ __forceinline__ float filter_wt_f(int pfilter, float d, float r2) {
@@ -933,7 +943,7 @@ struct GatherOutF {
 template <bool COUNT, bool PERQ>
 __global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed,
                                                   const float4 *smap, const uint32_t *start, double pw,
-                                                  const double *q_r2, int pfilter, int mode, GatherOutF out) {
+                                                  const double *q_r2, int pfilter, GatherOutF out) {
     constexpr unsigned CHUNK = PERQ ? 4u : 2u;
     const unsigned long long nq = n_hitpoints(st, n_fixed);
     const GridParams g = st->grid;
@@ -999,7 +1009,7 @@ __global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<f
                 bool in0 = v0 && d0 < r2_lo, in1 = TWO && v1 && d1 < r2_lo;
                 const bool b0 = v0 && !in0 && d0 <= r2_hi, b1 = TWO && v1 && !in1 && d1 <= r2_hi;
                 if (__any_sync(0xffffffffu, b0 || b1)) {
-                    const double qx = q.x, qy = q.y, qz = q.z;
+                    const double qx = f2d_here(q.x), qy = f2d_here(q.y), qz = f2d_here(q.z);
                     if (b0) in0 = sq_euclid(qx, qy, qz, (double)p0.x, (double)p0.y, (double)p0.z) <= r2;
                     if (b1) in1 = sq_euclid(qx, qy, qz, (double)p1.x, (double)p1.y, (double)p1.z) <= r2;
                 }
@@ -1037,7 +1047,7 @@ __global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<f
                 bool in = valid && d2f < r2_lo;
                 const bool band = valid && !in && d2f <= r2_hi;
                 if (__any_sync(0xffffffffu, band))
-                    if (band) in = sq_euclid((double)q.x, (double)q.y, (double)q.z, (double)pp.x, (double)pp.y,
+                    if (band) in = sq_euclid(f2d_here(q.x), f2d_here(q.y), f2d_here(q.z), (double)pp.x, (double)pp.y,
                                              (double)pp.z) <= r2;
                 if (in) {
                     uint32_t m = __float_as_uint(pp.w);
@@ -1066,7 +1076,7 @@ __global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<f
             }
         }
         if (lane == 0) {
-            if (mode == 0) {
+            if constexpr (!PERQ) {
                 // FP32 only here: an FP64 instruction costs a warp-wide slot of
                 // the narrow FP64 pipe even with one active lane
                 float *px = out.gathered + 3 * (size_t)h.pixel;

@@ -45,9 +45,11 @@ void launch_eye_level_f(const SceneView<float> &sc, const DCamera<float> &cam, u
                         bool classic = false);
 // per-query radii (q_r2) always take queries from the counter; otherwise dyn
 // chooses it (maps larger than L2)
+// q_r2 null: the render (pass radius, FP32 sums into out.gathered);
+// otherwise the estimate entry point (per-query radii, FP64 radiance into out.out_rgb)
 void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
-                     const uint32_t *start, double pw, const double *q_r2, int pfilter, int mode, GatherOutF out,
-                     int grid, cudaStream_t s);
+                     const uint32_t *start, double pw, const double *q_r2, int pfilter, GatherOutF out, int grid,
+                     cudaStream_t s);
 void launch_within_f(const float *q, long long nq, const double *q_r2, const PassState *st, const float4 *smap,
                      const uint32_t *start, const int32_t *sidx, unsigned long long *counts,
                      const unsigned long long *offsets, int32_t *idx_out, int grid, cudaStream_t s);
