@@ -49,12 +49,16 @@ __device__ __forceinline__ void slab(T o, T inv, float lo, float hi, T &t0, T &t
     t0 = a < b ? a : b;
     t1 = a < b ? b : a;
 }
-__device__ __forceinline__ void slab(float o, float inv, float lo, float hi, float &t0, float &t1) {
-    const float a = (lo - o) * inv, b = (hi - o) * inv;   // finite: inv is clamped by safe_inv
+// FP32: o is passed as o * inv, so each bound is one fused multiply-add
+// (lo * inv - o * inv); the few-ulp difference from (lo - o) * inv near the
+// origin is far inside the boxes' 2^-17 outward padding.
+__device__ __forceinline__ void slab(float oinv, float inv, float lo, float hi, float &t0, float &t1) {
+    const float a = __fmaf_rn(lo, inv, -oinv), b = __fmaf_rn(hi, inv, -oinv);   // finite: inv clamped by safe_inv
     t0 = fminf(a, b);
     t1 = fmaxf(a, b);
 }
 
+// o: the ray origin (FP64), or origin * inv (FP32, see slab)
 template <typename T>
 __device__ __forceinline__ bool box_hit(V3<T> o, V3<T> inv, float lx, float hx, float ly, float hy, float lz, float hz,
                                         T tmax, T &tnear) {
@@ -94,6 +98,7 @@ template <typename T, typename Test, typename Best>
 __device__ __forceinline__ void bvh_walk(const BvhNode *nodes, const int32_t *order, bool runs, int root,
                                          int max_steps, V3<T> o, V3<T> dir, Test &&test, Best &&best) {
     const V3<T> inv = mk3(safe_inv(dir.x), safe_inv(dir.y), safe_inv(dir.z));
+    if constexpr (sizeof(T) == 4) o = mk3(o.x * inv.x, o.y * inv.y, o.z * inv.z);   // the slabs' form
     int stack[BVH_STACK];
     int sp = 0;
     int node = root;
