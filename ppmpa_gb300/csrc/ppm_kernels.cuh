@@ -662,7 +662,10 @@ __device__ __forceinline__ RowSet make_rows(const GridParams &g, const uint32_t 
     rs.len = 0;
     int x0, x1;
     if (row < nrows) {
-        int zi = row / ny;
+        // row / ny without an integer division: (row + 1/2) / ny is at least
+        // 1/(2 ny) >= 1/34 from an integer (ny = 2 ext + 1 <= 17) and, with
+        // row < 2^10, __fdividef's error is below 2^-10, so truncation is exact
+        int zi = __float2int_rz(__fdividef((float)row + 0.5f, (float)ny));
         int yy = lo[1] + (row - zi * ny), zz = lo[2] + zi;
         if (RowCull<T>::range(g, q, r2, yy, zz, lo[0], hi[0], x0, x1)) {
             int base = (zz * g.dim[1] + yy) * g.dim[0];
@@ -922,6 +925,20 @@ __device__ __forceinline__ float filter_wt_f(int pfilter, float d, float r2) {
     return 1.0f;
 }
 
+// a hit point (40 B; its arrays start 256-byte aligned, so every element is
+// 8-byte aligned) as five 8-byte loads
+static_assert(sizeof(HitPoint<float>) == 40, "five float2 per hit point");
+__device__ __forceinline__ HitPoint<float> load_hit(const HitPoint<float> *p) {
+    const float2 *v = reinterpret_cast<const float2 *>(p);
+    const float2 a = v[0], b = v[1], c = v[2], d = v[3], e = v[4];
+    HitPoint<float> h;
+    h.pos[0] = a.x; h.pos[1] = a.y; h.pos[2] = b.x;
+    h.nrm[0] = b.y; h.nrm[1] = c.x; h.nrm[2] = c.y;
+    h.w[0] = d.x; h.w[1] = d.y; h.w[2] = e.x;
+    h.pixel = __float_as_int(e.y);
+    return h;
+}
+
 struct GatherOutF {
     float *gathered;     // render: per-pass gathered flux W * sum (normalised later in FP64)
     double *out_rgb;     // estimate entry: per-query radiance
@@ -958,7 +975,7 @@ __global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<f
             qi = c;
             qend = c + CHUNK < nq ? c + CHUNK : nq;
         }
-        const HitPoint<float> h = hits[qi];
+        const HitPoint<float> h = load_hit(hits + qi);
         double r2;
         float r2_lo, r2_hi, r2f;
         int ext = g.ext, extx = g.extx;
