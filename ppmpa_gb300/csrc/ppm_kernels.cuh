@@ -127,15 +127,20 @@ __device__ __forceinline__ uint32_t oct_pack(float x, float y, float z, int wl) 
 // fold maps (px, py) to ((1 - |py|) sign px, (1 - |px|) sign py), written here
 // as px - copysign(-z, px) (equal in exact arithmetic, no branch).  The
 // normalisation is applied to the dot product.
-__device__ __forceinline__ float oct_dot(uint32_t m, V3<float> n) {
+__device__ __forceinline__ V3<float> oct_raw(uint32_t m, float &inv_len) {
     float px = (float)(m & 32767u) * (2.0f / 32767.0f) - 1.0f;
     float py = (float)((m >> 15) & 32767u) * (2.0f / 32767.0f) - 1.0f;
     const float pz = 1.0f - fabsf(px) - fabsf(py);
     const float t = fmaxf(-pz, 0.0f);
     px -= copysignf(t, px);
     py -= copysignf(t, py);
-    const float len2 = __fmaf_rn(pz, pz, __fmaf_rn(py, py, px * px));
-    return (n.x * px + n.y * py + n.z * pz) * rsqrtf(len2);
+    inv_len = rsqrtf(__fmaf_rn(pz, pz, __fmaf_rn(py, py, px * px)));
+    return mk3(px, py, pz);
+}
+__device__ __forceinline__ float oct_dot(uint32_t m, V3<float> n) {
+    float inv;
+    const V3<float> p = oct_raw(m, inv);
+    return (n.x * p.x + n.y * p.y + n.z * p.z) * inv;
 }
 
 // unsorted photon record of the FP64 path (also the parity download format)
@@ -903,6 +908,12 @@ __device__ __forceinline__ double f2d_here(float x) {
     return d;
 }
 
+// the kdtree crate's f64 predicate for a candidate in the FP32 rounding band
+__device__ __forceinline__ void in_recheck(bool &in, double qx, double qy, double qz, double px, double py, double pz,
+                                           double r2) {
+    in = sq_euclid(qx, qy, qz, px, py, pz) <= r2;
+}
+
 __device__ __forceinline__ bool in_radius_f32(float qx, float qy, float qz, float4 pp, float r2_lo, float r2_hi,
                                               double r2, float &d2f) {
     float dx = qx - pp.x, dy = qy - pp.y, dz = qz - pp.z;
@@ -946,6 +957,127 @@ struct GatherOutF {
 };
 
 #if defined(PPM_BUILD_F32)
+// Two hit points of the render gather in one warp.  Consecutive hit points
+// are mostly neighbouring pixels, a few thousandths apart against radii of
+// a few hundredths, so they usually share a cell: then the warp walks the
+// union of their rows once and tests every photon against both, sharing
+// the photon's load, its index arithmetic and its direction decode, and
+// the per-query row set-up.  Returns false (nothing done) when the two are
+// in different cells.  Membership, weights and sums are those of the
+// one-query walk.
+template <bool COUNT>
+__device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, const HitPoint<float> *hp,
+                                            const uint32_t *start, const float4 *smap, int pfilter,
+                                            const GatherOutF &out) {
+    const HitPoint<float> ha = load_hit(hp), hb = load_hit(hp + 1);
+    const V3<float> qa = ld3(ha.pos), qb = ld3(hb.pos);
+    int c[3], lo[3], hi[3];
+    query_cells(g, qa, g.ext, g.extx, c, lo, hi);
+    if (CellMath<float>::coord(g, qb.x, 0) != c[0] || CellMath<float>::coord(g, qb.y, 1) != c[1] ||
+        CellMath<float>::coord(g, qb.z, 2) != c[2])
+        return false;
+    const V3<float> na = ld3(ha.nrm), nb = ld3(hb.nrm);
+    const float r2f = g.r2f, r2_lo = g.r2_lo, r2_hi = g.r2_hi;
+    const unsigned lane = lane_id();
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, b0 = 0.f, b1 = 0.f, b2 = 0.f;
+    unsigned long long c_slots = 0, c_valid = 0, c_hits = 0;
+    const int ny = hi[1] - lo[1] + 1, nrows = ny * (hi[2] - lo[2] + 1);
+    for (int row0 = 0; row0 < nrows; row0 += 32) {
+        // lane's row: the union of the two queries' chord ranges
+        uint32_t rbeg = 0, rlen = 0;
+        const int row = row0 + (int)lane;
+        if (row < nrows) {
+            const int zi = __float2int_rz(__fdividef((float)row + 0.5f, (float)ny));   // as make_rows
+            const int yy = lo[1] + (row - zi * ny), zz = lo[2] + zi;
+            int xa0, xa1, xb0, xb1;
+            const bool ra = RowCull<float>::range(g, qa, r2f, yy, zz, lo[0], hi[0], xa0, xa1);
+            const bool rb = RowCull<float>::range(g, qb, r2f, yy, zz, lo[0], hi[0], xb0, xb1);
+            if (ra || rb) {
+                const int x0 = ra ? (rb ? min(xa0, xb0) : xa0) : xb0;
+                const int x1 = ra ? (rb ? max(xa1, xb1) : xa1) : xb1;
+                const int base = (zz * g.dim[1] + yy) * g.dim[0];
+                rbeg = start[3 * (base + x0)];
+                rlen = start[3 * (base + x1 + 1)] - rbeg;
+            }
+        }
+        unsigned m = __ballot_sync(0xffffffffu, rlen > 0);
+        while (m) {
+            const int r = __ffs(m) - 1;
+            m &= m - 1;
+            const uint32_t b = __shfl_sync(0xffffffffu, rbeg, r);
+            const uint32_t n = __shfl_sync(0xffffffffu, rlen, r);
+            for (uint32_t base = 0; base < n; base += 32) {
+                const uint32_t o = base + lane;
+                const bool v = o < n;
+                const float4 p = __ldg(&smap[v ? b + o : b]);
+                float dx = qa.x - p.x, dy = qa.y - p.y, dz = qa.z - p.z;
+                const float da = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                dx = qb.x - p.x;
+                dy = qb.y - p.y;
+                dz = qb.z - p.z;
+                const float db = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                bool ia = v && da < r2_lo, ib = v && db < r2_lo;
+                const bool ba = v && !ia && da <= r2_hi, bb = v && !ib && db <= r2_hi;
+                if (__any_sync(0xffffffffu, ba || bb)) {   // FP64 recheck within rounding of r
+                    const double px = p.x, py = p.y, pz = p.z;
+                    if (ba) in_recheck(ia, f2d_here(qa.x), f2d_here(qa.y), f2d_here(qa.z), px, py, pz, r2);
+                    if (bb) in_recheck(ib, f2d_here(qb.x), f2d_here(qb.y), f2d_here(qb.z), px, py, pz, r2);
+                }
+                if (COUNT) {
+                    c_slots += 1;
+                    c_valid += 2 * (int)v;
+                    c_hits += (int)ia + (int)ib;
+                }
+                if (ia || ib) {
+                    const uint32_t mm = __float_as_uint(p.w);
+                    float inv;
+                    const V3<float> d = oct_raw(mm, inv);
+                    const float ca = (na.x * d.x + na.y * d.y + na.z * d.z) * inv;
+                    const float cb = (nb.x * d.x + nb.y * d.y + nb.z * d.z) * inv;
+                    float wa = (ia && ca < 0.0f) ? -ca : 0.0f, wb = (ib && cb < 0.0f) ? -cb : 0.0f;
+                    if (pfilter != PF_NONE) {
+                        wa *= filter_wt_f(pfilter, da, r2f);
+                        wb *= filter_wt_f(pfilter, db, r2f);
+                    }
+                    const uint32_t l = mm >> 30;
+                    a0 += l == 0u ? wa : 0.0f;
+                    a1 += l == 1u ? wa : 0.0f;
+                    a2 += l >= 2u ? wa : 0.0f;
+                    b0 += l == 0u ? wb : 0.0f;
+                    b1 += l == 1u ? wb : 0.0f;
+                    b2 += l >= 2u ? wb : 0.0f;
+                }
+            }
+        }
+    }
+    a0 = warp_sum(a0); a1 = warp_sum(a1); a2 = warp_sum(a2);
+    b0 = warp_sum(b0); b1 = warp_sum(b1); b2 = warp_sum(b2);
+    if (COUNT) {
+        for (int o = 16; o > 0; o >>= 1) {
+            c_slots += __shfl_xor_sync(0xffffffffu, c_slots, o);
+            c_valid += __shfl_xor_sync(0xffffffffu, c_valid, o);
+            c_hits += __shfl_xor_sync(0xffffffffu, c_hits, o);
+        }
+        if (lane == 0) {
+            atomicAdd(out.count + 0, c_valid);
+            atomicAdd(out.count + 1, c_hits);
+            atomicAdd(out.count + 2, c_slots);
+        }
+    }
+    if (lane == 0) {
+        float *pa = out.gathered + 3 * (size_t)ha.pixel, *pb = out.gathered + 3 * (size_t)hb.pixel;
+        atomicAdd(pa, ha.w[0] * a0);
+        atomicAdd(pa + 1, ha.w[1] * a1);
+        atomicAdd(pa + 2, ha.w[2] * a2);
+        atomicAdd(pb, hb.w[0] * b0);
+        atomicAdd(pb + 1, hb.w[1] * b1);
+        atomicAdd(pb + 2, hb.w[2] * b2);
+    }
+    return true;
+}
+#endif
+
+#if defined(PPM_BUILD_F32)
 // PERQ: per-query radii (the estimate entry point); otherwise the pass radius.
 //
 // Warps take their queries from a counter, a few at a time, so the queries
@@ -974,6 +1106,12 @@ __global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<f
             if (c >= nq) break;
             qi = c;
             qend = c + CHUNK < nq ? c + CHUNK : nq;
+        }
+        if constexpr (!PERQ) {
+            if (qend - qi == 2 && gather_pair<COUNT>(g, st->r2, hits + qi, start, smap, pfilter, out)) {
+                qi += 2;
+                continue;
+            }
         }
         const HitPoint<float> h = load_hit(hits + qi);
         double r2;
