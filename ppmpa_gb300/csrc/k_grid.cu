@@ -47,22 +47,26 @@ __global__ void k_grid_setup(PassState *st, double r2_override) {
     if (empty) for (int a = 0; a < 3; a++) { lo[a] = 0.0; hi[a] = 0.0; }
     double k = st->cell_factor > 0.0 ? st->cell_factor : 1.0;
     const int sx = st->cell_sx >= 1 ? st->cell_sx : 1;
-    double c = r / k * (1.0 + 1.0 / 128.0);
+    // One thread, and FP64 is a narrow, long-latency pipe on this GPU: two
+    // divisions, the rest multiplications by the reciprocal (the same
+    // product form cell_of uses, so the last cell holds hi exactly).
+    double c = r * ((1.0 + 1.0 / 128.0) / k);
     if (!(c > 0.0 && c < 1e30)) c = 1.0;
+    double inv = 1.0 / c;
     long long dim[3] = {1, 1, 1};
     for (int it = 0; it < 400; it++) {
         bool ok = true;
         long long tot = 1;
         for (int a = 0; a < 3; a++) {
-            const double ca = a == 0 ? c / sx : c;
-            double f = floor((hi[a] - lo[a]) / ca);
+            double f = floor((hi[a] - lo[a]) * (a == 0 ? inv * sx : inv));
             if (!(f >= 0.0 && f < 8192.0)) { ok = false; dim[a] = 8193; }
             else dim[a] = (long long)f + 1;
             tot *= dim[a];
         }
         if (ok && 3 * tot <= st->cell_cap) break;
         c *= 1.25;
-        if (it == 399) { dim[0] = dim[1] = dim[2] = 1; c = 1e30; }
+        inv = 1.0 / c;
+        if (it == 399) { dim[0] = dim[1] = dim[2] = 1; c = 1e30; inv = 1e-30; }
     }
     GridParams g;
     for (int a = 0; a < 3; a++) {
@@ -70,16 +74,16 @@ __global__ void k_grid_setup(PassState *st, double r2_override) {
         g.orgf[a] = (float)lo[a];
         g.dim[a] = (int32_t)dim[a];
     }
-    const double cx = c / sx;
+    const double invx = inv * sx;
     g.cell = c;
-    g.inv = 1.0 / c;
-    g.invf = (float)(1.0 / c);
-    g.invx = 1.0 / cx;
-    g.invxf = (float)(1.0 / cx);
-    double ef = ceil(r / c + 3e-3);
+    g.inv = inv;
+    g.invf = (float)inv;
+    g.invx = invx;
+    g.invxf = (float)invx;
+    double ef = ceil(r * inv + 3e-3);
     int ext = ef >= 1.0 && ef <= 8.0 ? (int)ef : (ef > 8.0 ? 8 : 1);
     g.ext = ext < 1 ? 1 : (ext > 8 ? 8 : ext);
-    double efx = ceil(r / cx + 3e-3);
+    double efx = ceil(r * invx + 3e-3);
     g.extx = efx >= 1.0 && efx <= 64.0 ? (int)efx : (efx > 64.0 ? 64 : 1);
     g.ncell = dim[0] * dim[1] * dim[2];
     g.nkeys = 3 * g.ncell;
@@ -90,8 +94,6 @@ __global__ void k_grid_setup(PassState *st, double r2_override) {
     st->grid = g;
 }
 
-// exclusive scan of count[0, ncell) into start[0, ncell], zeroing count
-// (reduce -> scan of tile sums -> downsweep; no inter-block waiting)
 // Exclusive scan of the per-key counts into start[] (the photon map's cell
 // starts) in tiles of SCAN_TILE keys: per-tile sums, a one-block scan of the
 // tile sums, then each tile scanned from its offset.  The tile kernels loop

@@ -167,6 +167,10 @@ template <> struct PhotonBuf<double> {
     }
     __device__ __forceinline__ V3<double> raw_pos(unsigned long long i) const { return ld3(raw[i].pos); }
     __device__ __forceinline__ int raw_wl(unsigned long long i) const { return raw[i].wl; }
+    __device__ __forceinline__ V3<double> raw_pos_wl(unsigned long long i, int &wl) const {
+        wl = raw[i].wl;
+        return ld3(raw[i].pos);
+    }
 };
 template <> struct PhotonBuf<float> {
     float4 *raw;           // unsorted: x, y, z, oct(dir) | wl
@@ -180,6 +184,11 @@ template <> struct PhotonBuf<float> {
         return mk3(r.x, r.y, r.z);
     }
     __device__ __forceinline__ int raw_wl(unsigned long long i) const { return (int)(__float_as_uint(raw[i].w) >> 30); }
+    __device__ __forceinline__ V3<float> raw_pos_wl(unsigned long long i, int &wl) const {
+        const float4 r = raw[i];
+        wl = (int)(__float_as_uint(r.w) >> 30);
+        return mk3(r.x, r.y, r.z);
+    }
 };
 
 template <typename T>
@@ -349,7 +358,9 @@ __global__ void __launch_bounds__(256) k_cell_hist(PhotonBuf<T> buf, PassState *
     const GridParams g = st->grid;
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
-        uint32_t c = 3u * cell_of(g, buf.raw_pos(i)) + (uint32_t)buf.raw_wl(i);
+        int wl;
+        const V3<T> pos = buf.raw_pos_wl(i, wl);
+        uint32_t c = 3u * cell_of(g, pos) + (uint32_t)wl;
         uint32_t r = atomicAdd(&count[c], 1u);
         keyrank[i] = make_uint2(c, r);
     }
