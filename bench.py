@@ -206,7 +206,7 @@ def run_reference(args, w):
             f"one full pass per step ({w['nphoton']} photons, {w['reso']}x{w['reso']} eye rays)")
     out = {
         "impl": "reference", "metric": METRIC, "value": value,
-        "unit": "Mphotons/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "unit": "Mphotons/s", "n_gpus": args.gpus, "host_only": True, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene, seeded photon streams)",
         "config": {"workload": args.workload, **w},
@@ -566,7 +566,8 @@ def run_sweep_reference(args, kind):
     print(json.dumps({
         "impl": "reference", "metric": f"gather sweep estimates/s ({len(pos)} FP32 photons, {len(q)} queries, "
                                        f"r log-uniform 1e-3..2e-2)",
-        "value": value, "unit": "Mqueries/s", "n_gpus": 0, "steps": args.steps, "warmup": max(1, args.warmup),
+        "value": value, "unit": "Mqueries/s", "n_gpus": args.gpus, "host_only": True, "steps": args.steps,
+        "warmup": max(1, args.warmup),
         "ms_per_step": total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded photons and queries)",
         "config": {"workload": args.workload, "distribution": kind, "photons": len(pos), "queries": len(q)},
