@@ -166,7 +166,6 @@ template <> struct PhotonBuf<double> {
         raw[i] = r;
     }
     __device__ __forceinline__ V3<double> raw_pos(unsigned long long i) const { return ld3(raw[i].pos); }
-    __device__ __forceinline__ int raw_wl(unsigned long long i) const { return raw[i].wl; }
     __device__ __forceinline__ V3<double> raw_pos_wl(unsigned long long i, int &wl) const {
         wl = raw[i].wl;
         return ld3(raw[i].pos);
@@ -183,7 +182,6 @@ template <> struct PhotonBuf<float> {
         float4 r = raw[i];
         return mk3(r.x, r.y, r.z);
     }
-    __device__ __forceinline__ int raw_wl(unsigned long long i) const { return (int)(__float_as_uint(raw[i].w) >> 30); }
     __device__ __forceinline__ V3<float> raw_pos_wl(unsigned long long i, int &wl) const {
         const float4 r = raw[i];
         wl = (int)(__float_as_uint(r.w) >> 30);
@@ -886,27 +884,11 @@ struct Kahan {
     }
 };
 
-// pairwise (tree) sum of the lanes' compensated partial sums
+// pairwise (tree) sum of the lanes' partial sums
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
-}
-
-// compensated pairwise combination (two-sum) across the warp
-__device__ __forceinline__ float warp_sum_comp(Kahan k) {
-    float s = k.s, c = -k.c;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        float so = __shfl_xor_sync(0xffffffffu, s, o);
-        float co = __shfl_xor_sync(0xffffffffu, c, o);
-        float t = s + so;
-        float bp = t - s;
-        float err = (s - (t - bp)) + (so - bp);
-        s = t;
-        c = c + co + err;
-    }
-    return s + c;
 }
 
 // float -> double that the compiler cannot hoist out of a branch (an inline
