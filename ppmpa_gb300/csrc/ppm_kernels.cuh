@@ -962,14 +962,19 @@ template <bool COUNT>
 __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, const HitPoint<float> *hp,
                                             const uint32_t *start, const float4 *smap, int pfilter,
                                             const GatherOutF &out) {
-    const HitPoint<float> ha = load_hit(hp), hb = load_hit(hp + 1);
-    const V3<float> qa = ld3(ha.pos), qb = ld3(hb.pos);
+    V3<float> qa, qb, na, nb;
+    {
+        const HitPoint<float> ha = load_hit(hp), hb = load_hit(hp + 1);
+        qa = ld3(ha.pos);
+        qb = ld3(hb.pos);
+        na = ld3(ha.nrm);
+        nb = ld3(hb.nrm);
+    }
     int c[3], lo[3], hi[3];
     query_cells(g, qa, g.ext, g.extx, c, lo, hi);
     if (CellMath<float>::coord(g, qb.x, 0) != c[0] || CellMath<float>::coord(g, qb.y, 1) != c[1] ||
         CellMath<float>::coord(g, qb.z, 2) != c[2])
         return false;
-    const V3<float> na = ld3(ha.nrm), nb = ld3(hb.nrm);
     const float r2f = g.r2f, r2_lo = g.r2_lo, r2_hi = g.r2_hi;
     const unsigned lane = lane_id();
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, b0 = 0.f, b1 = 0.f, b2 = 0.f;
@@ -1058,6 +1063,8 @@ __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, cons
         }
     }
     if (lane == 0) {
+        // weights and pixels re-read here (cached) rather than held through the walk
+        const HitPoint<float> ha = load_hit(hp), hb = load_hit(hp + 1);
         float *pa = out.gathered + 3 * (size_t)ha.pixel, *pb = out.gathered + 3 * (size_t)hb.pixel;
         atomicAdd(pa, ha.w[0] * a0);
         atomicAdd(pa + 1, ha.w[1] * a1);
