@@ -125,3 +125,32 @@ def test_batch_job_layout_matches_header(built_lib):
     assert C.sizeof(S.Job) == 120 and S.Job.cfg.offset == 48 and S.Job.image_out.offset == 112
     assert C.sizeof(S.RenderCfg) == 64
     assert C.sizeof(S.Stats) == 360 and S.Stats.photon_rays.offset == 344
+
+
+def test_every_context_entry_point_rejects_a_null_context(built_lib):
+    """Each entry point whose first argument is the context returns
+    PPM_ERR_INVALID_ARG for a null context before touching any other
+    argument or a device (null pointers and zeros everywhere else)."""
+    from ppmpa_gb300 import _lib
+    lib = _lib.load()
+    skip = {"ppm_ctx_destroy",      # null is a no-op (PPM_OK)
+            "ppm_last_error",       # null reads the process-wide message
+            "ppm_ctx_stream"}       # returns a pointer, not a status
+    checked = 0
+    for name, (res, args) in _lib.SIGNATURES.items():
+        if name in skip or res is not C.c_int or not args or args[0] is not C.c_void_p:
+            continue
+        if not name.startswith("ppm_") or name.startswith("ppm_batch"):
+            continue
+        vals = []
+        for t in args[1:]:
+            if t in (C.c_double, C.c_float):
+                vals.append(0.0)
+            elif t in (C.c_int, C.c_int32, C.c_int64, C.c_uint32, C.c_uint64, C.c_size_t):
+                vals.append(0)
+            else:
+                vals.append(None)
+        assert getattr(lib, name)(None, *vals) == 1, name
+        checked += 1
+    assert checked >= 25
+    assert lib.ppm_batch_render(None, None, 0, None) == 1
