@@ -1,0 +1,177 @@
+"""Conservativeness of the FP32 photon-map grid, on the CPU: a float32
+restatement of the grid set-up (k_grid_setup), the cell coordinates
+(CellMath<float>), the query's cell ranges (query_cells) and the row
+culling (RowCull<float>::range) checks that the rows and x-ranges the
+gather walks hold every photon within the radius -- for single queries and
+for the union the paired walk takes over two queries of one cell -- with
+queries and photons placed on and around cell boundaries.  (The GPU may
+contract some of these products into FMAs; the margins the test exercises
+are the ones that absorb such rounding.)"""
+import numpy as np
+import pytest
+
+f32 = np.float32
+
+
+def grid(lo, hi, r2, k=1.0, sx=4, cell_cap=1 << 24):
+    r = np.sqrt(r2)
+    c = r * ((1.0 + 1.0 / 128.0) / k)
+    inv = 1.0 / c
+    while True:
+        dim = [int(np.floor((hi[a] - lo[a]) * (inv * sx if a == 0 else inv))) + 1 for a in range(3)]
+        if all(d <= 8192 for d in dim) and 3 * dim[0] * dim[1] * dim[2] <= cell_cap:
+            break
+        c *= 1.25
+        inv = 1.0 / c
+    invx = inv * sx
+    ext = int(min(max(np.ceil(r * inv + 3e-3), 1), 8))
+    extx = int(min(max(np.ceil(r * invx + 3e-3), 1), 64))
+    return dict(orgf=lo.astype(f32), invf=f32(inv), invxf=f32(invx), cellf=f32(c), dim=dim, ext=ext, extx=extx,
+                r2f=f32(r2))
+
+
+def coord(g, p, a):
+    f = np.floor((f32(p) - g["orgf"][a]) * (g["invxf"] if a == 0 else g["invf"]))
+    return int(min(max(f, 0.0), g["dim"][a] - 1))
+
+
+def row_range(g, q, r2f, yy, zz, lo_x, hi_x):
+    c = g["cellf"]
+    m = f32(4e-3) * c
+    ylo = g["orgf"][1] + f32(yy) * c
+    zlo = g["orgf"][2] + f32(zz) * c
+    dy = max(f32(0), max(ylo - q[1], q[1] - (ylo + c)) - m)
+    dz = max(f32(0), max(zlo - q[2], q[2] - (zlo + c)) - m)
+    rem = r2f * f32(1.00002) - dy * dy - dz * dz
+    if rem < 0:
+        return None
+    rx = np.sqrt(rem, dtype=f32) * f32(1.00001)
+    fx0 = np.floor((q[0] - rx - g["orgf"][0]) * g["invxf"] - f32(4e-3))
+    fx1 = np.floor((q[0] + rx - g["orgf"][0]) * g["invxf"] + f32(4e-3))
+    x0 = max(lo_x, int(max(fx0, -1.0)))
+    x1 = min(hi_x, int(min(fx1, float(g["dim"][0]))))
+    return (x0, x1) if x0 <= x1 else None
+
+
+def walked_cells(g, queries):
+    """Cells (x, y, z) the gather walks for one query or a same-cell pair."""
+    q0 = queries[0]
+    c = [coord(g, q0[a], a) for a in range(3)]
+    e = (g["extx"], g["ext"], g["ext"])
+    lo = [max(c[a] - e[a], 0) for a in range(3)]
+    hi = [min(c[a] + e[a], g["dim"][a] - 1) for a in range(3)]
+    cells = set()
+    for zz in range(lo[2], hi[2] + 1):
+        for yy in range(lo[1], hi[1] + 1):
+            rs = [row_range(g, q, g["r2f"], yy, zz, lo[0], hi[0]) for q in queries]
+            rs = [r for r in rs if r is not None]
+            if not rs:
+                continue
+            x0, x1 = min(r[0] for r in rs), max(r[1] for r in rs)
+            cells.update((x, yy, zz) for x in range(x0, x1 + 1))
+    return cells
+
+
+def shell(rng, q, r2, n):
+    """Photons just inside the sphere around q (distance r (1 - 2^-20)),
+    where a chord or slab bound that is too tight loses them first."""
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    p = (q.astype(np.float64) + d * np.sqrt(r2) * (1 - 2.0 ** -20)).astype(f32)
+    return p[in_radius(q, p, r2)]
+
+
+def in_radius(q, p, r2):
+    d = q.astype(np.float64) - p.astype(np.float64)
+    return ((0.0 + d[..., 0] * d[..., 0]) + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2] <= r2
+
+
+def _boundary_points(rng, g, n):
+    """Points on, and a few ulps either side of, cell faces."""
+    pts = []
+    for _ in range(n):
+        p = []
+        for a in range(3):
+            cw = 1.0 / float(g["invxf"] if a == 0 else g["invf"])
+            k = rng.integers(1, g["dim"][a])
+            v = f32(float(g["orgf"][a]) + k * cw)
+            v = np.nextafter(v, f32(np.inf if rng.random() < 0.5 else -np.inf), dtype=f32) \
+                if rng.random() < 0.7 else v
+            for _ in range(int(rng.integers(0, 3))):
+                v = np.nextafter(v, f32(np.inf), dtype=f32)
+            p.append(v)
+        pts.append(p)
+    return np.array(pts, f32)
+
+
+@pytest.mark.parametrize("k", [1.0, 2.0])
+def test_culled_rows_hold_every_photon_in_radius(k):
+    rng = np.random.default_rng(11)
+    lo, hi = np.array([-1.0, 0.0, 0.0]), np.array([1.0, 2.0, 2.0])
+    r2 = 0.037 ** 2
+    g = grid(lo, hi, r2, k=k)
+    photons = np.vstack([rng.uniform(lo, hi, (40000, 3)).astype(f32), _boundary_points(rng, g, 4000)])
+    queries = np.vstack([rng.uniform(lo + 0.1, hi - 0.1, (150, 3)).astype(f32), _boundary_points(rng, g, 150)])
+    pc = [tuple(coord(g, p[a], a) for a in range(3)) for p in photons]
+    for q in queries:
+        cells = walked_cells(g, [q])
+        hit = np.nonzero(in_radius(q, photons, r2))[0]
+        missing = [i for i in hit if pc[i] not in cells]
+        assert not missing, (q, photons[missing[:3]])
+        for p in shell(rng, q, r2, 3000):
+            assert tuple(coord(g, p[a], a) for a in range(3)) in cells, (q, p)
+
+
+def test_paired_walk_holds_both_queries_photons():
+    rng = np.random.default_rng(12)
+    lo, hi = np.array([-1.0, 0.0, 0.0]), np.array([1.0, 2.0, 2.0])
+    r2 = 0.031 ** 2
+    g = grid(lo, hi, r2)
+    photons = np.vstack([rng.uniform(lo, hi, (40000, 3)).astype(f32), _boundary_points(rng, g, 4000)])
+    pc = [tuple(coord(g, p[a], a) for a in range(3)) for p in photons]
+    pairs = 0
+    for _ in range(400):
+        a = rng.uniform(lo + 0.1, hi - 0.1).astype(f32)
+        b = (a + rng.normal(0, 0.004, 3)).astype(f32)          # a neighbouring pixel's hit point
+        if any(coord(g, a[i], i) != coord(g, b[i], i) for i in range(3)):
+            continue                                            # the pair walk needs one cell
+        pairs += 1
+        cells = walked_cells(g, [a, b])
+        for q in (a, b):
+            hit = np.nonzero(in_radius(q, photons, r2))[0]
+            assert all(pc[i] in cells for i in hit), q
+            for p in shell(rng, q, r2, 1000):
+                assert tuple(coord(g, p[i], i) for i in range(3)) in cells, (q, p)
+    assert pairs > 50
+
+
+def test_sphere_extremes_just_past_a_cell_face_are_walked():
+    """Queries placed so that the sphere's extreme point along an axis lies
+    a few ulps past a cell face, with a photon just inside the radius there:
+    the chord (x) or the row slab (y, z) must still reach that cell."""
+    rng = np.random.default_rng(13)
+    lo, hi = np.array([-1.0, 0.0, 0.0]), np.array([1.0, 2.0, 2.0])
+    for r in (0.0123, 0.037, 0.051):
+        r2 = r * r
+        g = grid(lo, hi, r2)
+        checked = 0
+        for _ in range(300):
+            a = int(rng.integers(0, 3))
+            sgn = 1.0 if rng.random() < 0.5 else -1.0
+            cw = 1.0 / float(g["invxf"] if a == 0 else g["invf"])
+            k = int(rng.integers(3, g["dim"][a] - 3))
+            face = float(g["orgf"][a]) + k * cw
+            q = rng.uniform(lo + 0.2, hi - 0.2)
+            # the extreme point sits delta past the face, on the far side from q
+            delta = float(rng.integers(1, 64)) * 2.0 ** -23 * max(1.0, abs(face))
+            q[a] = face - sgn * r + sgn * delta
+            q = q.astype(f32)
+            p = q.astype(np.float64).copy()
+            p[a] += sgn * r * (1 - 2.0 ** -18)
+            p = p.astype(f32)
+            if not in_radius(q, p[None, :], r2)[0]:
+                continue
+            cell = tuple(coord(g, p[i], i) for i in range(3))
+            assert cell in walked_cells(g, [q]), (r, a, sgn, q, p)
+            checked += 1
+        assert checked > 150
