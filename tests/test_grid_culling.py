@@ -175,3 +175,80 @@ def test_sphere_extremes_just_past_a_cell_face_are_walked():
             assert cell in walked_cells(g, [q]), (r, a, sgn, q, p)
             checked += 1
         assert checked > 150
+
+
+# ---- the FP64 (plain) path: the same grid in doubles, RowCull<double> and
+# CellMath<double>; its kernels are built without FMA contraction, so these
+# float64 expressions round as the device's do
+def grid64(lo, hi, r2, k=1.0, sx=4):
+    g = grid(lo, hi, r2, k, sx)
+    r = np.sqrt(r2)
+    c = r * ((1.0 + 1.0 / 128.0) / k)
+    inv = 1.0 / c
+    while int(np.floor((hi[0] - lo[0]) * inv * sx)) + 1 != g["dim"][0]:   # follow the same growth
+        c *= 1.25
+        inv = 1.0 / c
+    return dict(org=lo.astype(np.float64), inv=inv, invx=inv * sx, cell=c, dim=g["dim"], ext=g["ext"],
+                extx=g["extx"])
+
+
+def coord64(g, p, a):
+    f = np.floor((p - g["org"][a]) * (g["invx"] if a == 0 else g["inv"]))
+    return int(min(max(f, 0.0), g["dim"][a] - 1))
+
+
+def row_range64(g, q, r2, yy, zz, lo_x, hi_x):
+    c = g["cell"]
+    m = 1e-6 * c
+    ylo = g["org"][1] + yy * c
+    zlo = g["org"][2] + zz * c
+    dy = max(0.0, max(ylo - q[1], q[1] - (ylo + c)) - m)
+    dz = max(0.0, max(zlo - q[2], q[2] - (zlo + c)) - m)
+    rem = r2 * (1.0 + 1e-12) - dy * dy - dz * dz
+    if rem < 0.0:
+        return None
+    rx = np.sqrt(rem) * (1.0 + 1e-12)
+    fx0 = np.floor((q[0] - rx - g["org"][0]) * g["invx"] - 1e-6)
+    fx1 = np.floor((q[0] + rx - g["org"][0]) * g["invx"] + 1e-6)
+    x0 = max(lo_x, int(max(fx0, -1.0)))
+    x1 = min(hi_x, int(min(fx1, float(g["dim"][0]))))
+    return (x0, x1) if x0 <= x1 else None
+
+
+def walked_cells64(g, q, r2):
+    c = [coord64(g, q[a], a) for a in range(3)]
+    e = (g["extx"], g["ext"], g["ext"])
+    lo = [max(c[a] - e[a], 0) for a in range(3)]
+    hi = [min(c[a] + e[a], g["dim"][a] - 1) for a in range(3)]
+    cells = set()
+    for zz in range(lo[2], hi[2] + 1):
+        for yy in range(lo[1], hi[1] + 1):
+            rr = row_range64(g, q, r2, yy, zz, lo[0], hi[0])
+            if rr is not None:
+                cells.update((x, yy, zz) for x in range(rr[0], rr[1] + 1))
+    return cells
+
+
+def test_fp64_culling_holds_sphere_extremes_just_past_a_cell_face():
+    rng = np.random.default_rng(14)
+    lo, hi = np.array([-1.0, 0.0, 0.0]), np.array([1.0, 2.0, 2.0])
+    for r in (0.0123, 0.037, 0.051):
+        r2 = r * r
+        g = grid64(lo, hi, r2)
+        checked = 0
+        for _ in range(300):
+            a = int(rng.integers(0, 3))
+            sgn = 1.0 if rng.random() < 0.5 else -1.0
+            cw = 1.0 / (g["invx"] if a == 0 else g["inv"])
+            k = int(rng.integers(3, g["dim"][a] - 3))
+            face = g["org"][a] + k * cw
+            q = rng.uniform(lo + 0.2, hi - 0.2)
+            q[a] = face - sgn * r + sgn * float(rng.integers(1, 64)) * 2.0 ** -52 * max(1.0, abs(face))
+            p = q.copy()
+            p[a] += sgn * r * (1 - 2.0 ** -40)
+            if not in_radius(q, p[None, :], r2)[0]:
+                continue
+            cell = tuple(coord64(g, p[i], i) for i in range(3))
+            assert cell in walked_cells64(g, q, r2), (r, a, sgn, q, p)
+            checked += 1
+        assert checked > 150
