@@ -135,7 +135,12 @@ enum { PPM_RENDER_TUNE_CELLS = 1,
  * (src/tracer.rs:221-259, the `rtc` binary) instead of photon mapping: each
  * pass traces the eye rays only (direct light + ambient, mirror and
  * refraction children); passes average anti-aliased images. */
-       PPM_RENDER_CLASSIC = 2 };
+       PPM_RENDER_CLASSIC = 2,
+/* PPM_RENDER_ROW_WALK: in the mixed render, gather with one warp per hit
+ * point (or per two in one cell) walking its own cell rows, in place of the
+ * default tile gather (one warp per 32 hit points, one lane each, sharing
+ * one walk of their photons).  Same sets and sums; kept to compare the two. */
+       PPM_RENDER_ROW_WALK = 4 };
 
 /* Per-pass statistics of the last rendered pass and accumulated timings. */
 typedef struct ppm_stats {
@@ -256,10 +261,12 @@ int ppm_estimate(ppm_ctx *ctx, const double *pos, const double *nrm, int64_t nq,
  * holds nearly all of the device, or one that cannot take the device-wide
  * wait a cudaFree implies while its other streams run.  The queries and
  * results are staged in one fixed device array (about 5 MB) per device,
- * shared by every context and call in the process.  The first call on a
- * device looks up that array's address; make it before any stream capture
- * begins.  Calls whose GPU work overlaps (two host threads, or two contexts
- * on the same device) race on the array: serialise them. */
+ * shared by every context and call in the process and held until the
+ * process exits.  ppm_ctx_create places that array on its device and looks
+ * up its address, so the entry point itself loads and allocates nothing;
+ * a context created after a device reset looks it up again.  Calls whose
+ * GPU work overlaps (two host threads, or two contexts on the same device)
+ * race on the array: serialise them. */
 #define PPM_ESTIMATE_NOALLOC_MAX_QUERIES 32768
 int ppm_estimate_noalloc(ppm_ctx *ctx, const double *pos, const double *nrm, int64_t nq,
                          int32_t pfilter, double *rgb);
@@ -312,6 +319,36 @@ int ppm_render_stats(ppm_ctx *ctx, ppm_stats *out);
  * eagerly, not as a graph); on = 2: also count gather candidates and hits. */
 int ppm_set_stage_timing(ppm_ctx *ctx, int32_t on);
 const char *ppm_stage_name(int32_t stage);
+
+/* Parity export of the mixed-precision render's gather.  No reference
+ * counterpart: it exposes, hit point by hit point, what the render's own
+ * gather computes, so that it can be checked against estimate_radiance
+ * (src/tracer.rs:179-216).  The call runs one more pass of the render begun
+ * by ppm_render_begin (precision PPM_PRECISION_MIXED, photon mapping),
+ * eagerly and counted like ppm_render_step(ctx, 1), in which the gather also
+ * records per hit point: the FP32 flux sums per wavelength,
+ *   sum over the photons p in radius of max(0, -n . dir_p) * wt(d2, r2),
+ * before the hit point's weight and the pass's pw / (pi r2) scale them; the
+ * number of photons in radius; and a checksum of that set, the sum (mod 2^64)
+ * over their slots s in the pass's sorted photon map of SplitMix64's output
+ * function of (s + 1) * 0x9e3779b97f4a7c15.  It copies out that pass's sorted
+ * photon map (x, y, z, then the direction word: 15 + 15-bit octahedral
+ * direction, wavelength in bits 30-31), its hit points and its FP32
+ * gathered-flux image.  With photons == NULL it sets n_photons and n_hits to
+ * the most one pass can produce and runs nothing. */
+typedef struct ppm_gather_export {
+    int64_t photon_cap, hit_cap;    /* in: entries the arrays below hold */
+    int64_t n_photons, n_hits;      /* out */
+    double radius2, photon_power;   /* out: the pass's r^2 and photon power pw */
+    int32_t pass, pfilter;          /* out: the pass index and the camera's filter */
+    float *photons;                 /* n_photons x 4: x, y, z, direction word (float bits) */
+    float *hits;                    /* n_hits x 10: position, normal, weight, pixel (int32 bits) */
+    float *sums;                    /* n_hits x 3 */
+    uint32_t *counts;               /* n_hits */
+    uint64_t *checksums;            /* n_hits */
+    float *gathered;                /* yreso x xreso x 3: per pixel, sum of weight x sums */
+} ppm_gather_export;
+int ppm_render_gather_export(ppm_ctx *ctx, ppm_gather_export *ex);
 
 /* ---- output ------------------------------------------------------------------ */
 /* Camera::radiance_to_rgb (src/camera.rs:92-100) for n values:

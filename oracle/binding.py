@@ -66,6 +66,8 @@ def lib() -> C.CDLL:
             "orc_estimate_radii": (None, [_dp, _dp, _u8p, C.c_int64, _dp, _dp, C.c_int64, _dp, C.c_double,
                                           C.c_int, _dp]),
             "orc_last_query_seconds": (C.c_double, []),
+            "orc_gather_sums": (None, [_dp, _dp, _u8p, C.c_int64, _dp, _dp, C.c_int64, C.c_double, C.c_int,
+                                       _i64p, C.POINTER(C.c_uint64), _dp]),
             "orc_trace_photons": (C.c_int64, [C.POINTER(_Scene), C.c_int64, C.c_int, C.c_uint64, C.c_uint32,
                                               _dp, _dp, _u8p, _i32p, _i8p, C.c_int64, _dp, _i64p]),
             "orc_classic_pass": (None, [C.POINTER(_Scene), C.c_void_p, C.c_uint64, C.c_uint32, _dp]),
@@ -164,6 +166,23 @@ class Oracle:
                                   _p(qpos, C.c_double), _p(qnrm, C.c_double), qpos.shape[0], _p(r2, C.c_double),
                                   float(pw), int(pfilter), _p(rgb, C.c_double))
         return rgb
+
+    def gather_sums(self, ppos, pdir, pwl, qpos, qnrm, r2, pfilter=0):
+        """Per query: photons within r2, their set checksum and the flux sums of
+        estimate_radiance before pw and 1/(pi r2) (orc_gather_sums)."""
+        ppos = np.ascontiguousarray(ppos, np.float64).reshape(-1, 3)
+        pdir = np.ascontiguousarray(pdir, np.float64).reshape(-1, 3)
+        pwl = np.ascontiguousarray(pwl, np.uint8)
+        qpos = np.ascontiguousarray(qpos, np.float64).reshape(-1, 3)
+        qnrm = np.ascontiguousarray(qnrm, np.float64).reshape(-1, 3)
+        nq = qpos.shape[0]
+        count = np.zeros(nq, np.int64)
+        check = np.zeros(nq, np.uint64)
+        sums = np.zeros((nq, 3))
+        self.L.orc_gather_sums(_p(ppos, C.c_double), _p(pdir, C.c_double), _p(pwl, C.c_uint8), ppos.shape[0],
+                               _p(qpos, C.c_double), _p(qnrm, C.c_double), nq, float(r2), int(pfilter),
+                               _p(count, C.c_int64), _p(check, C.c_uint64), _p(sums, C.c_double))
+        return count, check, sums
 
     def estimate(self, ppos, pdir, pwl, qpos, qnrm, r2, pw, pfilter=0):
         ppos = np.ascontiguousarray(ppos, np.float64).reshape(-1, 3)

@@ -1041,6 +1041,58 @@ void orc_estimate_radii(const double *ppos, const double *pdir, const uint8_t *p
     grid_free(&pm.g);
 }
 
+/* SplitMix64's output function (Steele, Lea and Flood, OOPSLA 2014) of
+ * (slot + 1) times its increment: the per-slot term of a neighbour-set
+ * checksum (the same function as the GPU export's). */
+static uint64_t slot_mix(uint64_t slot) {
+    uint64_t z = (slot + 1u) * 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+/* The flux sums of estimate_radiance (tracer.rs:179-195) before its pw and
+ * 1/(pi r2) factors, per query: for the photons within r2 (kdtree within,
+ * tracer.rs:180), in the reference's ascending-distance order, sums[3i+wl]
+ * += wt(d, r2) * max(0, -n . dir) (filters tracer.rs:197-216,
+ * photon_to_radiance optics.rs:224-236); count[i] = number in radius;
+ * hash[i] = sum of slot_mix(photon index) mod 2^64. */
+void orc_gather_sums(const double *ppos, const double *pdir, const uint8_t *pwl, int64_t np,
+                     const double *qpos, const double *qnrm, int64_t nq, double r2, int pfilter,
+                     int64_t *count, uint64_t *hash, double *sums) {
+    grid_t g;
+    grid_build(&g, ppos, np, sqrt(r2));
+#pragma omp parallel num_threads(orc_get_threads())
+    {
+        nb_t *buf = NULL;
+        int64_t bc = 0;
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t i = 0; i < nq; i++) {
+            int64_t k = grid_query(&g, ppos, qpos + 3 * i, r2, &buf, &bc);
+            qsort(buf, (size_t)k, sizeof(nb_t), nb_cmp_dist);
+            V3 n = v3p(qnrm + 3 * i);
+            double s[3] = {0.0, 0.0, 0.0};
+            uint64_t h = 0;
+            for (int64_t j = 0; j < k; j++) {
+                double d = buf[j].d;
+                int32_t p = buf[j].i;
+                double wt = 1.0;
+                if (pfilter == ORC_PF_CONE) wt = orc_filter_cone(d, r2);
+                else if (pfilter == ORC_PF_GAUSS) wt = orc_filter_gauss(d, r2);
+                double cos0 = vdot(n, v3p(pdir + 3 * (int64_t)p));
+                double w = cos0 < 0.0 ? wt * -cos0 : 0.0;
+                s[pwl[p] < 2 ? pwl[p] : 2] += w;
+                h += slot_mix((uint64_t)p);
+            }
+            count[i] = k;
+            hash[i] = h;
+            for (int c = 0; c < 3; c++) sums[3 * i + c] = s[c];
+        }
+        free(buf);
+    }
+    grid_free(&g);
+}
+
 /* ------------------------------------------------------------------------ */
 /* Direct light: get_radiance_from_light / illuminated, tracer.rs:263-290;  */
 /* Light::get_direction / get_radiance, light.rs:93-150.  The reference     */

@@ -141,6 +141,15 @@ void orc_estimate_radii(const double *ppos, const double *pdir, const uint8_t *p
 /* wall seconds of the query phase (grid build excluded) of the last call above */
 double orc_last_query_seconds(void);
 
+/* Per query, the flux sums of estimate_radiance before its pw and 1/(pi r2)
+ * factors: sums[3i + wl] = sum over the photons within r2, in ascending
+ * distance, of wt(d, r2) * max(0, -n_i . dir); count[i] = photons within r2;
+ * hash[i] = sum (mod 2^64) of SplitMix64's output function of
+ * (index + 1) * 0x9e3779b97f4a7c15 over their indices (a set checksum). */
+void orc_gather_sums(const double *ppos, const double *pdir, const uint8_t *pwl, int64_t np,
+                     const double *qpos, const double *qnrm, int64_t nq, double r2, int pfilter,
+                     int64_t *count, uint64_t *hash, double *sums);
+
 /* ---- photon tracing (src/tracer.rs:31-125, src/ray/light.rs:67-91) ------ */
 /* Emits the per-light counts of src/bin/ppmpa.rs:30-31 (pw = sum flux / nphoton,
  * n_l = round(flux_l / pw)) and traces every photon.  Stored photons are written

@@ -72,6 +72,7 @@ SIGNATURES = {
     "ppm_render_stats": (C.c_int, [_P, C.POINTER(S.Stats)]),
     "ppm_set_stage_timing": (C.c_int, [_P, C.c_int32]),
     "ppm_stage_name": (C.c_char_p, [C.c_int32]),
+    "ppm_render_gather_export": (C.c_int, [_P, C.POINTER(S.GatherExport)]),
 }
 
 _lib = None

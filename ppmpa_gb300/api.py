@@ -31,6 +31,7 @@ def _ptr(a: np.ndarray, ctype):
 # RenderConfig.flags bits (include/ppm_api.h)
 RENDER_TUNE_CELLS = 1   # time cells per radius 1 and 2 before the render, keep the faster
 RENDER_CLASSIC = 2      # the classic ray tracer (trace_ray_classic) instead of photon mapping
+RENDER_ROW_WALK = 4     # mixed render: per-hit-point row-walk gather instead of the tile gather
 
 
 @dataclass
@@ -269,6 +270,31 @@ class Context:
         img = np.zeros(self._image_shape(), np.float64)
         self._check(self.lib.ppm_render_pass_image(self.h, _ptr(img, C.c_double)))
         return img
+
+    def render_gather_export(self) -> dict:
+        """Runs one more pass of the begun mixed render with the gather's
+        per-hit-point records on (ppm_render_gather_export) and returns that
+        pass's sorted photon map (float32 n x 4; the last column holds the
+        direction word's bits), hit points (float32 n x 10; the pixel's bits in
+        the last column), per-hit-point FP32 flux sums, in-radius counts,
+        neighbour-set checksums and the FP32 gathered-flux image."""
+        ex = S.GatherExport()
+        self._check(self.lib.ppm_render_gather_export(self.h, C.byref(ex)))   # capacities only
+        ph = np.zeros((ex.n_photons, 4), np.float32)
+        hits = np.zeros((ex.n_hits, 10), np.float32)
+        sums = np.zeros((ex.n_hits, 3), np.float32)
+        counts = np.zeros(ex.n_hits, np.uint32)
+        checks = np.zeros(ex.n_hits, np.uint64)
+        gathered = np.zeros(self._image_shape(), np.float32)
+        ex.photon_cap, ex.hit_cap = ph.shape[0], hits.shape[0]
+        ex.photons, ex.hits, ex.sums = _ptr(ph, C.c_float), _ptr(hits, C.c_float), _ptr(sums, C.c_float)
+        ex.counts, ex.checksums = _ptr(counts, C.c_uint32), _ptr(checks, C.c_uint64)
+        ex.gathered = _ptr(gathered, C.c_float)
+        self._check(self.lib.ppm_render_gather_export(self.h, C.byref(ex)))
+        n, m = ex.n_photons, ex.n_hits
+        return dict(photons=ph[:n].copy(), hits=hits[:m].copy(), sums=sums[:m].copy(), counts=counts[:m].copy(),
+                    checksums=checks[:m].copy(), gathered=gathered, radius2=ex.radius2,
+                    photon_power=ex.photon_power, pass_index=ex.pass_, pfilter=ex.pfilter)
 
     def set_stage_timing(self, on):
         """0 off, 1 per-stage CUDA events, 2 events + gather candidate counters."""

@@ -40,11 +40,35 @@ void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fix
                      const uint32_t *start, double pw, const double *q_r2, int pfilter, GatherOutF out, int grid,
                      cudaStream_t s) {
 #define PPM_GATHER(C, P) k_gather_f<C, P><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pw, q_r2, pfilter, out)
-    if (q_r2 && out.count) PPM_GATHER(true, true);
+    if (!q_r2 && out.dump)   // the render gather's parity export
+        k_gather_f<false, false, true><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pw, q_r2, pfilter, out);
+    else if (q_r2 && out.count) PPM_GATHER(true, true);
     else if (q_r2) PPM_GATHER(false, true);
     else if (out.count) PPM_GATHER(true, false);
     else PPM_GATHER(false, false);
 #undef PPM_GATHER
+}
+void launch_gather_tile_f(const HitPoint<float> *hits, PassState *st, const float4 *smap, const uint32_t *start,
+                          int pfilter, GatherOutF out, int grid, cudaStream_t s) {
+#define PPM_TILE(C, D, F) k_gather_tile<C, D, F><<<grid, 32 * GATHER_TILE_WARPS, 0, s>>>(hits, st, smap, start, out)
+#define PPM_TILE_F(C, D)                                      \
+    do {                                                      \
+        if (pfilter == PF_CONE) PPM_TILE(C, D, PF_CONE);      \
+        else if (pfilter == PF_GAUSS) PPM_TILE(C, D, PF_GAUSS); \
+        else PPM_TILE(C, D, PF_NONE);                         \
+    } while (0)
+    if (out.dump) PPM_TILE_F(false, true);
+    else if (out.count) PPM_TILE_F(true, false);
+    else PPM_TILE_F(false, false);
+#undef PPM_TILE_F
+#undef PPM_TILE
+}
+int gather_tile_blocks_per_sm() {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_gather_tile<false, false, PF_NONE>, 32 * GATHER_TILE_WARPS,
+                                                      0) != cudaSuccess || n < 1)
+        n = 1;
+    return n;
 }
 void launch_within_f(const float *q, long long nq, const double *q_r2, const PassState *st, const float4 *smap,
                      const uint32_t *start, const int32_t *sidx, unsigned long long *counts,

@@ -50,6 +50,13 @@ void launch_make_queries_d(const double *pos, const double *nrm, long long n, Hi
     if (n <= 0) return;
     k_make_queries<double><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(pos, nrm, n, hits);
 }
+cudaError_t load_estimate_kernels_d() {
+    // an attribute query loads a lazily loaded kernel onto the current device
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, k_make_queries<double>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_gather_d);
+    return e;
+}
 void launch_intersect_d(const SceneView<double> &sc, const double *rays, long long n, double *t, int32_t *obj,
                         double *nrm, cudaStream_t s) {
     if (n <= 0) return;

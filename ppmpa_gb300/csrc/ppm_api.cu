@@ -11,7 +11,6 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <mutex>
 #include <string>
 #include <vector>
 
@@ -44,6 +43,7 @@ thread_local std::string g_create_error;
 struct ppm_ctx {
     int device = 0;
     int sm_count = 0;
+    int tile_blocks = 1;   // resident blocks per SM of the render's tile gather
     cudaStream_t s = nullptr, s2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::string err;
@@ -78,9 +78,12 @@ struct ppm_ctx {
     long long hit_cap = 0;
     DevBuf pass_img, sum_img;
     DevBuf pass_direct32, pass_gather32;   // FP32 path per-pass buffers
+    DevBuf gdump;                          // render gather parity export records
+    GatherDump *gather_dump = nullptr;     // set while the export pass is enqueued
     long long npx = 0;
     DevBuf scratch;   // parity entry-point staging
     DevBuf qstart;    // estimate queries: cell starts of the query sort
+    char *noalloc_base = nullptr;   // device address of the allocation-free estimate's array on this device
 
     // parity photon map
     int map_kind = 0;  // 0 none, 1 f64, 2 f32
@@ -399,9 +402,11 @@ static int enqueue_eye(ppm_ctx *ctx, HitPoint<T> *hits, Level level_fn, cudaStre
     using V = vec4_t<T>;
     EyeQueue<T> qa{as<V>(ctx->eqb[0]), as<V>(ctx->eqb[1]), as<V>(ctx->eqb[2])};
     EyeQueue<T> qb{as<V>(ctx->eqb[3]), as<V>(ctx->eqb[4]), as<V>(ctx->eqb[5])};
-    // Level 0 has one thread per pixel.  The deeper levels' sizes are only
-    // known on the device; their grids stride over the queue.
-    const int g0 = (int)std::max(1LL, std::min<long long>((ctx->npx + 127) / 128, (long long)ctx->sm_count * 16));
+    // Level 0 has one thread per pixel slot (pixels in tiles of 32, see
+    // eye_slots).  The deeper levels' sizes are only known on the device;
+    // their grids stride over the queue.
+    const long long slots = eye_slots(ctx->cam.xreso, ctx->cam.yreso);
+    const int g0 = (int)std::max(1LL, std::min<long long>((slots + 127) / 128, (long long)ctx->sm_count * 16));
     for (int l = 0; l < MAX_TRACE; l++)
         level_fn(l, (l & 1) ? qb : qa, (l & 1) ? qa : qb, (unsigned long long)ctx->eq_cap, hits,
                  l == 0 ? g0 : grid_blocks(ctx, 4), s);
@@ -426,6 +431,8 @@ extern "C" const char *ppm_status_string(int s) {
     default: return "unknown status";
     }
 }
+
+static cudaError_t noalloc_lookup(char **out);
 
 // The eye pass runs on a side stream beside the photon trace; it gets the
 // higher priority, so its blocks are scheduled first when both wait.
@@ -452,12 +459,23 @@ extern "C" int ppm_ctx_create(ppm_ctx **out, int device, uint64_t seed) {
         return PPM_ERR_CUDA;
     }
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    ctx->tile_blocks = gather_tile_blocks_per_sm();
     if (cudaStreamCreateWithFlags(&ctx->s, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithPriority(&ctx->s2, cudaStreamNonBlocking, eye_priority()) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaMalloc(&ctx->st, sizeof(PassState)) != cudaSuccess) {
         g_create_error = "stream/event/state allocation failed";
+        ppm_ctx_destroy(ctx);
+        return PPM_ERR_CUDA;
+    }
+    // the allocation-free estimate's array and kernels: placed on the device
+    // and its address resolved now, so that ppm_estimate_noalloc never loads
+    // or allocates anything
+    cudaError_t ea = noalloc_lookup(&ctx->noalloc_base);
+    if (ea == cudaSuccess) ea = load_estimate_kernels_d();
+    if (ea != cudaSuccess) {
+        g_create_error = std::string("placing the allocation-free estimate's array and kernels: ") + cudaGetErrorString(ea);
         ppm_ctx_destroy(ctx);
         return PPM_ERR_CUDA;
     }
@@ -482,7 +500,8 @@ extern "C" int ppm_ctx_destroy(ppm_ctx *ctx) {
                       &ctx->raw_d, &ctx->spos, &ctx->sdir, &ctx->raw_f, &ctx->sorted_f, &ctx->sidx,
                       &ctx->keyrank, &ctx->count, &ctx->start, &ctx->block_sums, &ctx->hits_d, &ctx->hits_f,
                       &ctx->pass_img, &ctx->sum_img, &ctx->scratch, &ctx->pass_direct32, &ctx->pass_gather32,
-                      &ctx->qstart, &ctx->bvh_nodes, &ctx->bvh_bounded, &ctx->bvh_unb, &ctx->bvh_order};
+                      &ctx->qstart, &ctx->bvh_nodes, &ctx->bvh_bounded, &ctx->bvh_unb, &ctx->bvh_order,
+                      &ctx->gdump};
     for (DevBuf *b : bufs) release(*b);
     for (DevBuf &b : ctx->eqb) release(b);
     if (ctx->st) cudaFree(ctx->st);
@@ -963,11 +982,13 @@ extern "C" int ppm_estimate(ppm_ctx *ctx, const double *pos, const double *nrm, 
 // fixed array in device memory instead, so it never allocates or frees.
 //
 // The array is one per device, shared by every context and every call in
-// this process.  Its device address is looked up the first time the entry
-// point runs on a device (with that device current); make that first call
-// before any stream capture begins.  Calls whose GPU work overlaps -- from
-// two host threads, or two contexts on the same device -- race on the array
-// and must be serialised by the caller.
+// this process.  ppm_ctx_create looks up its device address (with the
+// context's device current) and keeps it in the context: the lookup is what
+// loads this file's module onto the device and places the array there, so
+// that happens when the context is created, not in the middle of a run.  A
+// context created after a cudaDeviceReset looks the address up again.
+// Calls whose GPU work overlaps -- from two host threads, or two contexts on
+// the same device -- race on the array and must be serialised by the caller.
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -983,32 +1004,18 @@ constexpr size_t NOALLOC_BYTES = NOALLOC_OUT_OFF + sizeof(double) * 3 * NOALLOC_
 static_assert(NOALLOC_NRM_OFF % 256 == 0 && NOALLOC_HIT_OFF % 256 == 0 && NOALLOC_OUT_OFF % 256 == 0,
               "staging sections must stay 256-byte aligned");
 
-constexpr int NOALLOC_MAX_DEVICES = 64;
-std::mutex g_noalloc_mu;
-void *g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
-
 }  // namespace
 
 static __device__ __align__(256) unsigned char g_estimate_scratch[NOALLOC_BYTES];
 
-// Device address of g_estimate_scratch on ctx->device, looked up once per
-// device; ctx->device must be current.
-static int noalloc_scratch(ppm_ctx *ctx, char **out) {
-    if (ctx->device < 0 || ctx->device >= NOALLOC_MAX_DEVICES)
-        return set_err(ctx, PPM_ERR_INVALID_ARG, "device %d: the allocation-free estimate supports devices 0..%d",
-                       ctx->device, NOALLOC_MAX_DEVICES - 1);
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    void *&addr = g_noalloc_addr[ctx->device];
-    if (!addr) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_estimate_scratch);
-        if (e != cudaSuccess || !p)
-            return set_err(ctx, PPM_ERR_CUDA, "cudaGetSymbolAddress(estimate scratch) on device %d failed: %s",
-                           ctx->device, cudaGetErrorString(e));
-        addr = p;
-    }
-    *out = static_cast<char *>(addr);
-    return PPM_OK;
+// Device address of g_estimate_scratch on the current device (called by
+// ppm_ctx_create with the context's device current).
+static cudaError_t noalloc_lookup(char **out) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_estimate_scratch);
+    if (e == cudaSuccess && !p) e = cudaErrorInvalidSymbol;
+    *out = e == cudaSuccess ? static_cast<char *>(p) : nullptr;
+    return e;
 }
 
 extern "C" int ppm_estimate_noalloc(ppm_ctx *ctx, const double *pos, const double *nrm, int64_t nq,
@@ -1021,8 +1028,9 @@ extern "C" int ppm_estimate_noalloc(ppm_ctx *ctx, const double *pos, const doubl
     if (ctx->map_kind != 1) return set_err(ctx, PPM_ERR_NOT_READY, "no FP64 photon map built");
     if (nq == 0) return PPM_OK;
     CK(cudaSetDevice(ctx->device));
-    char *base = nullptr;
-    TRY(noalloc_scratch(ctx, &base));
+    char *base = ctx->noalloc_base;   // looked up by ppm_ctx_create
+    if (!base) return set_err(ctx, PPM_ERR_NOT_READY, "the allocation-free estimate's array is not placed on device %d",
+                              ctx->device);
     double *d_p = (double *)(base + NOALLOC_POS_OFF), *d_n = (double *)(base + NOALLOC_NRM_OFF);
     HitPoint<double> *d_h = (HitPoint<double> *)(base + NOALLOC_HIT_OFF);
     double *d_o = (double *)(base + NOALLOC_OUT_OFF);
@@ -1428,9 +1436,14 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
     CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
     if (ev) CK(cudaEventRecord(ev[7], s));
     if (mixed) {
-        GatherOutF go{as<float>(ctx->pass_gather32), nullptr, ctx->count_gather ? &ctx->st->candidates : nullptr};
-        launch_gather_f(as<HitPoint<float>>(ctx->hits_f), ctx->st, -1, as<float4>(ctx->sorted_f), as<uint32_t>(ctx->start),
-                        ctx->pw, nullptr, ctx->cam.pfilter, go, g8, s);
+        GatherOutF go{as<float>(ctx->pass_gather32), nullptr, ctx->count_gather ? &ctx->st->candidates : nullptr,
+                      ctx->gather_dump};
+        if (ctx->cfg.flags & PPM_RENDER_ROW_WALK)
+            launch_gather_f(as<HitPoint<float>>(ctx->hits_f), ctx->st, -1, as<float4>(ctx->sorted_f),
+                            as<uint32_t>(ctx->start), ctx->pw, nullptr, ctx->cam.pfilter, go, g8, s);
+        else
+            launch_gather_tile_f(as<HitPoint<float>>(ctx->hits_f), ctx->st, as<float4>(ctx->sorted_f),
+                                 as<uint32_t>(ctx->start), ctx->cam.pfilter, go, grid_blocks(ctx, ctx->tile_blocks), s);
     } else {
         GatherOutD go{as<double>(ctx->pass_img), nullptr, nullptr};
         launch_gather_d(as<HitPoint<double>>(ctx->hits_d), ctx->st, -1, as<double4>(ctx->spos), as<double4>(ctx->sdir),
@@ -1513,7 +1526,7 @@ extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
         return set_err(ctx, PPM_ERR_NOT_READY, "scene (with lights) and camera must be set first");
     if (cfg->nphoton <= 0 || cfg->passes < 0 || !(cfg->radius0 > 0.0) || cfg->precision < 0 || cfg->precision > 1 ||
         cfg->cell_factor < 0 || cfg->cell_factor > 2 || cfg->first_pass < 0 ||
-        (cfg->flags & ~(PPM_RENDER_TUNE_CELLS | PPM_RENDER_CLASSIC)))
+        (cfg->flags & ~(PPM_RENDER_TUNE_CELLS | PPM_RENDER_CLASSIC | PPM_RENDER_ROW_WALK)))
         return set_err(ctx, PPM_ERR_INVALID_ARG, "bad render configuration");
     cudaSetDevice(ctx->device);
     drop_graph(ctx);
@@ -1646,6 +1659,59 @@ extern "C" int ppm_render_stats(ppm_ctx *ctx, ppm_stats *out) {
         int64_t eye = (int64_t)ctx->cam.xreso * ctx->cam.yreso;
         for (int l = 1; l < MAX_TRACE + 2; l++) eye += (int64_t)h.eq[l];
         out->eye_rays = eye;
+    }
+    return PPM_OK;
+}
+
+// One eager pass with the gather's per-hit-point records on, then the pass's
+// photon map, hit points, records and gathered image to the host.
+extern "C" int ppm_render_gather_export(ppm_ctx *ctx, ppm_gather_export *ex) {
+    if (!ctx || !ex) return PPM_ERR_INVALID_ARG;
+    if (!ctx->render_ready) return set_err(ctx, PPM_ERR_NOT_READY, "ppm_render_begin first");
+    if (ctx->cfg.precision != PPM_PRECISION_MIXED || (ctx->cfg.flags & PPM_RENDER_CLASSIC))
+        return set_err(ctx, PPM_ERR_INVALID_ARG, "the gather export needs a mixed-precision photon-mapping render");
+    cudaSetDevice(ctx->device);
+    if (!ex->photons) {
+        ex->n_photons = ctx->photon_cap_f;
+        ex->n_hits = ctx->hit_cap;
+        return PPM_OK;
+    }
+    if (!ex->hits || !ex->sums || !ex->counts || !ex->checksums || !ex->gathered || ex->photon_cap < 0 ||
+        ex->hit_cap < 0)
+        return set_err(ctx, PPM_ERR_INVALID_ARG, "every export array is required");
+    TRY(ensure(ctx, ctx->gdump, sizeof(GatherDump) * (size_t)ctx->hit_cap));
+    PassState before;
+    TRY(read_state(ctx, before));   // the exported pass's radius and index
+    ctx->gather_dump = as<GatherDump>(ctx->gdump);
+    const int rc = enqueue_pass(ctx, false);
+    ctx->gather_dump = nullptr;
+    if (rc != PPM_OK) return rc;
+    ctx->passes_done++;
+    PassState h;
+    TRY(check_overflow(ctx, h));
+    const long long np = (long long)std::min<unsigned long long>(h.n_stored, h.photon_cap);
+    const long long nh = (long long)std::min<unsigned long long>(h.n_hits, h.hit_cap);
+    ex->n_photons = np;
+    ex->n_hits = nh;
+    ex->radius2 = before.r2;
+    ex->photon_power = ctx->pw;
+    ex->pass = before.pass;
+    ex->pfilter = ctx->cam.pfilter;
+    if (np > ex->photon_cap || nh > ex->hit_cap)
+        return set_err(ctx, PPM_ERR_CAPACITY, "export needs %lld photons and %lld hit points", np, nh);
+    std::vector<GatherDump> rec((size_t)nh);
+    if (np) CK(cudaMemcpyAsync(ex->photons, ctx->sorted_f.p, sizeof(float4) * np, cudaMemcpyDeviceToHost, ctx->s));
+    if (nh) {
+        CK(cudaMemcpyAsync(ex->hits, ctx->hits_f.p, sizeof(HitPoint<float>) * nh, cudaMemcpyDeviceToHost, ctx->s));
+        CK(cudaMemcpyAsync(rec.data(), ctx->gdump.p, sizeof(GatherDump) * nh, cudaMemcpyDeviceToHost, ctx->s));
+    }
+    CK(cudaMemcpyAsync(ex->gathered, ctx->pass_gather32.p, sizeof(float) * 3 * ctx->npx, cudaMemcpyDeviceToHost,
+                       ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    for (long long i = 0; i < nh; i++) {
+        for (int c = 0; c < 3; c++) ex->sums[3 * i + c] = rec[i].s[c];
+        ex->counts[i] = rec[i].count;
+        ex->checksums[i] = rec[i].hash;
     }
     return PPM_OK;
 }

@@ -441,6 +441,20 @@ template <> struct EyeOut<float> {
     }
 };
 
+// Camera rays are launched in tiles of EYE_TILE_W x EYE_TILE_H pixels, one
+// tile per warp (tiles row-major over the image, pixels row-major inside a
+// tile), so that the hit points a warp appends are a compact patch of the
+// scene: the render gather takes hit points 32 at a time and walks the
+// photons around all of them once.  Slots of tiles that overhang the image
+// edge have no pixel.  The random streams are keyed by pixel, so the order
+// changes no result.
+constexpr int EYE_TILE_W = 4, EYE_TILE_H = 8;
+static_assert(EYE_TILE_W * EYE_TILE_H == 32, "one tile per warp");
+__host__ __device__ __forceinline__ long long eye_tiles_x(int xreso) { return (xreso + EYE_TILE_W - 1) / EYE_TILE_W; }
+__host__ __device__ __forceinline__ long long eye_slots(int xreso, int yreso) {
+    return eye_tiles_x(xreso) * ((yreso + EYE_TILE_H - 1) / EYE_TILE_H) * 32;
+}
+
 // CLASSIC: trace_ray_classic (tracer.rs:221-259) instead of trace_ray:
 // direct light of every light plus the camera's ambient, no hit points, the
 // exact mirror direction, refraction about the normal with the child's
@@ -451,8 +465,8 @@ __device__ __forceinline__ void eye_level(const SceneView<T, B> &sc, const DCame
                                           unsigned long long qcap, HitPoint<T> *hits, EyeOut<T> pix) {
     const uint32_t pass = (uint32_t)st->pass;
     const unsigned long long hit_cap = st->hit_cap;
-    const long long npx = (long long)cam.xreso * cam.yreso;
-    unsigned long long n = level == 0 ? (unsigned long long)npx : st->eq[level];
+    const long long ntx = eye_tiles_x(cam.xreso);
+    unsigned long long n = level == 0 ? (unsigned long long)eye_slots(cam.xreso, cam.yreso) : st->eq[level];
     if (level > 0 && n > qcap) n = qcap;
     const T air[3] = {T(1), T(1), T(1)};
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -461,8 +475,12 @@ __device__ __forceinline__ void eye_level(const SceneView<T, B> &sc, const DCame
         uint32_t p, node;
         int medium;
         if (level == 0) {
-            p = (uint32_t)i;
-            const T y = (T)(p / (uint32_t)cam.xreso), x = (T)(p % (uint32_t)cam.xreso);
+            const uint32_t tile = (uint32_t)(i >> 5), k = (uint32_t)(i & 31);
+            const uint32_t px = (tile % (uint32_t)ntx) * EYE_TILE_W + k % EYE_TILE_W;
+            const uint32_t py = (tile / (uint32_t)ntx) * EYE_TILE_H + k / EYE_TILE_W;
+            if (px >= (uint32_t)cam.xreso || py >= (uint32_t)cam.yreso) continue;
+            p = py * (uint32_t)cam.xreso + px;
+            const T y = (T)py, x = (T)px;
             Rng rg;
             rg.init(seed, p, pass, TAG_CAMERA);
             V3<T> blur = mk3(T(0), T(0), T(0));
@@ -747,13 +765,14 @@ __device__ __forceinline__ void for_each_candidate_pair(const GridParams &g, con
 }
 
 // The render gather's walk: the same steps as for_each_candidate_pair, with
-// a lane's two candidates handed to one call, use(two, p0, valid0, p1,
-// valid1), so that their radius tests and direction decodes form two
-// independent instruction chains in one block (one branch per step instead
-// of two).  A step over a row's last 32 or fewer candidates passes
+// a lane's two candidates handed to one call, use(two, p0, valid0, slot0,
+// p1, valid1, slot1), so that their radius tests and direction decodes form
+// two independent instruction chains in one block (one branch per step
+// instead of two).  A step over a row's last 32 or fewer candidates passes
 // two = std::false_type and no second photon, so that the body compiled for
 // it does one candidate's work.  Every lane makes every call, so use() may
-// hold warp votes.
+// hold warp votes.  The slots (map positions) are used by the parity export
+// only; the production body ignores them.
 template <typename U>
 __device__ __forceinline__ void for_each_candidate_two(const GridParams &g, const uint32_t *start, V3<float> q,
                                                        float r2, const int lo[3], const int hi[3],
@@ -773,9 +792,9 @@ __device__ __forceinline__ void for_each_candidate_two(const GridParams &g, cons
                 const float4 p0 = __ldg(&smap[v0 ? b + o0 : b]);
                 if (base + 32 < n) {
                     const float4 p1 = __ldg(&smap[v1 ? b + o1 : b]);
-                    use(std::true_type{}, p0, v0, p1, v1);
+                    use(std::true_type{}, p0, v0, b + o0, p1, v1, b + o1);
                 } else {
-                    use(std::false_type{}, p0, v0, p0, false);   // the row's last 32 or fewer
+                    use(std::false_type{}, p0, v0, b + o0, p0, false, b);   // the row's last 32 or fewer
                 }
             }
         }
@@ -943,10 +962,32 @@ __device__ __forceinline__ HitPoint<float> load_hit(const HitPoint<float> *p) {
     return h;
 }
 
+// Parity export of the render gather, one record per hit point: the FP32
+// flux sums per wavelength before the hit point's weight and the pass's
+// pw / (pi r^2) scale them, the number of photons found in radius, and the
+// sum over those photons of slot_mix(map slot), a checksum of the set.
+struct GatherDump {
+    float s[3];
+    uint32_t count;
+    unsigned long long hash;
+};
+static_assert(sizeof(GatherDump) == 24, "export record layout");
+
+// SplitMix64's output function (Steele, Lea and Flood, OOPSLA 2014) over
+// (slot + 1) times its increment: a well-mixed 64-bit value per map slot, so
+// that a sum over a set changes when any member does
+__host__ __device__ __forceinline__ unsigned long long slot_mix(uint32_t slot) {
+    unsigned long long z = ((unsigned long long)slot + 1ull) * 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
 struct GatherOutF {
     float *gathered;     // render: per-pass gathered flux W * sum (normalised later in FP64)
     double *out_rgb;     // estimate entry: per-query radiance
     unsigned long long *count;
+    GatherDump *dump;    // render parity export (null in the production render)
 };
 
 #if defined(PPM_BUILD_F32)
@@ -958,10 +999,10 @@ struct GatherOutF {
 // the per-query row set-up.  Returns false (nothing done) when the two are
 // in different cells.  Membership, weights and sums are those of the
 // one-query walk.
-template <bool COUNT>
+template <bool COUNT, bool DUMP>
 __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, const HitPoint<float> *hp,
                                             const uint32_t *start, const float4 *smap, int pfilter,
-                                            const GatherOutF &out) {
+                                            const GatherOutF &out, unsigned long long qi) {
     V3<float> qa, qb, na, nb;
     {
         const HitPoint<float> ha = load_hit(hp), hb = load_hit(hp + 1);
@@ -979,6 +1020,8 @@ __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, cons
     const unsigned lane = lane_id();
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, b0 = 0.f, b1 = 0.f, b2 = 0.f;
     unsigned long long c_slots = 0, c_valid = 0, c_hits = 0;
+    uint32_t na_in = 0, nb_in = 0;             // export only
+    unsigned long long ha_in = 0, hb_in = 0;   // export only
     const int ny = hi[1] - lo[1] + 1, nrows = ny * (hi[2] - lo[2] + 1);
     for (int row0 = 0; row0 < nrows; row0 += 32) {
         // lane's row: the union of the two queries' chord ranges
@@ -1026,6 +1069,13 @@ __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, cons
                     c_valid += 2 * (int)v;
                     c_hits += (int)ia + (int)ib;
                 }
+                if (DUMP && (ia || ib)) {
+                    const unsigned long long hm = slot_mix(b + o);
+                    na_in += ia ? 1u : 0u;
+                    nb_in += ib ? 1u : 0u;
+                    ha_in += ia ? hm : 0ull;
+                    hb_in += ib ? hm : 0ull;
+                }
                 if (ia || ib) {
                     const uint32_t mm = __float_as_uint(p.w);
                     float inv;
@@ -1062,6 +1112,18 @@ __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, cons
             atomicAdd(out.count + 2, c_slots);
         }
     }
+    if (DUMP) {
+        for (int o = 16; o > 0; o >>= 1) {
+            na_in += __shfl_xor_sync(0xffffffffu, na_in, o);
+            nb_in += __shfl_xor_sync(0xffffffffu, nb_in, o);
+            ha_in += __shfl_xor_sync(0xffffffffu, ha_in, o);
+            hb_in += __shfl_xor_sync(0xffffffffu, hb_in, o);
+        }
+        if (lane == 0) {
+            out.dump[qi] = GatherDump{{a0, a1, a2}, na_in, ha_in};
+            out.dump[qi + 1] = GatherDump{{b0, b1, b2}, nb_in, hb_in};
+        }
+    }
     if (lane == 0) {
         // weights and pixels re-read here (cached) rather than held through the walk
         const HitPoint<float> ha = load_hit(hp), hb = load_hit(hp + 1);
@@ -1089,7 +1151,7 @@ __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, cons
 // point, whose maps exceed L2, takes 4.  Five blocks per SM for the render
 // (at most 51 registers; it needs 46 without spilling) measured 1 % faster
 // than four; the estimate variants keep four.
-template <bool COUNT, bool PERQ>
+template <bool COUNT, bool PERQ, bool DUMP = false>
 __global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed,
                                                   const float4 *smap, const uint32_t *start, double pw,
                                                   const double *q_r2, int pfilter, GatherOutF out) {
@@ -1108,7 +1170,7 @@ __global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<f
             qend = c + CHUNK < nq ? c + CHUNK : nq;
         }
         if constexpr (!PERQ) {
-            if (qend - qi == 2 && gather_pair<COUNT>(g, st->r2, hits + qi, start, smap, pfilter, out)) {
+            if (qend - qi == 2 && gather_pair<COUNT, DUMP>(g, st->r2, hits + qi, start, smap, pfilter, out, qi)) {
                 qi += 2;
                 continue;
             }
@@ -1140,9 +1202,11 @@ __global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<f
         // without a branch on its wavelength.
         Kahan k0 = {0.f, 0.f}, k1 = {0.f, 0.f}, k2 = {0.f, 0.f};
         unsigned long long c_slots = 0, c_valid = 0, c_hits = 0;
+        uint32_t d_in = 0;             // export only
+        unsigned long long d_hash = 0;   // export only
         if constexpr (!PERQ) {
             for_each_candidate_two(g, start, q, r2f, lo, hi, smap,
-                                   [&](auto two, float4 p0, bool v0, float4 p1, bool v1) {
+                                   [&](auto two, float4 p0, bool v0, uint32_t i0, float4 p1, bool v1, uint32_t i1) {
                 constexpr bool TWO = decltype(two)::value;
                 if (COUNT) {
                     c_slots += TWO ? 2 : 1;
@@ -1188,6 +1252,10 @@ __global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<f
                         k2.s += l0 >= 2u ? w0 : 0.0f;
                     }
                     if (COUNT) c_hits += (int)in0 + (int)in1;
+                    if (DUMP) {
+                        d_in += (in0 ? 1u : 0u) + (in1 ? 1u : 0u);
+                        d_hash += (in0 ? slot_mix(i0) : 0ull) + (in1 ? slot_mix(i1) : 0ull);
+                    }
                 }
             });
         } else {
@@ -1230,6 +1298,13 @@ __global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<f
                 atomicAdd(out.count + 2, c_slots);
             }
         }
+        if constexpr (DUMP) {
+            for (int o = 16; o > 0; o >>= 1) {
+                d_in += __shfl_xor_sync(0xffffffffu, d_in, o);
+                d_hash += __shfl_xor_sync(0xffffffffu, d_hash, o);
+            }
+            if (lane == 0) out.dump[qi] = GatherDump{{s0, s1, s2}, d_in, d_hash};
+        }
         if (lane == 0) {
             if constexpr (!PERQ) {
                 // FP32 only here: an FP64 instruction costs a warp-wide slot of
@@ -1251,6 +1326,272 @@ __global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<f
         qi += 1ull;
     }
 }
+
+// ---------------------------------------------------------------------------
+// Render gather, tile form.  A warp takes 32 consecutive hit points, one per
+// lane; the eye pass appends them in pixel tiles, so they are a compact
+// patch of the scene.  The warp walks the photons of the cell rows around
+// all of them once: each batch of 32 photons is loaded (one coalesced
+// 512-byte read), decoded once (position, unit direction, wavelength) and
+// staged in shared memory grouped by wavelength, and then every lane tests
+// every staged photon against its own hit point.  A test is a distance, a
+// compare and, in radius, a cosine added to the lane's sum of that
+// wavelength: no per-hit-point row set-up, no idle lanes at row ends, no
+// warp reduction.  Rows are laid end to end, so batches are full until the
+// last.  Membership is exactly the kdtree crate's f64 predicate: FP32 d^2
+// below the FP32 band [r2_lo, r2_hi] is in, above it out, and a batch in
+// which any lane met a photon inside the band is redone with those photons
+// re-decided in FP64 (one warp vote per batch; the band is 2e-6 r^2 wide).
+// Flux: per-batch FP32 partial sums (at most 32 terms) added to per-lane
+// Kahan-compensated totals.
+//
+// A chunk whose hit points are spread out (an object edge inside the tile,
+// reflected or refracted hit points) is split into groups of hit points
+// within 2r of a leader per axis, each walked on its own; the lanes outside
+// the current group carry a far-away position, so they find nothing.
+// ---------------------------------------------------------------------------
+#if defined(PPM_BUILD_F32)
+constexpr int GATHER_TILE_WARPS = 8;   // warps per block
+
+// Rows (y, z) and their culled x ranges around the box [lo, hi]: the box's
+// distance to the row's y/z slab bounds the chord of every member's sphere
+// in that row, so the row keeps the cells within that chord of the box (with
+// the margins of RowCull, which exceed the rounding of cell coordinates).
+__device__ __forceinline__ bool box_row_range(const GridParams &g, V3<float> lo, V3<float> hi, float r2, int yy,
+                                              int zz, int lo_x, int hi_x, int &x0, int &x1) {
+    const float c = g.cellf, m = 4e-3f * c;
+    const float ylo = g.orgf[1] + (float)yy * c, zlo = g.orgf[2] + (float)zz * c;
+    const float dy = fmaxf(0.0f, fmaxf(ylo - hi.y, lo.y - (ylo + c)) - m);
+    const float dz = fmaxf(0.0f, fmaxf(zlo - hi.z, lo.z - (zlo + c)) - m);
+    const float rem = r2 * 1.00002f - dy * dy - dz * dz;
+    if (rem < 0.0f) return false;
+    const float rx = sqrtf(rem) * 1.00001f;
+    const float fx0 = floorf((lo.x - rx - g.orgf[0]) * g.invxf - 4e-3f);
+    const float fx1 = floorf((hi.x + rx - g.orgf[0]) * g.invxf + 4e-3f);
+    x0 = max(lo_x, (int)fmaxf(fx0, -1.0f));
+    x1 = min(hi_x, (int)fminf(fx1, (float)g.dim[0]));
+    return x0 <= x1;
+}
+
+template <int FILTER>
+__device__ __forceinline__ float tile_filter(float d2, float r2f) {
+    if constexpr (FILTER == PF_NONE) return 1.0f;
+    else return filter_wt_f(FILTER, d2, r2f);
+}
+
+// the group's box and its cells, shared by the warp's lanes through shared
+// memory (they are needed once per 32 rows, not in the test loop)
+struct TileBox {
+    float lo[3], hi[3];
+    int cx0, cx1, cy0, cz0, ny, nrows;
+};
+
+template <bool COUNT, bool DUMP, int FILTER>
+__global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_gather_tile(const HitPoint<float> *hits, PassState *st,
+                                                                        const float4 *smap, const uint32_t *start,
+                                                                        GatherOutF out) {
+    __shared__ float4 s_pos[GATHER_TILE_WARPS][32];   // x, y, z, map slot (export only)
+    __shared__ float4 s_dir[GATHER_TILE_WARPS][32];   // -direction (unit)
+    __shared__ float4 s_own[GATHER_TILE_WARPS][32];   // each lane's hit point position
+    __shared__ TileBox s_box[GATHER_TILE_WARPS];
+    const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+    float4 *const sp = s_pos[wid], *const sd = s_dir[wid];
+    TileBox &box = s_box[wid];
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned long long nq = n_hitpoints(st, -1);
+    const GridParams g = st->grid;
+    const double r2 = st->r2;
+    const float r2f = g.r2f, r2_lo = g.r2_lo, r2_hi = g.r2_hi;
+    const float two_r = 2.0f * sqrtf(r2f) * 1.001f;
+    constexpr float FAR = 1e30f;   // position of lanes outside the group: no photon is within r of it
+    unsigned long long c_tests = 0, c_slots = 0, c_hits = 0;
+    for (;;) {
+        unsigned long long c0 = 0;
+        if (lane == 0) c0 = atomicAdd(&st->gather_next, 32ull);
+        c0 = __shfl_sync(0xffffffffu, c0, 0);
+        if (c0 >= nq) break;
+        const unsigned long long qi = c0 + lane;
+        const bool valid = qi < nq;
+        V3<float> n = mk3(0.f, 0.f, 0.f);
+        {
+            float4 own = make_float4(FAR, FAR, FAR, 0.f);
+            if (valid) {
+                const HitPoint<float> h = load_hit(hits + qi);
+                own = make_float4(h.pos[0], h.pos[1], h.pos[2], 0.f);
+                n = ld3(h.nrm);
+            }
+            s_own[wid][lane] = own;
+        }
+        Kahan k0 = {0.f, 0.f}, k1 = {0.f, 0.f}, k2 = {0.f, 0.f};
+        uint32_t d_in = 0;
+        unsigned long long d_hash = 0;
+        unsigned pending = __ballot_sync(0xffffffffu, valid);
+        while (pending) {
+            // the group: pending lanes within 2r of the leader on every axis
+            const int leader = __ffs(pending) - 1;
+            __syncwarp();
+            const float4 own = s_own[wid][lane], ld = s_own[wid][leader];
+            const bool member = ((pending >> lane) & 1u) && fabsf(own.x - ld.x) <= two_r &&
+                                fabsf(own.y - ld.y) <= two_r && fabsf(own.z - ld.z) <= two_r;
+            pending &= ~__ballot_sync(0xffffffffu, member);
+            const V3<float> q = member ? mk3(own.x, own.y, own.z) : mk3(FAR, FAR, FAR);
+            {
+                // the group's box and the cells around it
+                V3<float> lo = q, hi = member ? q : mk3(-FAR, -FAR, -FAR);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    lo.x = fminf(lo.x, __shfl_xor_sync(0xffffffffu, lo.x, o));
+                    lo.y = fminf(lo.y, __shfl_xor_sync(0xffffffffu, lo.y, o));
+                    lo.z = fminf(lo.z, __shfl_xor_sync(0xffffffffu, lo.z, o));
+                    hi.x = fmaxf(hi.x, __shfl_xor_sync(0xffffffffu, hi.x, o));
+                    hi.y = fmaxf(hi.y, __shfl_xor_sync(0xffffffffu, hi.y, o));
+                    hi.z = fmaxf(hi.z, __shfl_xor_sync(0xffffffffu, hi.z, o));
+                }
+                if (lane == 0) {
+                    box.lo[0] = lo.x; box.lo[1] = lo.y; box.lo[2] = lo.z;
+                    box.hi[0] = hi.x; box.hi[1] = hi.y; box.hi[2] = hi.z;
+                    box.cx0 = max(CellMath<float>::coord(g, lo.x, 0) - g.extx, 0);
+                    box.cx1 = min(CellMath<float>::coord(g, hi.x, 0) + g.extx, g.dim[0] - 1);
+                    box.cy0 = max(CellMath<float>::coord(g, lo.y, 1) - g.ext, 0);
+                    const int cy1 = min(CellMath<float>::coord(g, hi.y, 1) + g.ext, g.dim[1] - 1);
+                    box.cz0 = max(CellMath<float>::coord(g, lo.z, 2) - g.ext, 0);
+                    const int cz1 = min(CellMath<float>::coord(g, hi.z, 2) + g.ext, g.dim[2] - 1);
+                    box.ny = cy1 - box.cy0 + 1;
+                    box.nrows = box.ny * (cz1 - box.cz0 + 1);
+                }
+                __syncwarp();
+            }
+            const int nrows = box.nrows;
+            for (int row0 = 0; row0 < nrows; row0 += 32) {
+                // lane's row and its photon range; rows end to end
+                uint32_t rbeg = 0, rlen = 0;
+                const int row = row0 + (int)lane;
+                if (row < nrows) {
+                    const int ny = box.ny;
+                    const int zz = box.cz0 + row / ny, yy = box.cy0 + row % ny;
+                    int x0, x1;
+                    if (box_row_range(g, mk3(box.lo[0], box.lo[1], box.lo[2]), mk3(box.hi[0], box.hi[1], box.hi[2]),
+                                      r2f, yy, zz, box.cx0, box.cx1, x0, x1)) {
+                        const int base = (zz * g.dim[1] + yy) * g.dim[0];
+                        rbeg = start[3 * (base + x0)];
+                        rlen = start[3 * (base + x1 + 1)] - rbeg;
+                    }
+                }
+                uint32_t incl = rlen;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= (unsigned)o) incl += u;
+                }
+                const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+                const uint32_t excl = incl - rlen;
+                for (uint32_t b0 = 0; b0 < total; b0 += 32) {
+                    // this lane's photon: the row r with excl_r <= j < incl_r
+                    const uint32_t j = b0 + lane;
+                    int r = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1)
+                        if (__shfl_sync(0xffffffffu, incl, r + step - 1) <= j) r += step;
+                    const uint32_t rb = __shfl_sync(0xffffffffu, rbeg, r), rx = __shfl_sync(0xffffffffu, excl, r);
+                    const bool v = j < total;
+                    uint32_t wl = 3u;
+                    float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pd = pa;
+                    if (v) {
+                        const uint32_t slot = rb + (j - rx);
+                        const float4 p = __ldg(&smap[slot]);
+                        const uint32_t m = __float_as_uint(p.w);
+                        float inv;
+                        const V3<float> d = oct_raw(m, inv);
+                        pa = make_float4(p.x, p.y, p.z, __uint_as_float(slot));
+                        pd = make_float4(-d.x * inv, -d.y * inv, -d.z * inv, 0.f);
+                        wl = min(m >> 30, 2u);
+                    }
+                    // stage grouped by wavelength
+                    const unsigned m0 = __ballot_sync(0xffffffffu, wl == 0u), m1 = __ballot_sync(0xffffffffu, wl == 1u),
+                                   m2 = __ballot_sync(0xffffffffu, wl == 2u);
+                    const int n0 = __popc(m0), n01 = n0 + __popc(m1), nv = n01 + __popc(m2);
+                    if (v) {
+                        const int at = wl == 0u ? __popc(m0 & lt) : (wl == 1u ? n0 + __popc(m1 & lt) : n01 + __popc(m2 & lt));
+                        sp[at] = pa;
+                        sd[at] = pd;
+                    }
+                    __syncwarp();
+                    // the tests; EXACT re-decides band photons in FP64
+                    bool band = false;
+                    auto sweep = [&](auto exact, int t0, int t1) -> float {
+                        constexpr bool EXACT = decltype(exact)::value;
+                        float acc = 0.0f;
+#pragma unroll 2
+                        for (int t = t0; t < t1; t++) {
+                            const float4 a = sp[t], b = sd[t];
+                            const float dx = q.x - a.x, dy = q.y - a.y, dz = q.z - a.z;
+                            const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                            bool in = d2 < r2_lo;
+                            const bool bd = !in && d2 <= r2_hi;
+                            if constexpr (EXACT) {
+                                if (bd) in = sq_euclid(f2d_here(q.x), f2d_here(q.y), f2d_here(q.z), (double)a.x,
+                                                       (double)a.y, (double)a.z) <= r2;
+                            } else {
+                                band |= bd;
+                            }
+                            const float c = __fmaf_rn(n.z, b.z, __fmaf_rn(n.y, b.y, n.x * b.x));
+                            float w = in ? fmaxf(c, 0.0f) : 0.0f;
+                            if constexpr (FILTER != PF_NONE) w *= in ? tile_filter<FILTER>(d2, r2f) : 0.0f;
+                            acc += w;
+                            if constexpr (EXACT && (DUMP || COUNT)) {
+                                if (in) {
+                                    if (DUMP) { d_in += 1u; d_hash += slot_mix(__float_as_uint(a.w)); }
+                                    if (COUNT) c_hits += 1;
+                                }
+                            }
+                        }
+                        return acc;
+                    };
+                    float a0 = sweep(std::false_type{}, 0, n0);
+                    float a1 = sweep(std::false_type{}, n0, n01);
+                    float a2 = sweep(std::false_type{}, n01, nv);
+                    if (__any_sync(0xffffffffu, band) || DUMP || COUNT) {
+                        // exact pass: the same tests with band photons re-decided in FP64
+                        // (the export and the counters always take it, as they count members)
+                        a0 = sweep(std::true_type{}, 0, n0);
+                        a1 = sweep(std::true_type{}, n0, n01);
+                        a2 = sweep(std::true_type{}, n01, nv);
+                    }
+                    k0.add(a0);
+                    k1.add(a1);
+                    k2.add(a2);
+                    if (COUNT) {
+                        c_tests += member ? (unsigned long long)nv : 0ull;   // photon-hit point distance tests
+                        c_slots += (unsigned long long)nv;                   // lane slots the batch issued
+                    }
+                    __syncwarp();   // the next batch overwrites the stage
+                }
+            }
+        }
+        if (DUMP && valid) out.dump[qi] = GatherDump{{k0.s - k0.c, k1.s - k1.c, k2.s - k2.c}, d_in, d_hash};
+        if (valid) {
+            const HitPoint<float> h = load_hit(hits + qi);
+            float *px = out.gathered + 3 * (size_t)h.pixel;
+            atomicAdd(px, h.w[0] * (k0.s - k0.c));
+            atomicAdd(px + 1, h.w[1] * (k1.s - k1.c));
+            atomicAdd(px + 2, h.w[2] * (k2.s - k2.c));
+        }
+        __syncwarp();   // s_own is rewritten by the next chunk
+    }
+    if (COUNT) {
+        for (int o = 16; o > 0; o >>= 1) {
+            c_tests += __shfl_xor_sync(0xffffffffu, c_tests, o);
+            c_hits += __shfl_xor_sync(0xffffffffu, c_hits, o);
+            c_slots += __shfl_xor_sync(0xffffffffu, c_slots, o);
+        }
+        if (lane == 0) {
+            atomicAdd(out.count + 0, c_tests);
+            atomicAdd(out.count + 1, c_hits);
+            atomicAdd(out.count + 2, c_slots);
+        }
+    }
+}
+#endif  // PPM_BUILD_F32
 
 // Estimate queries are gathered in the map's cell order, so that the warps
 // running at the same time walk the same cells and share photons in L2

@@ -27,6 +27,9 @@ void launch_within_d(const double *q, long long nq, const double *q_r2, const Pa
                      const uint32_t *start, unsigned long long *counts, const unsigned long long *offsets,
                      int32_t *idx_out, int grid, cudaStream_t s);
 void launch_make_queries_d(const double *pos, const double *nrm, long long n, HitPoint<double> *hits, cudaStream_t s);
+// loads the two kernels of the FP64 estimate onto the current device (with
+// lazy module loading they would otherwise load at their first launch)
+cudaError_t load_estimate_kernels_d();
 void launch_intersect_d(const SceneView<double> &sc, const double *rays, long long n, double *t, int32_t *obj,
                         double *nrm, cudaStream_t s);
 
@@ -50,6 +53,12 @@ void launch_eye_level_f(const SceneView<float> &sc, const DCamera<float> &cam, u
 void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
                      const uint32_t *start, double pw, const double *q_r2, int pfilter, GatherOutF out, int grid,
                      cudaStream_t s);
+// the render gather, tile form (k_gather_tile): 32 hit points per warp;
+// out.count / out.dump select the counting and the parity-export variants
+void launch_gather_tile_f(const HitPoint<float> *hits, PassState *st, const float4 *smap, const uint32_t *start,
+                          int pfilter, GatherOutF out, int grid, cudaStream_t s);
+// resident blocks per SM of the tile gather (its persistent grid is this x SMs)
+int gather_tile_blocks_per_sm();
 void launch_within_f(const float *q, long long nq, const double *q_r2, const PassState *st, const float4 *smap,
                      const uint32_t *start, const int32_t *sidx, unsigned long long *counts,
                      const unsigned long long *offsets, int32_t *idx_out, int grid, cudaStream_t s);

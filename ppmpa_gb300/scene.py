@@ -80,6 +80,15 @@ class Stats(C.Structure):
                 ("eye_rays", C.c_int64)]
 
 
+class GatherExport(C.Structure):
+    """ppm_gather_export (include/ppm_api.h): the render gather's per-hit-point parity export."""
+    _fields_ = [("photon_cap", C.c_int64), ("hit_cap", C.c_int64), ("n_photons", C.c_int64), ("n_hits", C.c_int64),
+                ("radius2", C.c_double), ("photon_power", C.c_double), ("pass_", C.c_int32), ("pfilter", C.c_int32),
+                ("photons", C.POINTER(C.c_float)), ("hits", C.POINTER(C.c_float)), ("sums", C.POINTER(C.c_float)),
+                ("counts", C.POINTER(C.c_uint32)), ("checksums", C.POINTER(C.c_uint64)),
+                ("gathered", C.POINTER(C.c_float))]
+
+
 # ---------------------------------------------------------------------------
 # vector helpers in the reference's evaluation order (src/ray/algebra.rs)
 # ---------------------------------------------------------------------------

@@ -4,16 +4,18 @@ tests/golden/reference_kats.json.
 Reads the reference's Rust test modules as text (the reference cannot be
 built here: no Rust toolchain), finds each assert by pattern and records the
 literal values with their file:line.  Run from the repository root with the
-reference checked out at REF (default /root/reference):
+path of a reference checkout, as an argument or in PPM_REFERENCE:
 
-    python tests/golden/make_reference_kats.py [REF]
+    python tests/golden/make_reference_kats.py REF
 """
 import json
 import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PPM_REFERENCE", "")
+if __name__ == "__main__" and not os.path.isdir(os.path.join(REF, "src")):
+    sys.exit("usage: make_reference_kats.py REF (a checkout of the reference; or set PPM_REFERENCE)")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_kats.json")
 NUM = r"(-?[0-9]+(?:\.[0-9]+)?(?:e-?[0-9]+)?)"
 

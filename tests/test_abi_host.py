@@ -154,3 +154,41 @@ def test_every_context_entry_point_rejects_a_null_context(built_lib):
         checked += 1
     assert checked >= 25
     assert lib.ppm_batch_render(None, None, 0, None) == 1
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every struct of include/ppm_api.h against its ctypes mirror: a C
+    program compiled against the header prints each struct's size and each
+    field's offset, and the mirrors must agree field by field."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    from ppmpa_gb300 import scene as S
+    pairs = {"ppm_object": S.Object, "ppm_material": S.Material, "ppm_light": S.Light, "ppm_camera": S.Camera,
+             "ppm_render_cfg": S.RenderCfg, "ppm_stats": S.Stats, "ppm_job": S.Job,
+             "ppm_gather_export": S.GatherExport}
+    # ctypes field names that differ from the C ones (C keywords / reserved words in Python)
+    rename = {("ppm_gather_export", "pass_"): "pass"}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ppm_api.h"', "int main(void) {"]
+    for cname, py in pairs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f in py._fields_:
+            field = rename.get((cname, f[0]), f[0])
+            lines.append(f'printf("{cname} {f[0]} %zu\\n", offsetof({cname}, {field}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([gcc, "-std=c11", "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n"):
+        if line:
+            a, b, c = line.split()
+            got[(a, b)] = int(c)
+    for cname, py in pairs.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for f in py._fields_:
+            assert got[(cname, f[0])] == getattr(py, f[0]).offset, (cname, f[0])

@@ -177,6 +177,108 @@ def test_sphere_extremes_just_past_a_cell_face_are_walked():
         assert checked > 150
 
 
+# ---- the tile gather (k_gather_tile): one walk for a group of hit points,
+# rows around the group's box (cell ranges widened by ext from the box's
+# corner cells) culled by the box's distance to each row's slab
+def box_row_range(g, lo, hi, r2f, yy, zz, lo_x, hi_x):
+    c = g["cellf"]
+    m = f32(4e-3) * c
+    ylo = g["orgf"][1] + f32(yy) * c
+    zlo = g["orgf"][2] + f32(zz) * c
+    dy = max(f32(0), max(ylo - hi[1], lo[1] - (ylo + c)) - m)
+    dz = max(f32(0), max(zlo - hi[2], lo[2] - (zlo + c)) - m)
+    rem = r2f * f32(1.00002) - dy * dy - dz * dz
+    if rem < 0:
+        return None
+    rx = np.sqrt(rem, dtype=f32) * f32(1.00001)
+    fx0 = np.floor((lo[0] - rx - g["orgf"][0]) * g["invxf"] - f32(4e-3))
+    fx1 = np.floor((hi[0] + rx - g["orgf"][0]) * g["invxf"] + f32(4e-3))
+    x0 = max(lo_x, int(max(fx0, -1.0)))
+    x1 = min(hi_x, int(min(fx1, float(g["dim"][0]))))
+    return (x0, x1) if x0 <= x1 else None
+
+
+def tile_walked_cells(g, group):
+    lo = group.min(axis=0).astype(f32)
+    hi = group.max(axis=0).astype(f32)
+    e = (g["extx"], g["ext"], g["ext"])
+    c0 = [max(coord(g, lo[a], a) - e[a], 0) for a in range(3)]
+    c1 = [min(coord(g, hi[a], a) + e[a], g["dim"][a] - 1) for a in range(3)]
+    cells = set()
+    for zz in range(c0[2], c1[2] + 1):
+        for yy in range(c0[1], c1[1] + 1):
+            rr = box_row_range(g, lo, hi, g["r2f"], yy, zz, c0[0], c1[0])
+            if rr is not None:
+                cells.update((x, yy, zz) for x in range(rr[0], rr[1] + 1))
+    return cells
+
+
+def _tile_group(rng, lo, hi, r):
+    """Hit points of a 4 x 8 pixel tile on a plane through the box (a few
+    millimetres apart), sometimes with members up to 2r from the first, as
+    the tile gather's grouping allows."""
+    centre = rng.uniform(lo + 0.15, hi - 0.15)
+    u = rng.normal(size=3)
+    u /= np.linalg.norm(u)
+    v = np.cross(u, rng.normal(size=3))
+    v /= np.linalg.norm(v)
+    step = rng.uniform(0.001, 0.006)
+    pts = [centre + (i % 4) * step * u + (i // 4) * step * v for i in range(32)]
+    if rng.random() < 0.3:
+        pts[-1] = centre + rng.uniform(-2 * r, 2 * r, 3)
+    return np.array(pts).astype(f32)
+
+
+@pytest.mark.parametrize("k", [1.0, 2.0])
+def test_tile_walk_holds_every_members_photons(k):
+    rng = np.random.default_rng(15)
+    lo, hi = np.array([-1.0, 0.0, 0.0]), np.array([1.0, 2.0, 2.0])
+    r = 0.031
+    r2 = r * r
+    g = grid(lo, hi, r2, k=k)
+    photons = np.vstack([rng.uniform(lo, hi, (40000, 3)).astype(f32), _boundary_points(rng, g, 4000)])
+    pc = [tuple(coord(g, p[a], a) for a in range(3)) for p in photons]
+    for _ in range(60):
+        group = _tile_group(rng, lo, hi, r)
+        cells = tile_walked_cells(g, group)
+        for q in group:
+            hit = np.nonzero(in_radius(q, photons, r2))[0]
+            assert all(pc[i] in cells for i in hit), q
+            for p in shell(rng, q, r2, 300):
+                assert tuple(coord(g, p[a], a) for a in range(3)) in cells, (q, p)
+
+
+def test_tile_walk_holds_sphere_extremes_just_past_a_cell_face():
+    """A member whose sphere's extreme point lies a few ulps past a cell
+    face, with a photon just inside the radius there, in a group whose box
+    extends away from it: the box's rows and chords must still reach it."""
+    rng = np.random.default_rng(16)
+    lo, hi = np.array([-1.0, 0.0, 0.0]), np.array([1.0, 2.0, 2.0])
+    for r in (0.0123, 0.037):
+        r2 = r * r
+        g = grid(lo, hi, r2)
+        checked = 0
+        for _ in range(200):
+            a = int(rng.integers(0, 3))
+            sgn = 1.0 if rng.random() < 0.5 else -1.0
+            cw = 1.0 / float(g["invxf"] if a == 0 else g["invf"])
+            kk = int(rng.integers(3, g["dim"][a] - 3))
+            face = float(g["orgf"][a]) + kk * cw
+            q = rng.uniform(lo + 0.2, hi - 0.2)
+            q[a] = face - sgn * r + sgn * float(rng.integers(1, 64)) * 2.0 ** -23 * max(1.0, abs(face))
+            q = q.astype(f32)
+            p = q.astype(np.float64).copy()
+            p[a] += sgn * r * (1 - 2.0 ** -18)
+            p = p.astype(f32)
+            if not in_radius(q, p[None, :], r2)[0]:
+                continue
+            others = (q.astype(np.float64) - sgn * np.abs(rng.normal(0, r / 2, (7, 3)))).astype(f32)
+            cell = tuple(coord(g, p[i], i) for i in range(3))
+            assert cell in tile_walked_cells(g, np.vstack([q[None, :], others])), (r, a, sgn, q, p)
+            checked += 1
+        assert checked > 100
+
+
 # ---- the FP64 (plain) path: the same grid in doubles, RowCull<double> and
 # CellMath<double>; its kernels are built without FMA contraction, so these
 # float64 expressions round as the device's do
