@@ -63,6 +63,30 @@ void launch_gather_tile_f(const HitPoint<float> *hits, PassState *st, const floa
 #undef PPM_TILE_F
 #undef PPM_TILE
 }
+void launch_hit_sort_f(const HitPoint<float> *hits, PassState *st, uint32_t *count, uint32_t *block_sums,
+                       uint32_t *start, uint2 *keyrank, HitPoint<float> *sorted, int grid, cudaStream_t s) {
+    k_hit_bounds<<<grid / 4 > 0 ? grid / 4 : 1, 256, 0, s>>>(hits, st);
+    k_hit_key<<<grid, 256, 0, s>>>(hits, st, count, keyrank);
+    launch_scan(count, st, block_sums, start, HIT_KEYS, s, grid, HIT_KEYS);
+    k_hit_place<<<grid, 256, 0, s>>>(hits, st, keyrank, start, sorted);
+}
+int kernels_per_hit_sort() { return 3 + kernels_per_scan(); }
+void launch_estimate_tile_f(const HitPoint<float> *hits, const double *r2s, long long nq, PassState *st,
+                            const float4 *smap, const uint32_t *start, double pw, GatherOutF out, int grid,
+                            cudaStream_t s) {
+    if (nq <= 0) return;
+    if (out.count)
+        k_estimate_tile<true><<<grid, 32 * GATHER_TILE_WARPS, 0, s>>>(hits, r2s, nq, st, smap, start, pw, out);
+    else
+        k_estimate_tile<false><<<grid, 32 * GATHER_TILE_WARPS, 0, s>>>(hits, r2s, nq, st, smap, start, pw, out);
+}
+int estimate_tile_blocks_per_sm() {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_estimate_tile<false>, 32 * GATHER_TILE_WARPS, 0) !=
+            cudaSuccess || n < 1)
+        n = 1;
+    return n;
+}
 int gather_tile_blocks_per_sm() {
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_gather_tile<false, false, PF_NONE>, 32 * GATHER_TILE_WARPS,
@@ -80,10 +104,11 @@ void launch_make_queries_f(const float *pos, const float *nrm, long long n, HitP
     k_make_queries<float><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(pos, nrm, n, hits);
 }
 void launch_query_sort_f(const float *pos, const float *nrm, const double *r2, long long n, PassState *st,
-                         uint32_t *count, uint32_t *block_sums, uint32_t *qstart, long long cell_cap, uint2 *keyrank,
-                         HitPoint<float> *hits, double *r2_sorted, int grid, cudaStream_t s) {
+                         double r2max, uint32_t *count, uint32_t *block_sums, uint32_t *qstart, long long cell_cap,
+                         uint2 *keyrank, HitPoint<float> *hits, double *r2_sorted, int grid, cudaStream_t s) {
     if (n <= 0) return;
-    k_query_hist<<<grid, 256, 0, s>>>(pos, n, st, count, keyrank);
+    // radius classes: r below r_max / 4, below r_max / 2, the rest
+    k_query_hist<<<grid, 256, 0, s>>>(pos, r2, n, st, r2max / 16.0, r2max / 4.0, count, keyrank);
     launch_scan(count, st, block_sums, qstart, cell_cap, s, grid);
     k_query_place<<<grid, 256, 0, s>>>(pos, nrm, r2, n, qstart, keyrank, hits, r2_sorted);
 }

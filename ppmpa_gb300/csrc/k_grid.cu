@@ -24,6 +24,8 @@ __global__ void k_pass_begin(PassState *st) {
     for (int a = 0; a < 3; a++) {
         st->bb_lo[a] = ord_enc(1e300);
         st->bb_hi[a] = ord_enc(-1e300);
+        st->hb_lo[a] = ordf_enc(0x7f7fffffu);   // +FLT_MAX
+        st->hb_hi[a] = ordf_enc(0xff7fffffu);   // -FLT_MAX
     }
 }
 
@@ -112,8 +114,14 @@ __device__ __forceinline__ uint4 load_counts(const uint32_t *count, long long i,
     return v;
 }
 
-__global__ void __launch_bounds__(256) k_scan_reduce(const uint32_t *count, const PassState *st, uint32_t *block_sums) {
-    const long long n = st->grid.nkeys;
+// key count of a scan: the pass grid's (fixed < 0) or a fixed one
+__device__ __forceinline__ long long scan_keys(const PassState *st, long long fixed) {
+    return fixed >= 0 ? fixed : st->grid.nkeys;
+}
+
+__global__ void __launch_bounds__(256) k_scan_reduce(const uint32_t *count, const PassState *st, long long fixed,
+                                                     uint32_t *block_sums) {
+    const long long n = scan_keys(st, fixed);
     const long long ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     __shared__ uint32_t ws[8];
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -137,8 +145,8 @@ __global__ void __launch_bounds__(256) k_scan_reduce(const uint32_t *count, cons
     }
 }
 
-__global__ void __launch_bounds__(1024) k_scan_top(uint32_t *block_sums, const PassState *st) {
-    const long long n = st->grid.nkeys;
+__global__ void __launch_bounds__(1024) k_scan_top(uint32_t *block_sums, const PassState *st, long long fixed) {
+    const long long n = scan_keys(st, fixed);
     const int nb = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
     __shared__ uint32_t sh[1024];
     // each thread owns up to 4 consecutive tile sums
@@ -164,9 +172,9 @@ __global__ void __launch_bounds__(1024) k_scan_top(uint32_t *block_sums, const P
     }
 }
 
-__global__ void __launch_bounds__(256) k_scan_down(uint32_t *count, const PassState *st, const uint32_t *block_sums,
-                                                   uint32_t *start) {
-    const long long n = st->grid.nkeys;
+__global__ void __launch_bounds__(256) k_scan_down(uint32_t *count, const PassState *st, long long fixed,
+                                                   const uint32_t *block_sums, uint32_t *start) {
+    const long long n = scan_keys(st, fixed);
     const long long ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ uint32_t ws[8];
@@ -231,12 +239,13 @@ __global__ void k_pass_end(PassState *st) {
 void launch_pass_begin(PassState *st, cudaStream_t s) { k_pass_begin<<<1, 32, 0, s>>>(st); }
 void launch_grid_setup(PassState *st, double r2_override, cudaStream_t s) { k_grid_setup<<<1, 32, 0, s>>>(st, r2_override); }
 void launch_scan(uint32_t *count, const PassState *st, uint32_t *block_sums, uint32_t *start, long long cell_cap,
-                 cudaStream_t s, int grid) {
-    const long long tiles = (cell_cap + SCAN_TILE - 1) / SCAN_TILE;
+                 cudaStream_t s, int grid, long long fixed_keys) {
+    const long long cap = fixed_keys >= 0 ? fixed_keys : cell_cap;
+    const long long tiles = (cap + SCAN_TILE - 1) / SCAN_TILE;
     const int nb = (int)(tiles < grid ? tiles : grid);
-    k_scan_reduce<<<nb, 256, 0, s>>>(count, st, block_sums);
-    k_scan_top<<<1, 1024, 0, s>>>(block_sums, st);
-    k_scan_down<<<nb, 256, 0, s>>>(count, st, block_sums, start);
+    k_scan_reduce<<<nb, 256, 0, s>>>(count, st, fixed_keys, block_sums);
+    k_scan_top<<<1, 1024, 0, s>>>(block_sums, st, fixed_keys);
+    k_scan_down<<<nb, 256, 0, s>>>(count, st, fixed_keys, block_sums, start);
 }
 int kernels_per_scan() { return 3; }
 void launch_accum(const double *pass_img, double *sum, long long n, cudaStream_t s) {

@@ -44,6 +44,7 @@ struct ppm_ctx {
     int device = 0;
     int sm_count = 0;
     int tile_blocks = 1;   // resident blocks per SM of the render's tile gather
+    int est_blocks = 1;    // and of the estimate entry point's chunk gather
     cudaStream_t s = nullptr, s2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::string err;
@@ -79,6 +80,9 @@ struct ppm_ctx {
     DevBuf pass_img, sum_img;
     DevBuf pass_direct32, pass_gather32;   // FP32 path per-pass buffers
     DevBuf gdump;                          // render gather parity export records
+    // the mixed render's hit points in Morton order (the gathers' input):
+    // sorted copy, key/rank per hit point, key counts, starts, scan tile sums
+    DevBuf hits_sorted, hkeyrank, hcount, hstart, hblock;
     GatherDump *gather_dump = nullptr;     // set while the export pass is enqueued
     long long npx = 0;
     DevBuf scratch;   // parity entry-point staging
@@ -370,6 +374,20 @@ static int ensure_grid(ppm_ctx *ctx) {
 
 static int grid_blocks(ppm_ctx *ctx, int per_sm) { return ctx->sm_count * per_sm; }
 
+// buffers of the mixed render's hit point sort (hit_cap must be set); the key
+// counts start zeroed and every scan leaves them zeroed
+static int ensure_hit_sort(ppm_ctx *ctx) {
+    TRY(ensure(ctx, ctx->hits_sorted, sizeof(HitPoint<float>) * (size_t)ctx->hit_cap));
+    TRY(ensure(ctx, ctx->hkeyrank, sizeof(uint2) * (size_t)ctx->hit_cap));
+    if (ctx->hcount.bytes == 0) {
+        TRY(ensure(ctx, ctx->hcount, sizeof(uint32_t) * HIT_KEYS));
+        CK(cudaMemsetAsync(ctx->hcount.p, 0, sizeof(uint32_t) * HIT_KEYS, ctx->s));
+    }
+    TRY(ensure(ctx, ctx->hstart, sizeof(uint32_t) * (HIT_KEYS + 1)));
+    TRY(ensure(ctx, ctx->hblock, sizeof(uint32_t) * (HIT_KEYS / SCAN_TILE + 1)));
+    return PPM_OK;
+}
+
 constexpr int EYE_QUEUE_PER_PIXEL = 2;   // eye-tree vertices per pixel a level may hold
 
 static int ensure_eye_queues(ppm_ctx *ctx, long long npx, size_t vec_bytes) {
@@ -460,6 +478,7 @@ extern "C" int ppm_ctx_create(ppm_ctx **out, int device, uint64_t seed) {
     }
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     ctx->tile_blocks = gather_tile_blocks_per_sm();
+    ctx->est_blocks = estimate_tile_blocks_per_sm();
     if (cudaStreamCreateWithFlags(&ctx->s, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithPriority(&ctx->s2, cudaStreamNonBlocking, eye_priority()) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
@@ -501,7 +520,7 @@ extern "C" int ppm_ctx_destroy(ppm_ctx *ctx) {
                       &ctx->keyrank, &ctx->count, &ctx->start, &ctx->block_sums, &ctx->hits_d, &ctx->hits_f,
                       &ctx->pass_img, &ctx->sum_img, &ctx->scratch, &ctx->pass_direct32, &ctx->pass_gather32,
                       &ctx->qstart, &ctx->bvh_nodes, &ctx->bvh_bounded, &ctx->bvh_unb, &ctx->bvh_order,
-                      &ctx->gdump};
+                      &ctx->gdump, &ctx->hits_sorted, &ctx->hkeyrank, &ctx->hcount, &ctx->hstart, &ctx->hblock};
     for (DevBuf *b : bufs) release(*b);
     for (DevBuf &b : ctx->eqb) release(b);
     if (ctx->st) cudaFree(ctx->st);
@@ -1213,8 +1232,9 @@ static int stage_estimate_f32(ppm_ctx *ctx, const float *pos, const float *nrm, 
 static int run_estimate_f32(ppm_ctx *ctx, const EstBatch &b, int64_t nq, bool count, cudaEvent_t e0, cudaEvent_t e1,
                             cudaEvent_t e2) {
     if (e0) CK(cudaEventRecord(e0, ctx->s));
-    launch_query_sort_f(b.p, b.n, b.r2, nq, ctx->st, as<uint32_t>(ctx->count), as<uint32_t>(ctx->block_sums),
-                        as<uint32_t>(ctx->qstart), CELL_CAP, b.kr, b.h, b.r2s, grid_blocks(ctx, 8), ctx->s);
+    launch_query_sort_f(b.p, b.n, b.r2, nq, ctx->st, ctx->map_r2, as<uint32_t>(ctx->count),
+                        as<uint32_t>(ctx->block_sums), as<uint32_t>(ctx->qstart), CELL_CAP, b.kr, b.h, b.r2s,
+                        grid_blocks(ctx, 8), ctx->s);
     GatherOutF go{nullptr, b.o, nullptr};
     if (count) {
         CK(cudaMemsetAsync(&ctx->st->candidates, 0, 3 * sizeof(unsigned long long), ctx->s));
@@ -1222,8 +1242,8 @@ static int run_estimate_f32(ppm_ctx *ctx, const EstBatch &b, int64_t nq, bool co
     }
     CK(cudaMemsetAsync(&ctx->st->gather_next, 0, sizeof(unsigned long long), ctx->s));
     if (e1) CK(cudaEventRecord(e1, ctx->s));
-    launch_gather_f(b.h, ctx->st, nq, as<float4>(ctx->sorted_f), as<uint32_t>(ctx->start), ctx->map_pw, b.r2s, PF_NONE,
-                    go, grid_blocks(ctx, 8), ctx->s);
+    launch_estimate_tile_f(b.h, b.r2s, nq, ctx->st, as<float4>(ctx->sorted_f), as<uint32_t>(ctx->start), ctx->map_pw,
+                           go, grid_blocks(ctx, ctx->est_blocks), ctx->s);
     CK(cudaGetLastError());
     if (e2) CK(cudaEventRecord(e2, ctx->s));
     return PPM_OK;
@@ -1407,6 +1427,12 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
                 launch_eye_level_d(ctx->sv_d, ctx->cam_d, ctx->cfg.seed, ctx->st, uc, l, in, out, qcap, h,
                                    EyeOut<double>{as<double>(ctx->pass_img)}, g, st);
             }, s2);
+    if (mixed) {   // hit points into Morton order for the gather, still on the eye stream
+        launch_hit_sort_f(as<HitPoint<float>>(ctx->hits_f), ctx->st, as<uint32_t>(ctx->hcount),
+                          as<uint32_t>(ctx->hblock), as<uint32_t>(ctx->hstart), as<uint2>(ctx->hkeyrank),
+                          as<HitPoint<float>>(ctx->hits_sorted), grid_blocks(ctx, 8), s2);
+        kernels += kernels_per_hit_sort();
+    }
     if (ev) CK(cudaEventRecord(ev[6], s2));
     CK(cudaEventRecord(ctx->ev_join, s2));
     // photons
@@ -1439,10 +1465,10 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
         GatherOutF go{as<float>(ctx->pass_gather32), nullptr, ctx->count_gather ? &ctx->st->candidates : nullptr,
                       ctx->gather_dump};
         if (ctx->cfg.flags & PPM_RENDER_ROW_WALK)
-            launch_gather_f(as<HitPoint<float>>(ctx->hits_f), ctx->st, -1, as<float4>(ctx->sorted_f),
+            launch_gather_f(as<HitPoint<float>>(ctx->hits_sorted), ctx->st, -1, as<float4>(ctx->sorted_f),
                             as<uint32_t>(ctx->start), ctx->pw, nullptr, ctx->cam.pfilter, go, g8, s);
         else
-            launch_gather_tile_f(as<HitPoint<float>>(ctx->hits_f), ctx->st, as<float4>(ctx->sorted_f),
+            launch_gather_tile_f(as<HitPoint<float>>(ctx->hits_sorted), ctx->st, as<float4>(ctx->sorted_f),
                                  as<uint32_t>(ctx->start), ctx->cam.pfilter, go, grid_blocks(ctx, ctx->tile_blocks), s);
     } else {
         GatherOutD go{as<double>(ctx->pass_img), nullptr, nullptr};
@@ -1551,6 +1577,7 @@ extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
     if (cfg->precision == PPM_PRECISION_MIXED) {
         TRY(ensure(ctx, ctx->pass_direct32, sizeof(float) * 3 * ctx->npx));
         TRY(ensure(ctx, ctx->pass_gather32, sizeof(float) * 3 * ctx->npx));
+        if (photons) TRY(ensure_hit_sort(ctx));
     }
     TRY(ensure(ctx, ctx->sum_img, sizeof(double) * 3 * ctx->npx));
     CK(cudaMemsetAsync(ctx->sum_img.p, 0, sizeof(double) * 3 * ctx->npx, ctx->s));
@@ -1702,7 +1729,8 @@ extern "C" int ppm_render_gather_export(ppm_ctx *ctx, ppm_gather_export *ex) {
     std::vector<GatherDump> rec((size_t)nh);
     if (np) CK(cudaMemcpyAsync(ex->photons, ctx->sorted_f.p, sizeof(float4) * np, cudaMemcpyDeviceToHost, ctx->s));
     if (nh) {
-        CK(cudaMemcpyAsync(ex->hits, ctx->hits_f.p, sizeof(HitPoint<float>) * nh, cudaMemcpyDeviceToHost, ctx->s));
+        CK(cudaMemcpyAsync(ex->hits, ctx->hits_sorted.p, sizeof(HitPoint<float>) * nh, cudaMemcpyDeviceToHost,
+                           ctx->s));
         CK(cudaMemcpyAsync(rec.data(), ctx->gdump.p, sizeof(GatherDump) * nh, cudaMemcpyDeviceToHost, ctx->s));
     }
     CK(cudaMemcpyAsync(ex->gathered, ctx->pass_gather32.p, sizeof(float) * 3 * ctx->npx, cudaMemcpyDeviceToHost,

@@ -66,6 +66,7 @@ struct PassState {
     unsigned long long hit_cap;      // and this many hit points
     unsigned long long photon_rays;         // photon ray segments traced this pass (one per event)
     unsigned long long eq[MAX_TRACE + 2];   // eye-tree vertices at each depth
+    uint32_t hb_lo[3], hb_hi[3];            // hit point bounds (orderable FP32 encodings)
 };
 
 // number of valid photons / hit points (the counters keep counting past the
@@ -92,6 +93,29 @@ __device__ __forceinline__ double ord_dec(unsigned long long e) {
     unsigned long long b = (e >> 63) ? (e & 0x7fffffffffffffffULL) : ~e;
     return __longlong_as_double((long long)b);
 }
+
+// orderable encoding of a float for atomicMin / atomicMax on unsigned words
+__host__ __device__ __forceinline__ uint32_t ordf_enc(uint32_t bits) {
+    return (bits >> 31) ? ~bits : (bits | 0x80000000u);
+}
+__device__ __forceinline__ float ordf_dec(uint32_t e) {
+    return __uint_as_float((e >> 31) ? (e & 0x7fffffffu) : ~e);
+}
+
+// bits 0..9 of v spread to every third bit (Morton interleave)
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+// the hit point sort's grid: 2^7 cubic cells per axis over the hit points'
+// bounds, keys are Morton codes
+constexpr int HIT_MORTON_BITS = 7;
+constexpr long long HIT_KEYS = 1LL << (3 * HIT_MORTON_BITS);
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
@@ -1383,6 +1407,7 @@ __device__ __forceinline__ float tile_filter(float d2, float r2f) {
 // memory (they are needed once per 32 rows, not in the test loop)
 struct TileBox {
     float lo[3], hi[3];
+    float r2;   // the group's largest radius^2 (estimate entry point)
     int cx0, cx1, cy0, cz0, ny, nrows;
 };
 
@@ -1593,17 +1618,402 @@ __global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_gather_tile(const Hi
 }
 #endif  // PPM_BUILD_F32
 
+// ---------------------------------------------------------------------------
+// Hit points in Morton order, the tile gather's input.  The eye pass appends
+// hit points warp by warp in whatever order its warps run, so 32 consecutive
+// hit points are rarely one patch of the scene.  On the eye stream (beside
+// the photon trace) the hit points are counting-sorted by the Morton code of
+// their cell in a 128^3 grid of cubic cells over their bounds: bounds, key
+// and rank per hit point, scan of the 2^21 key counts, placement.  32
+// consecutive sorted hit points then lie in one or a few neighbouring cells.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_hit_bounds(const HitPoint<float> *hits, PassState *st) {
+    const unsigned long long n = n_hitpoints(st, -1);
+    float lo[3] = {3e38f, 3e38f, 3e38f}, hi[3] = {-3e38f, -3e38f, -3e38f};
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const float2 a = reinterpret_cast<const float2 *>(hits + i)[0];
+        const float z = reinterpret_cast<const float *>(hits + i)[2];
+        const float v[3] = {a.x, a.y, z};
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            if (v[k] > -3e38f && v[k] < 3e38f) {   // finite (false for NaN)
+                lo[k] = fminf(lo[k], v[k]);
+                hi[k] = fmaxf(hi[k], v[k]);
+            }
+    }
+    // warp, then block reduction; one atomic per block and bound
+    __shared__ float slo[3][8], shi[3][8];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+        }
+        if (lane_id() == 0) { slo[k][threadIdx.x >> 5] = lo[k]; shi[k][threadIdx.x >> 5] = hi[k]; }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int k = threadIdx.x;
+        float l = slo[k][0], h = shi[k][0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+            l = fminf(l, slo[k][w]);
+            h = fmaxf(h, shi[k][w]);
+        }
+        if (l <= h) {
+            atomicMin(&st->hb_lo[k], ordf_enc(__float_as_uint(l)));
+            atomicMax(&st->hb_hi[k], ordf_enc(__float_as_uint(h)));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_hit_key(const HitPoint<float> *hits, PassState *st, uint32_t *count,
+                                                 uint2 *keyrank) {
+    const unsigned long long n = n_hitpoints(st, -1);
+    float org[3], ext = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        org[k] = ordf_dec(st->hb_lo[k]);
+        ext = fmaxf(ext, ordf_dec(st->hb_hi[k]) - org[k]);
+    }
+    const float inv = ext > 0.0f && ext < 3e38f ? (float)(1 << HIT_MORTON_BITS) / ext : 0.0f;
+    const int top = (1 << HIT_MORTON_BITS) - 1;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const float2 a = reinterpret_cast<const float2 *>(hits + i)[0];
+        const float z = reinterpret_cast<const float *>(hits + i)[2];
+        const float v[3] = {a.x, a.y, z};
+        uint32_t key = 0;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const float f = (v[k] - org[k]) * inv;   // NaN and out-of-range clamp to the grid
+            const int c = f >= 0.0f ? (f < (float)top ? (int)f : top) : 0;
+            key |= spread3((uint32_t)c) << (2 - k);
+        }
+        keyrank[i] = make_uint2(key, atomicAdd(&count[key], 1u));
+    }
+}
+
+__global__ void __launch_bounds__(256) k_hit_place(const HitPoint<float> *hits, const PassState *st,
+                                                   const uint2 *keyrank, const uint32_t *start,
+                                                   HitPoint<float> *sorted) {
+    const unsigned long long n = n_hitpoints(st, -1);
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint2 kr = keyrank[i];
+        sorted[start[kr.x] + kr.y] = hits[i];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Estimate entry point (per-query radii, ppm_estimate_f32), chunk form.  A
+// warp takes 32 consecutive queries of the cell-sorted batch.  A compact
+// chunk -- one whose box, widened by its largest radius, is small beside the
+// members' own spheres (dense queries, e.g. inside a caustic blob) -- is
+// walked as in the render's tile gather: each photon of the union of the
+// members' rows is loaded and decoded once and tested by every lane against
+// its own query and radius.  Otherwise the warp estimates its queries one
+// after another, its lanes striding through each query's own culled rows.
+// Both modes add every flux term w = max(0, -n . dir) in [0, 1] as an
+// integer of 2^-23 units (one FFMA puts round(w 2^23) in the mantissa of
+// 2^23 + w 2^23), so each query's sum is exact whatever the order, the
+// chunking or the mode: a query's estimate depends only on the query.
+// ---------------------------------------------------------------------------
+constexpr float FIX_ONE = 8388608.0f;                 // 2^23
+constexpr uint32_t FIX_BIAS = 0x4b000000u;            // bits of 2^23
+constexpr double FIX_UNIT = 1.0 / 8388608.0;          // 2^-23
+constexpr float EST_TILE_RATIO = 0.5f;                // tile mode: union box <= this x sum of member cubes
+
+// round(w 2^23) + FIX_BIAS as the bits of one float (w in [0, 1])
+__device__ __forceinline__ uint32_t fix_bits(float w) { return __float_as_uint(__fmaf_rn(w, FIX_ONE, FIX_ONE)); }
+
+template <bool COUNT>
+__global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_estimate_tile(const HitPoint<float> *hits, const double *r2s,
+                                                                          long long nq, PassState *st,
+                                                                          const float4 *smap, const uint32_t *start,
+                                                                          double pw, GatherOutF out) {
+    __shared__ float4 s_pos[GATHER_TILE_WARPS][32];
+    __shared__ float4 s_dir[GATHER_TILE_WARPS][32];
+    __shared__ float4 s_own[GATHER_TILE_WARPS][32];   // x, y, z, radius
+    __shared__ TileBox s_box[GATHER_TILE_WARPS];
+    const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+    float4 *const sp = s_pos[wid], *const sd = s_dir[wid];
+    TileBox &box = s_box[wid];
+    const unsigned lt = (1u << lane) - 1u;
+    const GridParams g = st->grid;
+    constexpr float FAR = 1e30f;
+    unsigned long long c_tests = 0, c_slots = 0, c_hits = 0;
+    for (;;) {
+        unsigned long long c0 = 0;
+        if (lane == 0) c0 = atomicAdd(&st->gather_next, 32ull);
+        c0 = __shfl_sync(0xffffffffu, c0, 0);
+        if (c0 >= (unsigned long long)nq) break;
+        const unsigned long long qi = c0 + lane;
+        const bool valid = qi < (unsigned long long)nq;
+        V3<float> n = mk3(0.f, 0.f, 0.f);
+        double r2 = 0.0;
+        float r2_lo = -1.0f, r2_hi = -1.0f, rad = 0.0f;
+        float4 mine = make_float4(FAR, FAR, FAR, 0.f);
+        if (valid) {
+            const HitPoint<float> h = load_hit(hits + qi);
+            r2 = r2s[qi];
+            r2_lo = __double2float_rd(r2 * (1.0 - 1e-6));
+            r2_hi = __double2float_ru(r2 * (1.0 + 1e-6));
+            rad = sqrtf(r2_hi) * 1.000001f;   // at least the radius
+            mine = make_float4(h.pos[0], h.pos[1], h.pos[2], rad);
+            n = ld3(h.nrm);
+        }
+        s_own[wid][lane] = mine;
+        unsigned long long t0 = 0, t1 = 0, t2 = 0;   // flux sums in 2^-23 units
+        // the chunk: compact enough to share one walk?
+        float lox = mine.x, loy = mine.y, loz = mine.z;
+        float hix = valid ? mine.x : -FAR, hiy = valid ? mine.y : -FAR, hiz = valid ? mine.z : -FAR;
+        float rmax = rad, vsum = valid ? 8.0f * rad * rad * rad : 0.0f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lox = fminf(lox, __shfl_xor_sync(0xffffffffu, lox, o));
+            loy = fminf(loy, __shfl_xor_sync(0xffffffffu, loy, o));
+            loz = fminf(loz, __shfl_xor_sync(0xffffffffu, loz, o));
+            hix = fmaxf(hix, __shfl_xor_sync(0xffffffffu, hix, o));
+            hiy = fmaxf(hiy, __shfl_xor_sync(0xffffffffu, hiy, o));
+            hiz = fmaxf(hiz, __shfl_xor_sync(0xffffffffu, hiz, o));
+            rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+            vsum += __shfl_xor_sync(0xffffffffu, vsum, o);
+        }
+        const float vunion = (hix - lox + 2.0f * rmax) * (hiy - loy + 2.0f * rmax) * (hiz - loz + 2.0f * rmax);
+        unsigned pending = __ballot_sync(0xffffffffu, valid);
+        __syncwarp();
+        if (vunion <= EST_TILE_RATIO * vsum) {
+            while (pending) {
+                // the group: pending lanes within 2 rmax of the leader on every axis
+                const int leader = __ffs(pending) - 1;
+                const float4 own = mine, ld = s_own[wid][leader];
+                const float reach = 2.0f * rmax;
+                const bool member = ((pending >> lane) & 1u) && fabsf(own.x - ld.x) <= reach &&
+                                    fabsf(own.y - ld.y) <= reach && fabsf(own.z - ld.z) <= reach;
+                pending &= ~__ballot_sync(0xffffffffu, member);
+                const V3<float> q = member ? mk3(own.x, own.y, own.z) : mk3(FAR, FAR, FAR);
+                {
+                    V3<float> lo = q, hi = member ? q : mk3(-FAR, -FAR, -FAR);
+                    float gr = member ? own.w : 0.0f;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        lo.x = fminf(lo.x, __shfl_xor_sync(0xffffffffu, lo.x, o));
+                        lo.y = fminf(lo.y, __shfl_xor_sync(0xffffffffu, lo.y, o));
+                        lo.z = fminf(lo.z, __shfl_xor_sync(0xffffffffu, lo.z, o));
+                        hi.x = fmaxf(hi.x, __shfl_xor_sync(0xffffffffu, hi.x, o));
+                        hi.y = fmaxf(hi.y, __shfl_xor_sync(0xffffffffu, hi.y, o));
+                        hi.z = fmaxf(hi.z, __shfl_xor_sync(0xffffffffu, hi.z, o));
+                        gr = fmaxf(gr, __shfl_xor_sync(0xffffffffu, gr, o));
+                    }
+                    if (lane == 0) {
+                        // cells a radius gr can span (as the per-query walk's ext)
+                        const int ext = min(g.ext, max(1, (int)ceilf(gr * g.invf + 3e-3f)));
+                        const int extx = min(g.extx, max(1, (int)ceilf(gr * g.invxf + 3e-3f)));
+                        box.lo[0] = lo.x; box.lo[1] = lo.y; box.lo[2] = lo.z;
+                        box.hi[0] = hi.x; box.hi[1] = hi.y; box.hi[2] = hi.z;
+                        box.r2 = gr * gr;
+                        box.cx0 = max(CellMath<float>::coord(g, lo.x, 0) - extx, 0);
+                        box.cx1 = min(CellMath<float>::coord(g, hi.x, 0) + extx, g.dim[0] - 1);
+                        box.cy0 = max(CellMath<float>::coord(g, lo.y, 1) - ext, 0);
+                        const int cy1 = min(CellMath<float>::coord(g, hi.y, 1) + ext, g.dim[1] - 1);
+                        box.cz0 = max(CellMath<float>::coord(g, lo.z, 2) - ext, 0);
+                        const int cz1 = min(CellMath<float>::coord(g, hi.z, 2) + ext, g.dim[2] - 1);
+                        box.ny = cy1 - box.cy0 + 1;
+                        box.nrows = box.ny * (cz1 - box.cz0 + 1);
+                    }
+                    __syncwarp();
+                }
+                const int nrows = box.nrows;
+                for (int row0 = 0; row0 < nrows; row0 += 32) {
+                    uint32_t rbeg = 0, rlen = 0;
+                    const int row = row0 + (int)lane;
+                    if (row < nrows) {
+                        const int ny = box.ny;
+                        const int zz = box.cz0 + row / ny, yy = box.cy0 + row % ny;
+                        int x0, x1;
+                        if (box_row_range(g, mk3(box.lo[0], box.lo[1], box.lo[2]), mk3(box.hi[0], box.hi[1], box.hi[2]),
+                                          box.r2, yy, zz, box.cx0, box.cx1, x0, x1)) {
+                            const int base = (zz * g.dim[1] + yy) * g.dim[0];
+                            rbeg = start[3 * (base + x0)];
+                            rlen = start[3 * (base + x1 + 1)] - rbeg;
+                        }
+                    }
+                    uint32_t incl = rlen;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= (unsigned)o) incl += u;
+                    }
+                    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+                    const uint32_t excl = incl - rlen;
+                    for (uint32_t b0 = 0; b0 < total; b0 += 32) {
+                        const uint32_t j = b0 + lane;
+                        int r = 0;
+#pragma unroll
+                        for (int step = 16; step > 0; step >>= 1)
+                            if (__shfl_sync(0xffffffffu, incl, r + step - 1) <= j) r += step;
+                        const uint32_t rb = __shfl_sync(0xffffffffu, rbeg, r), rx = __shfl_sync(0xffffffffu, excl, r);
+                        const bool v = j < total;
+                        uint32_t wl = 3u;
+                        float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pd = pa;
+                        if (v) {
+                            const uint32_t slot = rb + (j - rx);
+                            const float4 p = __ldg(&smap[slot]);
+                            const uint32_t m = __float_as_uint(p.w);
+                            float inv;
+                            const V3<float> d = oct_raw(m, inv);
+                            pa = make_float4(p.x, p.y, p.z, 0.f);
+                            pd = make_float4(-d.x * inv, -d.y * inv, -d.z * inv, 0.f);
+                            wl = min(m >> 30, 2u);
+                        }
+                        const unsigned m0 = __ballot_sync(0xffffffffu, wl == 0u), m1 = __ballot_sync(0xffffffffu, wl == 1u),
+                                       m2 = __ballot_sync(0xffffffffu, wl == 2u);
+                        const int n0 = __popc(m0), n01 = n0 + __popc(m1), nv = n01 + __popc(m2);
+                        if (v) {
+                            const int at = wl == 0u ? __popc(m0 & lt) : (wl == 1u ? n0 + __popc(m1 & lt) : n01 + __popc(m2 & lt));
+                            sp[at] = pa;
+                            sd[at] = pd;
+                        }
+                        __syncwarp();
+                        bool band = false;
+                        auto sweep = [&](auto exact, int ta, int tb) -> uint32_t {
+                            constexpr bool EXACT = decltype(exact)::value;
+                            uint32_t acc = 0u;
+#pragma unroll 2
+                            for (int t = ta; t < tb; t++) {
+                                const float4 a = sp[t], b = sd[t];
+                                const float dx = q.x - a.x, dy = q.y - a.y, dz = q.z - a.z;
+                                const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                                bool in = d2 < r2_lo;
+                                const bool bd = !in && d2 <= r2_hi;
+                                if constexpr (EXACT) {
+                                    if (bd) in = sq_euclid(f2d_here(q.x), f2d_here(q.y), f2d_here(q.z), (double)a.x,
+                                                           (double)a.y, (double)a.z) <= r2;
+                                    if (COUNT && in) c_hits += 1;
+                                } else {
+                                    band |= bd;
+                                }
+                                const float c = __fmaf_rn(n.z, b.z, __fmaf_rn(n.y, b.y, n.x * b.x));
+                                acc += fix_bits(in ? fmaxf(c, 0.0f) : 0.0f) - FIX_BIAS;
+                            }
+                            return acc;
+                        };
+                        uint32_t a0 = sweep(std::false_type{}, 0, n0);
+                        uint32_t a1 = sweep(std::false_type{}, n0, n01);
+                        uint32_t a2 = sweep(std::false_type{}, n01, nv);
+                        if (__any_sync(0xffffffffu, band) || COUNT) {
+                            a0 = sweep(std::true_type{}, 0, n0);
+                            a1 = sweep(std::true_type{}, n0, n01);
+                            a2 = sweep(std::true_type{}, n01, nv);
+                        }
+                        t0 += a0;
+                        t1 += a1;
+                        t2 += a2;
+                        if (COUNT) {
+                            c_tests += member ? (unsigned long long)nv : 0ull;
+                            c_slots += (unsigned long long)nv;
+                        }
+                        __syncwarp();
+                    }
+                }
+            }
+        } else {
+            // one query after another, the warp's lanes striding through its rows
+            while (pending) {
+                const int l = __ffs(pending) - 1;
+                pending &= pending - 1;
+                const float4 ql4 = s_own[wid][l];
+                const V3<float> q = mk3(ql4.x, ql4.y, ql4.z);
+                const V3<float> nl = mk3(__shfl_sync(0xffffffffu, n.x, l), __shfl_sync(0xffffffffu, n.y, l),
+                                         __shfl_sync(0xffffffffu, n.z, l));
+                const double r2l = __shfl_sync(0xffffffffu, r2, l);
+                const float lo2 = __shfl_sync(0xffffffffu, r2_lo, l), hi2 = __shfl_sync(0xffffffffu, r2_hi, l);
+                const float rl = ql4.w;
+                const int ext = min(g.ext, max(1, (int)ceilf(rl * g.invf + 3e-3f)));
+                const int extx = min(g.extx, max(1, (int)ceilf(rl * g.invxf + 3e-3f)));
+                int c[3], lo[3], hi[3];
+                query_cells(g, q, ext, extx, c, lo, hi);
+                unsigned long long u0 = 0, u1 = 0, u2 = 0;
+                for_each_candidate(g, start, q, rl * rl, lo, hi, [&](uint32_t idx, bool valid2) {
+                    const float4 p = __ldg(&smap[idx]);
+                    const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+                    const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                    bool in = valid2 && d2 < lo2;
+                    const bool bd = valid2 && !in && d2 <= hi2;
+                    if (__any_sync(0xffffffffu, bd))
+                        if (bd) in = sq_euclid(f2d_here(q.x), f2d_here(q.y), f2d_here(q.z), (double)p.x, (double)p.y,
+                                               (double)p.z) <= r2l;
+                    const uint32_t m = __float_as_uint(p.w);
+                    float inv;
+                    const V3<float> d = oct_raw(m, inv);
+                    const float bx = -d.x * inv, by = -d.y * inv, bz = -d.z * inv;
+                    const float cc = __fmaf_rn(nl.z, bz, __fmaf_rn(nl.y, by, nl.x * bx));
+                    const uint32_t term = fix_bits(in ? fmaxf(cc, 0.0f) : 0.0f) - FIX_BIAS;
+                    const uint32_t w = m >> 30;
+                    u0 += w == 0u ? term : 0u;
+                    u1 += w == 1u ? term : 0u;
+                    u2 += w >= 2u ? term : 0u;
+                    if (COUNT) {
+                        c_slots += 1;
+                        c_tests += valid2 ? 1 : 0;
+                        c_hits += in ? 1 : 0;
+                    }
+                });
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    u0 += __shfl_xor_sync(0xffffffffu, u0, o);
+                    u1 += __shfl_xor_sync(0xffffffffu, u1, o);
+                    u2 += __shfl_xor_sync(0xffffffffu, u2, o);
+                }
+                if ((int)lane == l) { t0 = u0; t1 = u1; t2 = u2; }
+            }
+        }
+        if (valid) {
+            // the query's slot in the caller's arrays is its pixel field
+            const int32_t dst = hits[qi].pixel;
+            const double kk = FIX_UNIT * (pw * (ONE_PI_D / r2));
+            double *o = out.out_rgb + 3 * (size_t)dst;
+            o[0] = (double)t0 * kk;
+            o[1] = (double)t1 * kk;
+            o[2] = (double)t2 * kk;
+        }
+        __syncwarp();   // s_own is rewritten by the next chunk
+    }
+    if (COUNT) {
+        for (int o = 16; o > 0; o >>= 1) {
+            c_tests += __shfl_xor_sync(0xffffffffu, c_tests, o);
+            c_hits += __shfl_xor_sync(0xffffffffu, c_hits, o);
+            c_slots += __shfl_xor_sync(0xffffffffu, c_slots, o);
+        }
+        if (lane == 0) {
+            atomicAdd(out.count + 0, c_tests);
+            atomicAdd(out.count + 1, c_hits);
+            atomicAdd(out.count + 2, c_slots);
+        }
+    }
+}
+
 // Estimate queries are gathered in the map's cell order, so that the warps
 // running at the same time walk the same cells and share photons in L2
 // (random query order re-reads the map from HBM once per neighbourhood).
 // k_query_hist ranks each query inside its cell (key 3*cell, the map's key
 // space, so the map's scan sizes apply); k_query_place writes the hit point
 // and its radius to the sorted slot, keeping the caller's index in pixel.
-__global__ void __launch_bounds__(256) k_query_hist(const float *pos, long long n, const PassState *st,
-                                                    uint32_t *count, uint2 *keyrank) {
+// The key's wavelength slot holds the query's radius class (r^2 below
+// r2_a, below r2_b, the rest), so that inside a cell the queries are grouped
+// by size: 32 consecutive queries then have similar radii, which is what
+// lets k_estimate_tile share one walk among them.  Non-negative doubles
+// order as their bit patterns, so the classes take integer compares.
+__global__ void __launch_bounds__(256) k_query_hist(const float *pos, const double *r2, long long n,
+                                                    const PassState *st, double r2_a, double r2_b, uint32_t *count,
+                                                    uint2 *keyrank) {
     const GridParams g = st->grid;
+    const long long ba = __double_as_longlong(r2_a), bb = __double_as_longlong(r2_b);
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        uint32_t c = 3u * cell_of(g, ld3(pos + 3 * i));
+        const long long br = __double_as_longlong(r2[i]);
+        const uint32_t cls = br < ba ? 0u : (br < bb ? 1u : 2u);
+        const uint32_t c = 3u * cell_of(g, ld3(pos + 3 * i)) + cls;
         keyrank[i] = make_uint2(c, atomicAdd(&count[c], 1u));
     }
 }

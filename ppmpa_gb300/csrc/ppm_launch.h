@@ -59,14 +59,26 @@ void launch_gather_tile_f(const HitPoint<float> *hits, PassState *st, const floa
                           int pfilter, GatherOutF out, int grid, cudaStream_t s);
 // resident blocks per SM of the tile gather (its persistent grid is this x SMs)
 int gather_tile_blocks_per_sm();
+int estimate_tile_blocks_per_sm();
+// the hit points counting-sorted into Morton order of a 128^3 grid over their
+// bounds (k_hit_bounds, k_hit_key, scan of HIT_KEYS counts, k_hit_place);
+// count must hold HIT_KEYS zeros (the scan leaves it zeroed again)
+void launch_hit_sort_f(const HitPoint<float> *hits, PassState *st, uint32_t *count, uint32_t *block_sums,
+                       uint32_t *start, uint2 *keyrank, HitPoint<float> *sorted, int grid, cudaStream_t s);
+int kernels_per_hit_sort();
 void launch_within_f(const float *q, long long nq, const double *q_r2, const PassState *st, const float4 *smap,
                      const uint32_t *start, const int32_t *sidx, unsigned long long *counts,
                      const unsigned long long *offsets, int32_t *idx_out, int grid, cudaStream_t s);
 void launch_make_queries_f(const float *pos, const float *nrm, long long n, HitPoint<float> *hits, cudaStream_t s);
 // sorts estimate queries by map cell (count -> scan -> place); count is left zeroed
+// (key: the map cell and a radius class from r2max)
 void launch_query_sort_f(const float *pos, const float *nrm, const double *r2, long long n, PassState *st,
-                         uint32_t *count, uint32_t *block_sums, uint32_t *qstart, long long cell_cap, uint2 *keyrank,
-                         HitPoint<float> *hits, double *r2_sorted, int grid, cudaStream_t s);
+                         double r2max, uint32_t *count, uint32_t *block_sums, uint32_t *qstart, long long cell_cap,
+                         uint2 *keyrank, HitPoint<float> *hits, double *r2_sorted, int grid, cudaStream_t s);
+// the estimate entry point's gather over the sorted queries (k_estimate_tile)
+void launch_estimate_tile_f(const HitPoint<float> *hits, const double *r2s, long long nq, PassState *st,
+                            const float4 *smap, const uint32_t *start, double pw, GatherOutF out, int grid,
+                            cudaStream_t s);
 void launch_intersect_f(const SceneView<float> &sc, const double *rays, long long n, double *t, int32_t *obj,
                         cudaStream_t s);
 void launch_pack_photons_f(const float *pos, const float *dir, const uint8_t *wl, long long n, float4 *raw,
@@ -86,8 +98,10 @@ constexpr int SCAN_TILE = 4096;
 void launch_pass_begin(PassState *st, cudaStream_t s);
 void launch_grid_setup(PassState *st, double r2_override, cudaStream_t s);
 // grid: blocks of the two tile kernels (each loops over the pass's tiles)
+// fixed_keys >= 0: scan that many keys instead of the pass grid's (at most
+// 4096 * SCAN_TILE keys: k_scan_top holds 4096 tile sums)
 void launch_scan(uint32_t *count, const PassState *st, uint32_t *block_sums, uint32_t *start, long long cell_cap,
-                 cudaStream_t s, int grid);
+                 cudaStream_t s, int grid, long long fixed_keys = -1);
 void launch_accum(const double *pass_img, double *sum, long long n, cudaStream_t s);
 void launch_accum_mixed(const float *direct, const float *gathered, const PassState *st, double pw, double *pass_img,
                         double *sum, long long n, cudaStream_t s);
