@@ -37,16 +37,13 @@ void launch_eye_level_f(const SceneView<float> &sc, const DCamera<float> &cam, u
         k_eye_level<float, false><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
 }
 void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
-                     const uint32_t *start, double pw, const double *q_r2, int pfilter, GatherOutF out, int grid,
-                     cudaStream_t s) {
-#define PPM_GATHER(C, P) k_gather_f<C, P><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pw, q_r2, pfilter, out)
-    if (!q_r2 && out.dump)   // the render gather's parity export
-        k_gather_f<false, false, true><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pw, q_r2, pfilter, out);
-    else if (q_r2 && out.count) PPM_GATHER(true, true);
-    else if (q_r2) PPM_GATHER(false, true);
-    else if (out.count) PPM_GATHER(true, false);
-    else PPM_GATHER(false, false);
-#undef PPM_GATHER
+                     const uint32_t *start, int pfilter, GatherOutF out, int grid, cudaStream_t s) {
+    if (out.dump)   // the parity export
+        k_gather_f<false, true><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pfilter, out);
+    else if (out.count)
+        k_gather_f<true><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pfilter, out);
+    else
+        k_gather_f<false><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pfilter, out);
 }
 void launch_gather_tile_f(const HitPoint<float> *hits, PassState *st, const float4 *smap, const uint32_t *start,
                           int pfilter, GatherOutF out, int grid, cudaStream_t s) {

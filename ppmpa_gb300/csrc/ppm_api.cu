@@ -1466,7 +1466,7 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
                       ctx->gather_dump};
         if (ctx->cfg.flags & PPM_RENDER_ROW_WALK)
             launch_gather_f(as<HitPoint<float>>(ctx->hits_sorted), ctx->st, -1, as<float4>(ctx->sorted_f),
-                            as<uint32_t>(ctx->start), ctx->pw, nullptr, ctx->cam.pfilter, go, g8, s);
+                            as<uint32_t>(ctx->start), ctx->cam.pfilter, go, g8, s);
         else
             launch_gather_tile_f(as<HitPoint<float>>(ctx->hits_sorted), ctx->st, as<float4>(ctx->sorted_f),
                                  as<uint32_t>(ctx->start), ctx->cam.pfilter, go, grid_blocks(ctx, ctx->tile_blocks), s);

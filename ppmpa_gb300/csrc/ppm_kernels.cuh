@@ -758,38 +758,8 @@ __device__ __forceinline__ void for_each_candidate(const GridParams &g, const ui
     }
 }
 
-// The same walk for the FP32 gather, two candidates per lane per step: both
-// photons are loaded before either is used (two loads in flight per lane,
-// half the loop overhead).  Every lane makes every use(photon, valid) call
-// (the second call of a step is skipped by the whole warp when no lane has a
-// second photon), so use() may hold warp votes.
-template <typename T, typename U>
-__device__ __forceinline__ void for_each_candidate_pair(const GridParams &g, const uint32_t *start, V3<T> q, T r2,
-                                                        const int lo[3], const int hi[3], const float4 *smap,
-                                                        U &&use) {
-    const int nrows = (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
-    for (int row0 = 0; row0 < nrows; row0 += 32) {
-        RowSet rs = make_rows(g, start, q, r2, lo, hi, row0);
-        unsigned m = rs.nonempty;
-        while (m) {
-            int r = __ffs(m) - 1;
-            m &= m - 1;
-            const uint32_t b = __shfl_sync(0xffffffffu, rs.begin, r);
-            const uint32_t n = __shfl_sync(0xffffffffu, rs.len, r);
-            for (uint32_t base = 0; base < n; base += 64) {
-                const uint32_t o0 = base + lane_id(), o1 = o0 + 32;
-                const bool v0 = o0 < n, v1 = o1 < n;
-                const float4 p0 = __ldg(&smap[v0 ? b + o0 : b]);
-                const float4 p1 = __ldg(&smap[v1 ? b + o1 : b]);
-                use(p0, v0);
-                if (base + 32 < n) use(p1, v1);
-            }
-        }
-    }
-}
-
-// The render gather's walk: the same steps as for_each_candidate_pair, with
-// a lane's two candidates handed to one call, use(two, p0, valid0, slot0,
+// The render row walk: the steps of for_each_candidate, two candidates per
+// lane per step (both loaded before either is used), handed to one call, use(two, p0, valid0, slot0,
 // p1, valid1, slot1), so that their radius tests and direction decodes form
 // two independent instruction chains in one block (one branch per step
 // instead of two).  A step over a row's last 32 or fewer candidates passes
@@ -1164,22 +1134,19 @@ __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, cons
 #endif
 
 #if defined(PPM_BUILD_F32)
-// PERQ: per-query radii (the estimate entry point); otherwise the pass radius.
-//
-// Warps take their queries from a counter, a few at a time, so the queries
-// in flight are a narrow window of the batch (which is in pixel or cell
-// order): neighbouring warps read the same photons, from L1 or L2, and a
-// slow warp does not hold up the rest.  The render takes 2 queries per
-// increment (measured best on the glass box: 0.402 ms against 0.406 for 1,
-// 0.410 for 4 and 0.43 for 8 or a fixed warp stride); the estimate entry
-// point, whose maps exceed L2, takes 4.  Five blocks per SM for the render
-// (at most 51 registers; it needs 46 without spilling) measured 1 % faster
-// than four; the estimate variants keep four.
-template <bool COUNT, bool PERQ, bool DUMP = false>
-__global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed,
-                                                  const float4 *smap, const uint32_t *start, double pw,
-                                                  const double *q_r2, int pfilter, GatherOutF out) {
-    constexpr unsigned CHUNK = PERQ ? 4u : 2u;
+// The render gather, row-walk form (PPM_RENDER_ROW_WALK): one warp per hit
+// point, or per two hit points of one cell (gather_pair).  Warps take their
+// hit points from a counter, two at a time, so the hit points in flight are
+// a narrow window of the (spatially sorted) list: neighbouring warps read the
+// same photons, from L1 or L2, and a slow warp does not hold up the rest
+// (measured on the glass box: 0.402 ms against 0.406 for 1, 0.410 for 4 and
+// 0.43 for 8 or a fixed warp stride).  Five blocks per SM (at most 51
+// registers; it needs 46 without spilling) measured 1 % faster than four.
+template <bool COUNT, bool DUMP = false>
+__global__ void __launch_bounds__(256, 5) k_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed,
+                                                     const float4 *smap, const uint32_t *start, int pfilter,
+                                                     GatherOutF out) {
+    constexpr unsigned CHUNK = 2u;
     const unsigned long long nq = n_hitpoints(st, n_fixed);
     const GridParams g = st->grid;
     const unsigned lane = lane_id();
@@ -1193,42 +1160,24 @@ __global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<f
             qi = c;
             qend = c + CHUNK < nq ? c + CHUNK : nq;
         }
-        if constexpr (!PERQ) {
-            if (qend - qi == 2 && gather_pair<COUNT, DUMP>(g, st->r2, hits + qi, start, smap, pfilter, out, qi)) {
-                qi += 2;
-                continue;
-            }
+        if (qend - qi == 2 && gather_pair<COUNT, DUMP>(g, st->r2, hits + qi, start, smap, pfilter, out, qi)) {
+            qi += 2;
+            continue;
         }
         const HitPoint<float> h = load_hit(hits + qi);
-        double r2;
-        float r2_lo, r2_hi, r2f;
-        int ext = g.ext, extx = g.extx;
-        if constexpr (PERQ) {
-            r2 = q_r2[qi];
-            r2_lo = __double2float_rd(r2 * (1.0 - 1e-6));
-            r2_hi = __double2float_ru(r2 * (1.0 + 1e-6));
-            r2f = (float)r2;
-            ext = min(g.ext, max(1, (int)ceil(sqrt(r2) * g.inv + 3e-3)));
-            extx = min(g.extx, max(1, (int)ceil(sqrt(r2) * g.invx + 3e-3)));
-        } else {
-            r2 = st->r2;
-            r2_lo = g.r2_lo;
-            r2_hi = g.r2_hi;
-            r2f = g.r2f;
-        }
+        const double r2 = st->r2;
+        const float r2_lo = g.r2_lo, r2_hi = g.r2_hi, r2f = g.r2f;
         V3<float> q = ld3(h.pos), n = ld3(h.nrm);
         int c[3], lo[3], hi[3];
-        query_cells(g, q, ext, extx, c, lo, hi);
-        // Per-lane sums: compensated (Kahan) for the estimate entry point
-        // (PERQ), whose queries can gather thousands of photons per lane;
-        // plain for the render, where a lane adds a few dozen terms (relative
-        // error < 1e-6) and the three sums take the photon's value or zero
-        // without a branch on its wavelength.
-        Kahan k0 = {0.f, 0.f}, k1 = {0.f, 0.f}, k2 = {0.f, 0.f};
+        query_cells(g, q, g.ext, g.extx, c, lo, hi);
+        // Per-lane sums: a lane adds a few dozen terms (relative error <
+        // 1e-6), and the three sums take the photon's value or zero without
+        // a branch on its wavelength.
+        float k0 = 0.f, k1 = 0.f, k2 = 0.f;
         unsigned long long c_slots = 0, c_valid = 0, c_hits = 0;
         uint32_t d_in = 0;             // export only
         unsigned long long d_hash = 0;   // export only
-        if constexpr (!PERQ) {
+        {
             for_each_candidate_two(g, start, q, r2f, lo, hi, smap,
                                    [&](auto two, float4 p0, bool v0, uint32_t i0, float4 p1, bool v1, uint32_t i1) {
                 constexpr bool TWO = decltype(two)::value;
@@ -1267,13 +1216,13 @@ __global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<f
                     }
                     const uint32_t l0 = m0 >> 30, l1 = m1 >> 30;
                     if constexpr (TWO) {
-                        k0.s += (l0 == 0u ? w0 : 0.0f) + (l1 == 0u ? w1 : 0.0f);
-                        k1.s += (l0 == 1u ? w0 : 0.0f) + (l1 == 1u ? w1 : 0.0f);
-                        k2.s += (l0 >= 2u ? w0 : 0.0f) + (l1 >= 2u ? w1 : 0.0f);
+                        k0 += (l0 == 0u ? w0 : 0.0f) + (l1 == 0u ? w1 : 0.0f);
+                        k1 += (l0 == 1u ? w0 : 0.0f) + (l1 == 1u ? w1 : 0.0f);
+                        k2 += (l0 >= 2u ? w0 : 0.0f) + (l1 >= 2u ? w1 : 0.0f);
                     } else {
-                        k0.s += l0 == 0u ? w0 : 0.0f;
-                        k1.s += l0 == 1u ? w0 : 0.0f;
-                        k2.s += l0 >= 2u ? w0 : 0.0f;
+                        k0 += l0 == 0u ? w0 : 0.0f;
+                        k1 += l0 == 1u ? w0 : 0.0f;
+                        k2 += l0 >= 2u ? w0 : 0.0f;
                     }
                     if (COUNT) c_hits += (int)in0 + (int)in1;
                     if (DUMP) {
@@ -1282,34 +1231,8 @@ __global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<f
                     }
                 }
             });
-        } else {
-            for_each_candidate_pair(g, start, q, r2f, lo, hi, smap, [&](float4 pp, bool valid) {
-                if (COUNT) {
-                    c_slots += 1;
-                    c_valid += valid;
-                }
-                // in_radius_f32, with the FP64 recheck behind a warp vote (see the render walk)
-                const float dx = q.x - pp.x, dy = q.y - pp.y, dz = q.z - pp.z;
-                const float d2f = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                bool in = valid && d2f < r2_lo;
-                const bool band = valid && !in && d2f <= r2_hi;
-                if (__any_sync(0xffffffffu, band))
-                    if (band) in = sq_euclid(f2d_here(q.x), f2d_here(q.y), f2d_here(q.z), (double)pp.x, (double)pp.y,
-                                             (double)pp.z) <= r2;
-                if (in) {
-                    uint32_t m = __float_as_uint(pp.w);
-                    float cos0 = oct_dot(m, n);
-                    float val = cos0 < 0.0f ? -cos0 : 0.0f;
-                    if (pfilter != PF_NONE) val *= filter_wt_f(pfilter, d2f, r2f);
-                    const uint32_t wl = m >> 30;
-                    if (wl == 0u) k0.add(val);
-                    else if (wl == 1u) k1.add(val);
-                    else k2.add(val);
-                    if (COUNT) c_hits += 1;
-                }
-            });
         }
-        float s0 = warp_sum(k0.s - k0.c), s1 = warp_sum(k1.s - k1.c), s2 = warp_sum(k2.s - k2.c);
+        const float s0 = warp_sum(k0), s1 = warp_sum(k1), s2 = warp_sum(k2);
         if (COUNT) {
             for (int o = 16; o > 0; o >>= 1) {
                 c_slots += __shfl_xor_sync(0xffffffffu, c_slots, o);
@@ -1330,22 +1253,12 @@ __global__ void __launch_bounds__(256, PERQ ? 4 : 5) k_gather_f(const HitPoint<f
             if (lane == 0) out.dump[qi] = GatherDump{{s0, s1, s2}, d_in, d_hash};
         }
         if (lane == 0) {
-            if constexpr (!PERQ) {
-                // FP32 only here: an FP64 instruction costs a warp-wide slot of
-                // the narrow FP64 pipe even with one active lane
-                float *px = out.gathered + 3 * (size_t)h.pixel;
-                atomicAdd(px, h.w[0] * s0);
-                atomicAdd(px + 1, h.w[1] * s1);
-                atomicAdd(px + 2, h.w[2] * s2);
-            } else {
-                // the estimate entry point gathers its queries in cell order;
-                // h.pixel is the query's slot in the caller's arrays
-                double kk = pw * (ONE_PI_D / r2);
-                double *o = out.out_rgb + 3 * (size_t)h.pixel;
-                o[0] = (double)s0 * kk;
-                o[1] = (double)s1 * kk;
-                o[2] = (double)s2 * kk;
-            }
+            // FP32 only here: an FP64 instruction costs a warp-wide slot of
+            // the narrow FP64 pipe even with one active lane
+            float *px = out.gathered + 3 * (size_t)h.pixel;
+            atomicAdd(px, h.w[0] * s0);
+            atomicAdd(px + 1, h.w[1] * s1);
+            atomicAdd(px + 2, h.w[2] * s2);
         }
         qi += 1ull;
     }

@@ -46,13 +46,10 @@ void launch_eye_level_f(const SceneView<float> &sc, const DCamera<float> &cam, u
                         int level, EyeQueue<float> in, EyeQueue<float> out, unsigned long long qcap,
                         HitPoint<float> *hits, EyeOut<float> pix, int grid, cudaStream_t s,
                         bool classic = false);
-// per-query radii (q_r2) always take queries from the counter; otherwise dyn
-// chooses it (maps larger than L2)
-// q_r2 null: the render (pass radius, FP32 sums into out.gathered);
-// otherwise the estimate entry point (per-query radii, FP64 radiance into out.out_rgb)
+// the render gather, row-walk form (k_gather_f): out.count / out.dump select
+// the counting and the parity-export variants
 void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
-                     const uint32_t *start, double pw, const double *q_r2, int pfilter, GatherOutF out, int grid,
-                     cudaStream_t s);
+                     const uint32_t *start, int pfilter, GatherOutF out, int grid, cudaStream_t s);
 // the render gather, tile form (k_gather_tile): 32 hit points per warp;
 // out.count / out.dump select the counting and the parity-export variants
 void launch_gather_tile_f(const HitPoint<float> *hits, PassState *st, const float4 *smap, const uint32_t *start,
