@@ -121,14 +121,14 @@ typedef struct ppm_render_cfg {
     int32_t schedule_offset;  /* 1: iterator.rb:33-38; 0: radius.rb / averager.rb */
     int32_t precision;        /* PPM_PRECISION_* */
     int32_t use_graph;        /* capture one pass as a CUDA graph and replay it */
-    int32_t cell_factor;      /* grid cells per radius (1 or 2; 0 = auto) */
+    int32_t cell_factor;      /* grid cells per radius (1 to 4; 0 = auto) */
     uint64_t seed;
     int32_t first_pass;       /* index of the first pass (for sharded/resumed runs) */
     int32_t flags;            /* PPM_RENDER_* bits; others must be 0 */
 } ppm_render_cfg;
 
 /* Render flags.  PPM_RENDER_TUNE_CELLS: pick the photon-map cells per radius
- * (1 or 2) by timing one trial pass with each before the render starts; the
+ * (1 to 4) by timing one trial pass with each before the render starts; the
  * trial passes leave no trace in the image.  No reference counterpart. */
 enum { PPM_RENDER_TUNE_CELLS = 1,
 /* PPM_RENDER_CLASSIC: the reference's classic ray tracer trace_ray_classic

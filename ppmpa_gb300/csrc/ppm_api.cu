@@ -35,6 +35,7 @@ constexpr int TIMING_SLOTS = 256;
 constexpr int HITS_PER_PIXEL = 8;
 constexpr long long CELL_CAP = 1LL << 24;
 constexpr int BVH_MIN_OBJECTS = 32;   // below this a loop over the objects is faster
+constexpr int MAX_CELL_FACTOR = 4;    // render grids: 1 to 4 cells per radius (the tuner tries each)
 
 thread_local std::string g_create_error;
 
@@ -1499,8 +1500,8 @@ static double schedule_r2(const ppm_render_cfg &c, int upto) {
     return r;
 }
 
-// Grid cell autotuner of a render: one untimed and two timed passes with 1
-// and with 2 cells per radius at the render's middle pass (the captured pass
+// Grid cell autotuner of a render: one untimed and two timed passes with each
+// of 1 to MAX_CELL_FACTOR cells per radius at the render's middle pass (the captured pass
 // graph, which reads the cell factor from the device state, or eager passes
 // without a graph); the faster wins.  The trial passes write
 // only buffers that the caller's render then resets (state, pass and sum
@@ -1516,7 +1517,7 @@ static int tune_cells(ppm_ctx *ctx, const ppm_render_cfg &cfg, long long cap, in
     const int trial = cfg.first_pass + cfg.passes / 2;
     float best_ms = 1e30f;
     int rc = PPM_OK;
-    for (int k = 1; k <= 2 && rc == PPM_OK; k++) {
+    for (int k = 1; k <= MAX_CELL_FACTOR && rc == PPM_OK; k++) {
         float total = 0.0f;
         for (int rep = 0; rep < 3 && rc == PPM_OK; rep++) {   // one warm-up, two timed passes
             rc = upload_state(ctx, schedule_r2(cfg, trial), trial, cfg.alpha, cfg.schedule_offset, (double)k, cap,
@@ -1551,7 +1552,7 @@ extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
     if (!ctx->have_scene || !ctx->have_cam || ctx->lights.empty())
         return set_err(ctx, PPM_ERR_NOT_READY, "scene (with lights) and camera must be set first");
     if (cfg->nphoton <= 0 || cfg->passes < 0 || !(cfg->radius0 > 0.0) || cfg->precision < 0 || cfg->precision > 1 ||
-        cfg->cell_factor < 0 || cfg->cell_factor > 2 || cfg->first_pass < 0 ||
+        cfg->cell_factor < 0 || cfg->cell_factor > MAX_CELL_FACTOR || cfg->first_pass < 0 ||
         (cfg->flags & ~(PPM_RENDER_TUNE_CELLS | PPM_RENDER_CLASSIC | PPM_RENDER_ROW_WALK)))
         return set_err(ctx, PPM_ERR_INVALID_ARG, "bad render configuration");
     cudaSetDevice(ctx->device);
