@@ -46,13 +46,19 @@ void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fix
         k_gather_f<false><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pfilter, out);
 }
 void launch_gather_tile_f(const HitPoint<float> *hits, PassState *st, const float4 *smap, const uint32_t *start,
-                          int pfilter, GatherOutF out, int grid, cudaStream_t s) {
-#define PPM_TILE(C, D, F) k_gather_tile<C, D, F><<<grid, 32 * GATHER_TILE_WARPS, 0, s>>>(hits, st, smap, start, out)
-#define PPM_TILE_F(C, D)                                      \
-    do {                                                      \
-        if (pfilter == PF_CONE) PPM_TILE(C, D, PF_CONE);      \
+                          int pfilter, TileItem *items, unsigned long long cap, GatherOutF out, int grid,
+                          cudaStream_t s) {
+    const TileQueue q{items, cap};
+#define PPM_TILE(C, D, F)                                                                                   \
+    do {                                                                                                    \
+        k_gather_tile<C, D, F><<<grid, 32 * GATHER_TILE_WARPS, 0, s>>>(hits, st, smap, start, q, out);       \
+        k_gather_tile_items<C, D, F><<<grid, 32 * GATHER_TILE_WARPS, 0, s>>>(hits, st, smap, start, q, out); \
+    } while (0)
+#define PPM_TILE_F(C, D)                                        \
+    do {                                                        \
+        if (pfilter == PF_CONE) PPM_TILE(C, D, PF_CONE);        \
         else if (pfilter == PF_GAUSS) PPM_TILE(C, D, PF_GAUSS); \
-        else PPM_TILE(C, D, PF_NONE);                         \
+        else PPM_TILE(C, D, PF_NONE);                           \
     } while (0)
     if (out.dump) PPM_TILE_F(false, true);
     else if (out.count) PPM_TILE_F(true, false);
@@ -68,6 +74,7 @@ void launch_hit_sort_f(const HitPoint<float> *hits, PassState *st, uint32_t *cou
     k_hit_place<<<grid, 256, 0, s>>>(hits, st, keyrank, start, sorted);
 }
 int kernels_per_hit_sort() { return 3 + kernels_per_scan(); }
+int kernels_per_tile_gather() { return 2; }
 void launch_estimate_tile_f(const HitPoint<float> *hits, const double *r2s, long long nq, PassState *st,
                             const float4 *smap, const uint32_t *start, double pw, GatherOutF out, int grid,
                             cudaStream_t s) {

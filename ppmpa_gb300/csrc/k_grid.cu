@@ -17,6 +17,8 @@ __global__ void k_pass_begin(PassState *st) {
     st->slots = 0;
     st->rows = 0;
     st->gather_next = 0;
+    st->tile_items = 0;
+    st->tile_next = 0;
     st->emit_next = 0;
     st->photon_rays = 0;
     for (int l = 0; l < MAX_TRACE + 2; l++) st->eq[l] = 0;

@@ -84,6 +84,8 @@ struct ppm_ctx {
     // the mixed render's hit points in Morton order (the gathers' input):
     // sorted copy, key/rank per hit point, key counts, starts, scan tile sums
     DevBuf hits_sorted, hkeyrank, hcount, hstart, hblock;
+    DevBuf tile_queue;                     // the tile gather's queue of split walks
+    unsigned long long tile_cap = 0;       // its entries
     GatherDump *gather_dump = nullptr;     // set while the export pass is enqueued
     long long npx = 0;
     DevBuf scratch;   // parity entry-point staging
@@ -386,6 +388,10 @@ static int ensure_hit_sort(ppm_ctx *ctx) {
     }
     TRY(ensure(ctx, ctx->hstart, sizeof(uint32_t) * (HIT_KEYS + 1)));
     TRY(ensure(ctx, ctx->hblock, sizeof(uint32_t) * (HIT_KEYS / SCAN_TILE + 1)));
+    // split walks: up to 8 per chunk of 32 hit points (a full queue only
+    // means the warps walk the rest themselves)
+    ctx->tile_cap = std::max(1024ULL, (unsigned long long)ctx->hit_cap / 4);
+    TRY(ensure(ctx, ctx->tile_queue, sizeof(TileItem) * (size_t)ctx->tile_cap));
     return PPM_OK;
 }
 
@@ -521,7 +527,8 @@ extern "C" int ppm_ctx_destroy(ppm_ctx *ctx) {
                       &ctx->keyrank, &ctx->count, &ctx->start, &ctx->block_sums, &ctx->hits_d, &ctx->hits_f,
                       &ctx->pass_img, &ctx->sum_img, &ctx->scratch, &ctx->pass_direct32, &ctx->pass_gather32,
                       &ctx->qstart, &ctx->bvh_nodes, &ctx->bvh_bounded, &ctx->bvh_unb, &ctx->bvh_order,
-                      &ctx->gdump, &ctx->hits_sorted, &ctx->hkeyrank, &ctx->hcount, &ctx->hstart, &ctx->hblock};
+                      &ctx->gdump, &ctx->hits_sorted, &ctx->hkeyrank, &ctx->hcount, &ctx->hstart, &ctx->hblock,
+                      &ctx->tile_queue};
     for (DevBuf *b : bufs) release(*b);
     for (DevBuf &b : ctx->eqb) release(b);
     if (ctx->st) cudaFree(ctx->st);
@@ -1465,12 +1472,15 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
     if (mixed) {
         GatherOutF go{as<float>(ctx->pass_gather32), nullptr, ctx->count_gather ? &ctx->st->candidates : nullptr,
                       ctx->gather_dump};
-        if (ctx->cfg.flags & PPM_RENDER_ROW_WALK)
+        if (ctx->cfg.flags & PPM_RENDER_ROW_WALK) {
             launch_gather_f(as<HitPoint<float>>(ctx->hits_sorted), ctx->st, -1, as<float4>(ctx->sorted_f),
                             as<uint32_t>(ctx->start), ctx->cam.pfilter, go, g8, s);
-        else
+        } else {
             launch_gather_tile_f(as<HitPoint<float>>(ctx->hits_sorted), ctx->st, as<float4>(ctx->sorted_f),
-                                 as<uint32_t>(ctx->start), ctx->cam.pfilter, go, grid_blocks(ctx, ctx->tile_blocks), s);
+                                 as<uint32_t>(ctx->start), ctx->cam.pfilter, as<TileItem>(ctx->tile_queue),
+                                 ctx->tile_cap, go, grid_blocks(ctx, ctx->tile_blocks), s);
+            kernels += kernels_per_tile_gather() - 1;
+        }
     } else {
         GatherOutD go{as<double>(ctx->pass_img), nullptr, nullptr};
         launch_gather_d(as<HitPoint<double>>(ctx->hits_d), ctx->st, -1, as<double4>(ctx->spos), as<double4>(ctx->sdir),
@@ -1708,6 +1718,7 @@ extern "C" int ppm_render_gather_export(ppm_ctx *ctx, ppm_gather_export *ex) {
         ex->hit_cap < 0)
         return set_err(ctx, PPM_ERR_INVALID_ARG, "every export array is required");
     TRY(ensure(ctx, ctx->gdump, sizeof(GatherDump) * (size_t)ctx->hit_cap));
+    CK(cudaMemsetAsync(ctx->gdump.p, 0, sizeof(GatherDump) * (size_t)ctx->hit_cap, ctx->s));   // walks add into it
     PassState before;
     TRY(read_state(ctx, before));   // the exported pass's radius and index
     ctx->gather_dump = as<GatherDump>(ctx->gdump);

@@ -67,6 +67,8 @@ struct PassState {
     unsigned long long photon_rays;         // photon ray segments traced this pass (one per event)
     unsigned long long eq[MAX_TRACE + 2];   // eye-tree vertices at each depth
     uint32_t hb_lo[3], hb_hi[3];            // hit point bounds (orderable FP32 encodings)
+    unsigned long long tile_items;          // tile gather: items queued this pass
+    unsigned long long tile_next;           // and the next one to take
 };
 
 // number of valid photons / hit points (the counters keep counting past the
@@ -984,6 +986,22 @@ struct GatherOutF {
     GatherDump *dump;    // render parity export (null in the production render)
 };
 
+// a queued part of a tile gather walk (see k_gather_tile)
+struct TileItem {
+    uint32_t qi0, mask;   // the chunk's first hit point and the group's lanes
+    float lo[3], hi[3];   // the group's box
+    int32_t row0;         // the slab's first row
+    uint32_t b0, b1;      // its batches [b0, b1)
+    uint32_t pad;
+};
+static_assert(sizeof(TileItem) == 48, "queue item layout");
+
+struct TileQueue {
+    TileItem *items;
+    unsigned long long cap;
+};
+
+
 #if defined(PPM_BUILD_F32)
 // Two hit points of the render gather in one warp.  Consecutive hit points
 // are mostly neighbouring pixels, a few thousandths apart against radii of
@@ -1324,10 +1342,193 @@ struct TileBox {
     int cx0, cx1, cy0, cz0, ny, nrows;
 };
 
+// A group's walk is capped: the warp walks at most TILE_SPLIT batches of each
+// row slab of its group itself and queues the rest of the slab as items of
+// TILE_SPLIT batches, which k_gather_tile_items takes up after all chunks
+// are done.  A few dense chunks (caustics) hold far more photons than the
+// rest; uncapped, they decide when the launch ends.  Every walk adds its
+// part of a hit point's sums to the pixel with FP32 atomics (the estimate is
+// linear in the photons), so a split walk gives the same sums up to the
+// order of the additions.  A full queue is never an error: the warp then
+// walks the item itself.
+constexpr uint32_t TILE_SPLIT = 8;
+
+// per-lane counters of the counting and export variants
+struct TileCount {
+    uint32_t d_in = 0;
+    unsigned long long d_hash = 0, tests = 0, slots = 0, hits = 0;
+};
+
+// the box's cell ranges (one lane; box.lo / hi set)
+__device__ __forceinline__ void tile_box_cells(const GridParams &g, TileBox &box) {
+    box.cx0 = max(CellMath<float>::coord(g, box.lo[0], 0) - g.extx, 0);
+    box.cx1 = min(CellMath<float>::coord(g, box.hi[0], 0) + g.extx, g.dim[0] - 1);
+    box.cy0 = max(CellMath<float>::coord(g, box.lo[1], 1) - g.ext, 0);
+    const int cy1 = min(CellMath<float>::coord(g, box.hi[1], 1) + g.ext, g.dim[1] - 1);
+    box.cz0 = max(CellMath<float>::coord(g, box.lo[2], 2) - g.ext, 0);
+    const int cz1 = min(CellMath<float>::coord(g, box.hi[2], 2) + g.ext, g.dim[2] - 1);
+    box.ny = cy1 - box.cy0 + 1;
+    box.nrows = box.ny * (cz1 - box.cz0 + 1);
+}
+
+// Batches [b_begin, b_end) of the row slab that starts at row0 (32 rows of
+// the box, end to end); returns the slab's batch count.  Lanes outside the
+// group carry a far-away q.
+template <bool COUNT, bool DUMP, int FILTER>
+__device__ __forceinline__ uint32_t tile_walk(const GridParams &g, const TileBox &box, int row0, uint32_t b_begin,
+                                              uint32_t b_end, const uint32_t *start, const float4 *smap, float4 *sp,
+                                              float4 *sd, V3<float> q, V3<float> n, bool member, double r2, Kahan &k0,
+                                              Kahan &k1, Kahan &k2, TileCount &cn) {
+    const unsigned lane = lane_id(), lt = (1u << lane) - 1u;
+    const float r2f = g.r2f, r2_lo = g.r2_lo, r2_hi = g.r2_hi;
+    const int nrows = box.nrows;
+    uint32_t rbeg = 0, rlen = 0;
+    const int row = row0 + (int)lane;
+    if (row < nrows) {
+        const int ny = box.ny;
+        const int zz = box.cz0 + row / ny, yy = box.cy0 + row % ny;
+        int x0, x1;
+        if (box_row_range(g, mk3(box.lo[0], box.lo[1], box.lo[2]), mk3(box.hi[0], box.hi[1], box.hi[2]), r2f, yy, zz,
+                          box.cx0, box.cx1, x0, x1)) {
+            const int base = (zz * g.dim[1] + yy) * g.dim[0];
+            rbeg = start[3 * (base + x0)];
+            rlen = start[3 * (base + x1 + 1)] - rbeg;
+        }
+    }
+    uint32_t incl = rlen;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (unsigned)o) incl += u;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    const uint32_t excl = incl - rlen;
+    const uint32_t nb = (total + 31) / 32;
+    const uint32_t bend = b_end < nb ? b_end : nb;
+    for (uint32_t bi = b_begin; bi < bend; bi++) {
+        // this lane's photon: the row r with excl_r <= j < incl_r
+        const uint32_t j = bi * 32 + lane;
+        int r = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+            if (__shfl_sync(0xffffffffu, incl, r + step - 1) <= j) r += step;
+        const uint32_t rb = __shfl_sync(0xffffffffu, rbeg, r), rx = __shfl_sync(0xffffffffu, excl, r);
+        const bool v = j < total;
+        uint32_t wl = 3u;
+        float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pd = pa;
+        if (v) {
+            const uint32_t slot = rb + (j - rx);
+            const float4 p = __ldg(&smap[slot]);
+            const uint32_t m = __float_as_uint(p.w);
+            float inv;
+            const V3<float> d = oct_raw(m, inv);
+            pa = make_float4(p.x, p.y, p.z, __uint_as_float(slot));
+            pd = make_float4(-d.x * inv, -d.y * inv, -d.z * inv, 0.f);
+            wl = min(m >> 30, 2u);
+        }
+        // stage grouped by wavelength
+        const unsigned m0 = __ballot_sync(0xffffffffu, wl == 0u), m1 = __ballot_sync(0xffffffffu, wl == 1u),
+                       m2 = __ballot_sync(0xffffffffu, wl == 2u);
+        const int n0 = __popc(m0), n01 = n0 + __popc(m1), nv = n01 + __popc(m2);
+        if (v) {
+            const int at = wl == 0u ? __popc(m0 & lt) : (wl == 1u ? n0 + __popc(m1 & lt) : n01 + __popc(m2 & lt));
+            sp[at] = pa;
+            sd[at] = pd;
+        }
+        __syncwarp();
+        // the tests; EXACT re-decides band photons in FP64
+        bool band = false;
+        auto sweep = [&](auto exact, int t0, int t1) -> float {
+            constexpr bool EXACT = decltype(exact)::value;
+            float acc = 0.0f;
+#pragma unroll 2
+            for (int t = t0; t < t1; t++) {
+                const float4 a = sp[t], b = sd[t];
+                const float dx = q.x - a.x, dy = q.y - a.y, dz = q.z - a.z;
+                const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                bool in = d2 < r2_lo;
+                const bool bd = !in && d2 <= r2_hi;
+                if constexpr (EXACT) {
+                    if (bd) in = sq_euclid(f2d_here(q.x), f2d_here(q.y), f2d_here(q.z), (double)a.x, (double)a.y,
+                                           (double)a.z) <= r2;
+                } else {
+                    band |= bd;
+                }
+                const float c = __fmaf_rn(n.z, b.z, __fmaf_rn(n.y, b.y, n.x * b.x));
+                float w = in ? fmaxf(c, 0.0f) : 0.0f;
+                if constexpr (FILTER != PF_NONE) w *= in ? tile_filter<FILTER>(d2, r2f) : 0.0f;
+                acc += w;
+                if constexpr (EXACT && (DUMP || COUNT)) {
+                    if (in) {
+                        if (DUMP) { cn.d_in += 1u; cn.d_hash += slot_mix(__float_as_uint(a.w)); }
+                        if (COUNT) cn.hits += 1;
+                    }
+                }
+            }
+            return acc;
+        };
+        float a0 = sweep(std::false_type{}, 0, n0);
+        float a1 = sweep(std::false_type{}, n0, n01);
+        float a2 = sweep(std::false_type{}, n01, nv);
+        if (__any_sync(0xffffffffu, band) || DUMP || COUNT) {
+            // exact pass: the same tests with band photons re-decided in FP64
+            // (the export and the counters always take it, as they count members)
+            a0 = sweep(std::true_type{}, 0, n0);
+            a1 = sweep(std::true_type{}, n0, n01);
+            a2 = sweep(std::true_type{}, n01, nv);
+        }
+        k0.add(a0);
+        k1.add(a1);
+        k2.add(a2);
+        if (COUNT) {
+            cn.tests += member ? (unsigned long long)nv : 0ull;   // photon-hit point distance tests
+            cn.slots += (unsigned long long)nv;                   // lane slots the batch issued
+        }
+        __syncwarp();   // the next batch overwrites the stage
+    }
+    return nb;
+}
+
+// a member lane's sums into its pixel (and into its export record)
+template <bool DUMP>
+__device__ __forceinline__ void tile_flush(const HitPoint<float> *hits, unsigned long long qi, const Kahan &k0,
+                                           const Kahan &k1, const Kahan &k2, const TileCount &cn,
+                                           const GatherOutF &out) {
+    const float s0 = k0.s - k0.c, s1 = k1.s - k1.c, s2 = k2.s - k2.c;
+    const HitPoint<float> h = load_hit(hits + qi);
+    float *px = out.gathered + 3 * (size_t)h.pixel;
+    atomicAdd(px, h.w[0] * s0);
+    atomicAdd(px + 1, h.w[1] * s1);
+    atomicAdd(px + 2, h.w[2] * s2);
+    if (DUMP) {
+        GatherDump &d = out.dump[qi];
+        atomicAdd(&d.s[0], s0);
+        atomicAdd(&d.s[1], s1);
+        atomicAdd(&d.s[2], s2);
+        atomicAdd(&d.count, cn.d_in);
+        atomicAdd(&d.hash, cn.d_hash);
+    }
+}
+
+template <bool COUNT>
+__device__ __forceinline__ void tile_count_flush(TileCount &cn, const GatherOutF &out) {
+    if (!COUNT) return;
+    for (int o = 16; o > 0; o >>= 1) {
+        cn.tests += __shfl_xor_sync(0xffffffffu, cn.tests, o);
+        cn.hits += __shfl_xor_sync(0xffffffffu, cn.hits, o);
+        cn.slots += __shfl_xor_sync(0xffffffffu, cn.slots, o);
+    }
+    if (lane_id() == 0) {
+        atomicAdd(out.count + 0, cn.tests);
+        atomicAdd(out.count + 1, cn.hits);
+        atomicAdd(out.count + 2, cn.slots);
+    }
+}
+
 template <bool COUNT, bool DUMP, int FILTER>
 __global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_gather_tile(const HitPoint<float> *hits, PassState *st,
                                                                         const float4 *smap, const uint32_t *start,
-                                                                        GatherOutF out) {
+                                                                        TileQueue queue, GatherOutF out) {
     __shared__ float4 s_pos[GATHER_TILE_WARPS][32];   // x, y, z, map slot (export only)
     __shared__ float4 s_dir[GATHER_TILE_WARPS][32];   // -direction (unit)
     __shared__ float4 s_own[GATHER_TILE_WARPS][32];   // each lane's hit point position
@@ -1335,14 +1536,12 @@ __global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_gather_tile(const Hi
     const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
     float4 *const sp = s_pos[wid], *const sd = s_dir[wid];
     TileBox &box = s_box[wid];
-    const unsigned lt = (1u << lane) - 1u;
     const unsigned long long nq = n_hitpoints(st, -1);
     const GridParams g = st->grid;
     const double r2 = st->r2;
-    const float r2f = g.r2f, r2_lo = g.r2_lo, r2_hi = g.r2_hi;
-    const float two_r = 2.0f * sqrtf(r2f) * 1.001f;
+    const float two_r = 2.0f * sqrtf(g.r2f) * 1.001f;
     constexpr float FAR = 1e30f;   // position of lanes outside the group: no photon is within r of it
-    unsigned long long c_tests = 0, c_slots = 0, c_hits = 0;
+    TileCount cn;
     for (;;) {
         unsigned long long c0 = 0;
         if (lane == 0) c0 = atomicAdd(&st->gather_next, 32ull);
@@ -1361,8 +1560,6 @@ __global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_gather_tile(const Hi
             s_own[wid][lane] = own;
         }
         Kahan k0 = {0.f, 0.f}, k1 = {0.f, 0.f}, k2 = {0.f, 0.f};
-        uint32_t d_in = 0;
-        unsigned long long d_hash = 0;
         unsigned pending = __ballot_sync(0xffffffffu, valid);
         while (pending) {
             // the group: pending lanes within 2r of the leader on every axis
@@ -1371,10 +1568,10 @@ __global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_gather_tile(const Hi
             const float4 own = s_own[wid][lane], ld = s_own[wid][leader];
             const bool member = ((pending >> lane) & 1u) && fabsf(own.x - ld.x) <= two_r &&
                                 fabsf(own.y - ld.y) <= two_r && fabsf(own.z - ld.z) <= two_r;
-            pending &= ~__ballot_sync(0xffffffffu, member);
+            const unsigned gmask = __ballot_sync(0xffffffffu, member);
+            pending &= ~gmask;
             const V3<float> q = member ? mk3(own.x, own.y, own.z) : mk3(FAR, FAR, FAR);
             {
-                // the group's box and the cells around it
                 V3<float> lo = q, hi = member ? q : mk3(-FAR, -FAR, -FAR);
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
@@ -1388,146 +1585,91 @@ __global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_gather_tile(const Hi
                 if (lane == 0) {
                     box.lo[0] = lo.x; box.lo[1] = lo.y; box.lo[2] = lo.z;
                     box.hi[0] = hi.x; box.hi[1] = hi.y; box.hi[2] = hi.z;
-                    box.cx0 = max(CellMath<float>::coord(g, lo.x, 0) - g.extx, 0);
-                    box.cx1 = min(CellMath<float>::coord(g, hi.x, 0) + g.extx, g.dim[0] - 1);
-                    box.cy0 = max(CellMath<float>::coord(g, lo.y, 1) - g.ext, 0);
-                    const int cy1 = min(CellMath<float>::coord(g, hi.y, 1) + g.ext, g.dim[1] - 1);
-                    box.cz0 = max(CellMath<float>::coord(g, lo.z, 2) - g.ext, 0);
-                    const int cz1 = min(CellMath<float>::coord(g, hi.z, 2) + g.ext, g.dim[2] - 1);
-                    box.ny = cy1 - box.cy0 + 1;
-                    box.nrows = box.ny * (cz1 - box.cz0 + 1);
+                    tile_box_cells(g, box);
                 }
                 __syncwarp();
             }
             const int nrows = box.nrows;
             for (int row0 = 0; row0 < nrows; row0 += 32) {
-                // lane's row and its photon range; rows end to end
-                uint32_t rbeg = 0, rlen = 0;
-                const int row = row0 + (int)lane;
-                if (row < nrows) {
-                    const int ny = box.ny;
-                    const int zz = box.cz0 + row / ny, yy = box.cy0 + row % ny;
-                    int x0, x1;
-                    if (box_row_range(g, mk3(box.lo[0], box.lo[1], box.lo[2]), mk3(box.hi[0], box.hi[1], box.hi[2]),
-                                      r2f, yy, zz, box.cx0, box.cx1, x0, x1)) {
-                        const int base = (zz * g.dim[1] + yy) * g.dim[0];
-                        rbeg = start[3 * (base + x0)];
-                        rlen = start[3 * (base + x1 + 1)] - rbeg;
-                    }
-                }
-                uint32_t incl = rlen;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= (unsigned)o) incl += u;
-                }
-                const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-                const uint32_t excl = incl - rlen;
-                for (uint32_t b0 = 0; b0 < total; b0 += 32) {
-                    // this lane's photon: the row r with excl_r <= j < incl_r
-                    const uint32_t j = b0 + lane;
-                    int r = 0;
-#pragma unroll
-                    for (int step = 16; step > 0; step >>= 1)
-                        if (__shfl_sync(0xffffffffu, incl, r + step - 1) <= j) r += step;
-                    const uint32_t rb = __shfl_sync(0xffffffffu, rbeg, r), rx = __shfl_sync(0xffffffffu, excl, r);
-                    const bool v = j < total;
-                    uint32_t wl = 3u;
-                    float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pd = pa;
-                    if (v) {
-                        const uint32_t slot = rb + (j - rx);
-                        const float4 p = __ldg(&smap[slot]);
-                        const uint32_t m = __float_as_uint(p.w);
-                        float inv;
-                        const V3<float> d = oct_raw(m, inv);
-                        pa = make_float4(p.x, p.y, p.z, __uint_as_float(slot));
-                        pd = make_float4(-d.x * inv, -d.y * inv, -d.z * inv, 0.f);
-                        wl = min(m >> 30, 2u);
-                    }
-                    // stage grouped by wavelength
-                    const unsigned m0 = __ballot_sync(0xffffffffu, wl == 0u), m1 = __ballot_sync(0xffffffffu, wl == 1u),
-                                   m2 = __ballot_sync(0xffffffffu, wl == 2u);
-                    const int n0 = __popc(m0), n01 = n0 + __popc(m1), nv = n01 + __popc(m2);
-                    if (v) {
-                        const int at = wl == 0u ? __popc(m0 & lt) : (wl == 1u ? n0 + __popc(m1 & lt) : n01 + __popc(m2 & lt));
-                        sp[at] = pa;
-                        sd[at] = pd;
-                    }
-                    __syncwarp();
-                    // the tests; EXACT re-decides band photons in FP64
-                    bool band = false;
-                    auto sweep = [&](auto exact, int t0, int t1) -> float {
-                        constexpr bool EXACT = decltype(exact)::value;
-                        float acc = 0.0f;
-#pragma unroll 2
-                        for (int t = t0; t < t1; t++) {
-                            const float4 a = sp[t], b = sd[t];
-                            const float dx = q.x - a.x, dy = q.y - a.y, dz = q.z - a.z;
-                            const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                            bool in = d2 < r2_lo;
-                            const bool bd = !in && d2 <= r2_hi;
-                            if constexpr (EXACT) {
-                                if (bd) in = sq_euclid(f2d_here(q.x), f2d_here(q.y), f2d_here(q.z), (double)a.x,
-                                                       (double)a.y, (double)a.z) <= r2;
-                            } else {
-                                band |= bd;
-                            }
-                            const float c = __fmaf_rn(n.z, b.z, __fmaf_rn(n.y, b.y, n.x * b.x));
-                            float w = in ? fmaxf(c, 0.0f) : 0.0f;
-                            if constexpr (FILTER != PF_NONE) w *= in ? tile_filter<FILTER>(d2, r2f) : 0.0f;
-                            acc += w;
-                            if constexpr (EXACT && (DUMP || COUNT)) {
-                                if (in) {
-                                    if (DUMP) { d_in += 1u; d_hash += slot_mix(__float_as_uint(a.w)); }
-                                    if (COUNT) c_hits += 1;
-                                }
-                            }
+                const uint32_t nb = tile_walk<COUNT, DUMP, FILTER>(g, box, row0, 0, TILE_SPLIT, start, smap, sp, sd, q,
+                                                                  n, member, r2, k0, k1, k2, cn);
+                for (uint32_t b = TILE_SPLIT; b < nb; b += TILE_SPLIT) {
+                    const uint32_t be = b + TILE_SPLIT < nb ? b + TILE_SPLIT : nb;
+                    unsigned long long slot = 0;
+                    if (lane == 0) slot = atomicAdd(&st->tile_items, 1ull);
+                    slot = __shfl_sync(0xffffffffu, slot, 0);
+                    if (slot < queue.cap) {
+                        if (lane == 0) {
+                            TileItem it;
+                            it.qi0 = (uint32_t)c0;
+                            it.mask = gmask;
+                            for (int a = 0; a < 3; a++) { it.lo[a] = box.lo[a]; it.hi[a] = box.hi[a]; }
+                            it.row0 = row0;
+                            it.b0 = b;
+                            it.b1 = be;
+                            it.pad = 0;
+                            queue.items[slot] = it;
                         }
-                        return acc;
-                    };
-                    float a0 = sweep(std::false_type{}, 0, n0);
-                    float a1 = sweep(std::false_type{}, n0, n01);
-                    float a2 = sweep(std::false_type{}, n01, nv);
-                    if (__any_sync(0xffffffffu, band) || DUMP || COUNT) {
-                        // exact pass: the same tests with band photons re-decided in FP64
-                        // (the export and the counters always take it, as they count members)
-                        a0 = sweep(std::true_type{}, 0, n0);
-                        a1 = sweep(std::true_type{}, n0, n01);
-                        a2 = sweep(std::true_type{}, n01, nv);
+                    } else {   // queue full: walk it here
+                        tile_walk<COUNT, DUMP, FILTER>(g, box, row0, b, be, start, smap, sp, sd, q, n, member, r2, k0,
+                                                       k1, k2, cn);
                     }
-                    k0.add(a0);
-                    k1.add(a1);
-                    k2.add(a2);
-                    if (COUNT) {
-                        c_tests += member ? (unsigned long long)nv : 0ull;   // photon-hit point distance tests
-                        c_slots += (unsigned long long)nv;                   // lane slots the batch issued
-                    }
-                    __syncwarp();   // the next batch overwrites the stage
                 }
             }
         }
-        if (DUMP && valid) out.dump[qi] = GatherDump{{k0.s - k0.c, k1.s - k1.c, k2.s - k2.c}, d_in, d_hash};
-        if (valid) {
-            const HitPoint<float> h = load_hit(hits + qi);
-            float *px = out.gathered + 3 * (size_t)h.pixel;
-            atomicAdd(px, h.w[0] * (k0.s - k0.c));
-            atomicAdd(px + 1, h.w[1] * (k1.s - k1.c));
-            atomicAdd(px + 2, h.w[2] * (k2.s - k2.c));
-        }
+        if (valid) tile_flush<DUMP>(hits, qi, k0, k1, k2, cn, out);
+        cn.d_in = 0;
+        cn.d_hash = 0;
         __syncwarp();   // s_own is rewritten by the next chunk
     }
-    if (COUNT) {
-        for (int o = 16; o > 0; o >>= 1) {
-            c_tests += __shfl_xor_sync(0xffffffffu, c_tests, o);
-            c_hits += __shfl_xor_sync(0xffffffffu, c_hits, o);
-            c_slots += __shfl_xor_sync(0xffffffffu, c_slots, o);
+    tile_count_flush<COUNT>(cn, out);
+}
+
+// The queued parts of the walks: one item per warp at a time.
+template <bool COUNT, bool DUMP, int FILTER>
+__global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_gather_tile_items(const HitPoint<float> *hits,
+                                                                              PassState *st, const float4 *smap,
+                                                                              const uint32_t *start, TileQueue queue,
+                                                                              GatherOutF out) {
+    __shared__ float4 s_pos[GATHER_TILE_WARPS][32];
+    __shared__ float4 s_dir[GATHER_TILE_WARPS][32];
+    __shared__ TileBox s_box[GATHER_TILE_WARPS];
+    const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+    float4 *const sp = s_pos[wid], *const sd = s_dir[wid];
+    TileBox &box = s_box[wid];
+    const GridParams g = st->grid;
+    const double r2 = st->r2;
+    const unsigned long long n_items = st->tile_items < queue.cap ? st->tile_items : queue.cap;
+    constexpr float FAR = 1e30f;
+    TileCount cn;
+    for (;;) {
+        unsigned long long i = 0;
+        if (lane == 0) i = atomicAdd(&st->tile_next, 1ull);
+        i = __shfl_sync(0xffffffffu, i, 0);
+        if (i >= n_items) break;
+        const TileItem it = queue.items[i];
+        const bool member = (it.mask >> lane) & 1u;
+        const unsigned long long qi = (unsigned long long)it.qi0 + lane;
+        V3<float> q = mk3(FAR, FAR, FAR), n = mk3(0.f, 0.f, 0.f);
+        if (member) {
+            const HitPoint<float> h = load_hit(hits + qi);
+            q = ld3(h.pos);
+            n = ld3(h.nrm);
         }
+        __syncwarp();   // the previous item's walk is done with the box
         if (lane == 0) {
-            atomicAdd(out.count + 0, c_tests);
-            atomicAdd(out.count + 1, c_hits);
-            atomicAdd(out.count + 2, c_slots);
+            for (int a = 0; a < 3; a++) { box.lo[a] = it.lo[a]; box.hi[a] = it.hi[a]; }
+            tile_box_cells(g, box);
         }
+        __syncwarp();
+        Kahan k0 = {0.f, 0.f}, k1 = {0.f, 0.f}, k2 = {0.f, 0.f};
+        tile_walk<COUNT, DUMP, FILTER>(g, box, it.row0, it.b0, it.b1, start, smap, sp, sd, q, n, member, r2, k0, k1,
+                                       k2, cn);
+        if (member) tile_flush<DUMP>(hits, qi, k0, k1, k2, cn, out);
+        cn.d_in = 0;
+        cn.d_hash = 0;
     }
+    tile_count_flush<COUNT>(cn, out);
 }
 #endif  // PPM_BUILD_F32
 

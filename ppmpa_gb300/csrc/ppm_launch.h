@@ -50,10 +50,14 @@ void launch_eye_level_f(const SceneView<float> &sc, const DCamera<float> &cam, u
 // the counting and the parity-export variants
 void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
                      const uint32_t *start, int pfilter, GatherOutF out, int grid, cudaStream_t s);
-// the render gather, tile form (k_gather_tile): 32 hit points per warp;
-// out.count / out.dump select the counting and the parity-export variants
+// the render gather, tile form (k_gather_tile, then k_gather_tile_items for
+// the queued parts of long walks): 32 hit points per warp; out.count /
+// out.dump select the counting and the parity-export variants (the export
+// records must be zeroed first); items holds cap queue entries
 void launch_gather_tile_f(const HitPoint<float> *hits, PassState *st, const float4 *smap, const uint32_t *start,
-                          int pfilter, GatherOutF out, int grid, cudaStream_t s);
+                          int pfilter, TileItem *items, unsigned long long cap, GatherOutF out, int grid,
+                          cudaStream_t s);
+int kernels_per_tile_gather();
 // resident blocks per SM of the tile gather (its persistent grid is this x SMs)
 int gather_tile_blocks_per_sm();
 int estimate_tile_blocks_per_sm();
