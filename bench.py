@@ -91,7 +91,7 @@ def parse():
     p.add_argument("--precision", default="mixed", choices=["mixed", "plain"])
     p.add_argument("--cell-factor", type=int, default=0, help="grid cells per radius (0: tuned per render)")
     p.add_argument("--nphoton", type=int, default=0, help="photons per pass (0: the workload's); for profiling")
-    p.add_argument("--row-walk", action="store_true", help="mixed render: the row-walk gather (comparison)")
+    p.add_argument("--tile-gather", action="store_true", help="mixed render: the tile gather (comparison)")
     return p.parse_args()
 
 
@@ -107,7 +107,7 @@ def dist_env():
 
 def run_profile(args, w):
     from ppmpa_gb300 import MIXED, PLAIN, Context, RenderConfig
-    from ppmpa_gb300.api import RENDER_ROW_WALK
+    from ppmpa_gb300.api import RENDER_TILE_GATHER
     sc, cam = scene_of(w)
     with Context(0, seed=args.seed) as ctx:
         ctx.upload_scene(sc)
@@ -116,7 +116,7 @@ def run_profile(args, w):
         ctx.render_begin(RenderConfig(nphoton=w["nphoton"], passes=args.profile + 1, radius0=w["r0"],
                                       alpha=w["alpha"], precision=prec, use_graph=True, seed=args.seed,
                                       cell_factor=args.cell_factor,
-                                      flags=RENDER_ROW_WALK if args.row_walk else 0))
+                                      flags=RENDER_TILE_GATHER if args.tile_gather else 0))
         ctx.render_step(args.profile + 1)
         img = ctx.render_image()
         st = ctx.stats()
@@ -312,7 +312,7 @@ def measure_render(args, name, w, ctx, stream, flush, world, rank, local, headli
     """Every GPU measurement of one render workload on an open context."""
     import torch
     from ppmpa_gb300 import MIXED, PLAIN, RenderConfig
-    from ppmpa_gb300.api import RENDER_ROW_WALK, RENDER_TUNE_CELLS
+    from ppmpa_gb300.api import RENDER_TILE_GATHER, RENDER_TUNE_CELLS
 
     sc, cam = scene_of(w)
     ctx.upload_scene(sc)
@@ -325,7 +325,7 @@ def measure_render(args, name, w, ctx, stream, flush, world, rank, local, headli
         d = rng.normal(size=(262144, 3))
         d /= np.linalg.norm(d, axis=1, keepdims=True)
         leaf, _ = ctx.tune_bvh_leaf(np.hstack([p, d]))
-    walk = RENDER_ROW_WALK if args.row_walk else 0
+    walk = RENDER_TILE_GATHER if args.tile_gather else 0
     P = w["passes"]
     steps = min(args.steps, w.get("max_steps", args.steps))
     warmup = max(3, args.warmup) if headline else 3
@@ -496,7 +496,7 @@ def measure_render(args, name, w, ctx, stream, flush, world, rank, local, headli
         "value": value, "unit": "Mphotons/s", "steps": steps, "warmup": warmup, "ms_per_step": ms / steps,
         "config": {"workload": name, **{k: v for k, v in w.items() if not k.startswith("cpu_")},
                    "precision": "mixed", "cuda_graph": True, "bvh_leaf": leaf, "cells_per_radius": cells,
-                   "gather": "row walk" if args.row_walk else "tile",
+                   "gather": "tile" if args.tile_gather else "row walk",
                    "timed_passes": [0, steps - 1], "schedule_passes": max(P, steps),
                    "l2": "flushed between timed passes (2x L2 write)", "parallelism": f"passes x{world}"},
         "full_schedule": full,

@@ -136,11 +136,15 @@ enum { PPM_RENDER_TUNE_CELLS = 1,
  * pass traces the eye rays only (direct light + ambient, mirror and
  * refraction children); passes average anti-aliased images. */
        PPM_RENDER_CLASSIC = 2,
-/* PPM_RENDER_ROW_WALK: in the mixed render, gather with one warp per hit
- * point (or per two in one cell) walking its own cell rows, in place of the
- * default tile gather (one warp per 32 hit points, one lane each, sharing
- * one walk of their photons).  Same sets and sums; kept to compare the two. */
-       PPM_RENDER_ROW_WALK = 4 };
+/* PPM_RENDER_TILE_GATHER: in the mixed render, gather with one warp per 32
+ * hit points (one lane each, sorted into a compact patch of the scene,
+ * sharing one walk of the photons around them) in place of the default row
+ * walk (one warp per hit point, or per two in one cell, walking its own
+ * cell rows).  Same neighbour sets and sums.  The tile form costs fewer
+ * instructions per photon test but tests more photons (the union of 32
+ * spheres against each sphere); which is faster depends on how dense the
+ * hit points are beside the radius.  No reference counterpart. */
+       PPM_RENDER_TILE_GATHER = 4 };
 
 /* Per-pass statistics of the last rendered pass and accumulated timings. */
 typedef struct ppm_stats {

@@ -31,7 +31,7 @@ def _ptr(a: np.ndarray, ctype):
 # RenderConfig.flags bits (include/ppm_api.h)
 RENDER_TUNE_CELLS = 1   # time cells per radius 1 and 2 before the render, keep the faster
 RENDER_CLASSIC = 2      # the classic ray tracer (trace_ray_classic) instead of photon mapping
-RENDER_ROW_WALK = 4     # mixed render: per-hit-point row-walk gather instead of the tile gather
+RENDER_TILE_GATHER = 4  # mixed render: the tile gather (32 hit points per warp) instead of the row walk
 
 
 @dataclass

@@ -1435,7 +1435,8 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
                 launch_eye_level_d(ctx->sv_d, ctx->cam_d, ctx->cfg.seed, ctx->st, uc, l, in, out, qcap, h,
                                    EyeOut<double>{as<double>(ctx->pass_img)}, g, st);
             }, s2);
-    if (mixed) {   // hit points into Morton order for the gather, still on the eye stream
+    const bool tile = mixed && (ctx->cfg.flags & PPM_RENDER_TILE_GATHER);
+    if (tile) {   // hit points into Morton order for the tile gather, still on the eye stream
         launch_hit_sort_f(as<HitPoint<float>>(ctx->hits_f), ctx->st, as<uint32_t>(ctx->hcount),
                           as<uint32_t>(ctx->hblock), as<uint32_t>(ctx->hstart), as<uint2>(ctx->hkeyrank),
                           as<HitPoint<float>>(ctx->hits_sorted), grid_blocks(ctx, 8), s2);
@@ -1472,8 +1473,8 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
     if (mixed) {
         GatherOutF go{as<float>(ctx->pass_gather32), nullptr, ctx->count_gather ? &ctx->st->candidates : nullptr,
                       ctx->gather_dump};
-        if (ctx->cfg.flags & PPM_RENDER_ROW_WALK) {
-            launch_gather_f(as<HitPoint<float>>(ctx->hits_sorted), ctx->st, -1, as<float4>(ctx->sorted_f),
+        if (!(ctx->cfg.flags & PPM_RENDER_TILE_GATHER)) {
+            launch_gather_f(as<HitPoint<float>>(ctx->hits_f), ctx->st, -1, as<float4>(ctx->sorted_f),
                             as<uint32_t>(ctx->start), ctx->cam.pfilter, go, g8, s);
         } else {
             launch_gather_tile_f(as<HitPoint<float>>(ctx->hits_sorted), ctx->st, as<float4>(ctx->sorted_f),
@@ -1563,7 +1564,7 @@ extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
         return set_err(ctx, PPM_ERR_NOT_READY, "scene (with lights) and camera must be set first");
     if (cfg->nphoton <= 0 || cfg->passes < 0 || !(cfg->radius0 > 0.0) || cfg->precision < 0 || cfg->precision > 1 ||
         cfg->cell_factor < 0 || cfg->cell_factor > MAX_CELL_FACTOR || cfg->first_pass < 0 ||
-        (cfg->flags & ~(PPM_RENDER_TUNE_CELLS | PPM_RENDER_CLASSIC | PPM_RENDER_ROW_WALK)))
+        (cfg->flags & ~(PPM_RENDER_TUNE_CELLS | PPM_RENDER_CLASSIC | PPM_RENDER_TILE_GATHER)))
         return set_err(ctx, PPM_ERR_INVALID_ARG, "bad render configuration");
     cudaSetDevice(ctx->device);
     drop_graph(ctx);
@@ -1588,7 +1589,7 @@ extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
     if (cfg->precision == PPM_PRECISION_MIXED) {
         TRY(ensure(ctx, ctx->pass_direct32, sizeof(float) * 3 * ctx->npx));
         TRY(ensure(ctx, ctx->pass_gather32, sizeof(float) * 3 * ctx->npx));
-        if (photons) TRY(ensure_hit_sort(ctx));
+        if (photons && (cfg->flags & PPM_RENDER_TILE_GATHER)) TRY(ensure_hit_sort(ctx));
     }
     TRY(ensure(ctx, ctx->sum_img, sizeof(double) * 3 * ctx->npx));
     CK(cudaMemsetAsync(ctx->sum_img.p, 0, sizeof(double) * 3 * ctx->npx, ctx->s));
@@ -1741,8 +1742,8 @@ extern "C" int ppm_render_gather_export(ppm_ctx *ctx, ppm_gather_export *ex) {
     std::vector<GatherDump> rec((size_t)nh);
     if (np) CK(cudaMemcpyAsync(ex->photons, ctx->sorted_f.p, sizeof(float4) * np, cudaMemcpyDeviceToHost, ctx->s));
     if (nh) {
-        CK(cudaMemcpyAsync(ex->hits, ctx->hits_sorted.p, sizeof(HitPoint<float>) * nh, cudaMemcpyDeviceToHost,
-                           ctx->s));
+        const DevBuf &hb = (ctx->cfg.flags & PPM_RENDER_TILE_GATHER) ? ctx->hits_sorted : ctx->hits_f;
+        CK(cudaMemcpyAsync(ex->hits, hb.p, sizeof(HitPoint<float>) * nh, cudaMemcpyDeviceToHost, ctx->s));
         CK(cudaMemcpyAsync(rec.data(), ctx->gdump.p, sizeof(GatherDump) * nh, cudaMemcpyDeviceToHost, ctx->s));
     }
     CK(cudaMemcpyAsync(ex->gathered, ctx->pass_gather32.p, sizeof(float) * 3 * ctx->npx, cudaMemcpyDeviceToHost,

@@ -1152,10 +1152,10 @@ __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, cons
 #endif
 
 #if defined(PPM_BUILD_F32)
-// The render gather, row-walk form (PPM_RENDER_ROW_WALK): one warp per hit
-// point, or per two hit points of one cell (gather_pair).  Warps take their
-// hit points from a counter, two at a time, so the hit points in flight are
-// a narrow window of the (spatially sorted) list: neighbouring warps read the
+// The render gather, row-walk form (the default): one warp per hit point,
+// or per two hit points of one cell (gather_pair).  Warps take their hit
+// points from a counter, two at a time, so the hit points in flight are a
+// narrow window of the list (appended in pixel tiles by the eye pass): neighbouring warps read the
 // same photons, from L1 or L2, and a slow warp does not hold up the rest
 // (measured on the glass box: 0.402 ms against 0.406 for 1, 0.410 for 4 and
 // 0.43 for 8 or a fixed warp stride).  Five blocks per SM (at most 51

@@ -22,16 +22,16 @@ Bars:
 Cases: the glass box (512 x 512, 1M photons per pass) at pass 0 and pass 33
 with 1 and 2 cells per radius, the cone and Gauss filters at pass 33, and
 the diffuse-sphere box (256 x 256, 200k photons) at its full size; each for
-the default tile gather and for the row-walk gather (PPM_RENDER_ROW_WALK).
+the default row-walk gather and for the tile gather (PPM_RENDER_TILE_GATHER).
 """
 import numpy as np
 import pytest
 
 from oracle.binding import Oracle
 from ppmpa_gb300 import MIXED, Context, RenderConfig, scene as S
-from ppmpa_gb300.api import RENDER_ROW_WALK
+from ppmpa_gb300.api import RENDER_TILE_GATHER
 
-GATHERS = {"tile": 0, "row_walk": RENDER_ROW_WALK}
+GATHERS = {"row_walk": 0, "tile": RENDER_TILE_GATHER}
 
 pytestmark = pytest.mark.gpu
 
