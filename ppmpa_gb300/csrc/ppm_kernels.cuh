@@ -485,18 +485,16 @@ __host__ __device__ __forceinline__ long long eye_slots(int xreso, int yreso) {
 // direct light of every light plus the camera's ambient, no hit points, the
 // exact mirror direction, refraction about the normal with the child's
 // medium by the side the refracted ray leaves on, and the bsdf at cos1.
+// One vertex of the eye tree: slot i of level 0 (a camera ray) or entry i
+// of the level's queue.
 template <typename T, bool B, bool CLASSIC = false>
-__device__ __forceinline__ void eye_level(const SceneView<T, B> &sc, const DCamera<T> &cam, uint64_t seed,
-                                          PassState *st, int uc, int level, EyeQueue<T> in, EyeQueue<T> out,
-                                          unsigned long long qcap, HitPoint<T> *hits, EyeOut<T> pix) {
-    const uint32_t pass = (uint32_t)st->pass;
-    const unsigned long long hit_cap = st->hit_cap;
-    const long long ntx = eye_tiles_x(cam.xreso);
-    unsigned long long n = level == 0 ? (unsigned long long)eye_slots(cam.xreso, cam.yreso) : st->eq[level];
-    if (level > 0 && n > qcap) n = qcap;
+__device__ __forceinline__ void eye_vertex(const SceneView<T, B> &sc, const DCamera<T> &cam, uint64_t seed,
+                                           PassState *st, int uc, int level, EyeQueue<T> in, EyeQueue<T> out,
+                                           unsigned long long qcap, HitPoint<T> *hits, EyeOut<T> pix,
+                                           unsigned long long i, uint32_t pass, unsigned long long hit_cap,
+                                           long long ntx) {
     const T air[3] = {T(1), T(1), T(1)};
-    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
+    {
         V3<T> rp, rd, w;
         uint32_t p, node;
         int medium;
@@ -504,7 +502,7 @@ __device__ __forceinline__ void eye_level(const SceneView<T, B> &sc, const DCame
             const uint32_t tile = (uint32_t)(i >> 5), k = (uint32_t)(i & 31);
             const uint32_t px = (tile % (uint32_t)ntx) * EYE_TILE_W + k % EYE_TILE_W;
             const uint32_t py = (tile / (uint32_t)ntx) * EYE_TILE_H + k / EYE_TILE_W;
-            if (px >= (uint32_t)cam.xreso || py >= (uint32_t)cam.yreso) continue;
+            if (px >= (uint32_t)cam.xreso || py >= (uint32_t)cam.yreso) return;
             p = py * (uint32_t)cam.xreso + px;
             const T y = (T)py, x = (T)px;
             Rng rg;
@@ -623,6 +621,20 @@ __device__ __forceinline__ void eye_level(const SceneView<T, B> &sc, const DCame
         if (level == 0) pix.set(p, acc);
         else if (any_nz(acc)) pix.add(p, acc);
     }
+}
+
+template <typename T, bool B, bool CLASSIC = false>
+__device__ __forceinline__ void eye_level(const SceneView<T, B> &sc, const DCamera<T> &cam, uint64_t seed,
+                                          PassState *st, int uc, int level, EyeQueue<T> in, EyeQueue<T> out,
+                                          unsigned long long qcap, HitPoint<T> *hits, EyeOut<T> pix) {
+    const uint32_t pass = (uint32_t)st->pass;
+    const unsigned long long hit_cap = st->hit_cap;
+    const long long ntx = eye_tiles_x(cam.xreso);
+    unsigned long long n = level == 0 ? (unsigned long long)eye_slots(cam.xreso, cam.yreso) : st->eq[level];
+    if (level > 0 && n > qcap) n = qcap;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x)
+        eye_vertex<T, B, CLASSIC>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix, i, pass, hit_cap, ntx);
 }
 
 // Two entry points over the same body: without a hierarchy the compiler's
@@ -1160,6 +1172,114 @@ __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, cons
 // (measured on the glass box: 0.402 ms against 0.406 for 1, 0.410 for 4 and
 // 0.43 for 8 or a fixed warp stride).  Five blocks per SM (at most 51
 // registers; it needs 46 without spilling) measured 1 % faster than four.
+// One step of the row walk: hit points qi and qi + 1 in one walk when both
+// are left and share a cell (returns 2), else hit point qi alone (returns
+// 1).  All lanes of the warp enter with the same arguments.
+template <bool COUNT, bool DUMP>
+__device__ __forceinline__ unsigned gather_step(const GridParams &g, double r2, const HitPoint<float> *hits,
+                                                unsigned long long qi, unsigned long long left,
+                                                const uint32_t *start, const float4 *smap, int pfilter,
+                                                const GatherOutF &out) {
+    if (left == 2 && gather_pair<COUNT, DUMP>(g, r2, hits + qi, start, smap, pfilter, out, qi)) return 2u;
+    const unsigned lane = lane_id();
+    const HitPoint<float> h = load_hit(hits + qi);
+    const float r2_lo = g.r2_lo, r2_hi = g.r2_hi, r2f = g.r2f;
+    V3<float> q = ld3(h.pos), n = ld3(h.nrm);
+    int c[3], lo[3], hi[3];
+    query_cells(g, q, g.ext, g.extx, c, lo, hi);
+    // Per-lane sums: a lane adds a few dozen terms (relative error <
+    // 1e-6), and the three sums take the photon's value or zero without
+    // a branch on its wavelength.
+    float k0 = 0.f, k1 = 0.f, k2 = 0.f;
+    unsigned long long c_slots = 0, c_valid = 0, c_hits = 0;
+    uint32_t d_in = 0;             // export only
+    unsigned long long d_hash = 0;   // export only
+    {
+        for_each_candidate_two(g, start, q, r2f, lo, hi, smap,
+                               [&](auto two, float4 p0, bool v0, uint32_t i0, float4 p1, bool v1, uint32_t i1) {
+            constexpr bool TWO = decltype(two)::value;
+            if (COUNT) {
+                c_slots += TWO ? 2 : 1;
+                c_valid += (int)v0 + (int)v1;
+            }
+            float dx = q.x - p0.x, dy = q.y - p0.y, dz = q.z - p0.z;
+            const float d0 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+            float d1 = 0.0f;
+            if constexpr (TWO) {
+                dx = q.x - p1.x;
+                dy = q.y - p1.y;
+                dz = q.z - p1.z;
+                d1 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+            }
+            // in_radius_f32 on both: below r2_lo in, above r2_hi out, between in FP64.
+            // The vote keeps the FP64 recheck a branch that warps almost never
+            // take; left to the compiler it was predicated into every step,
+            // which costs issue slots on this GPU's narrow FP64 pipe.
+            bool in0 = v0 && d0 < r2_lo, in1 = TWO && v1 && d1 < r2_lo;
+            const bool b0 = v0 && !in0 && d0 <= r2_hi, b1 = TWO && v1 && !in1 && d1 <= r2_hi;
+            if (__any_sync(0xffffffffu, b0 || b1)) {
+                const double qx = f2d_here(q.x), qy = f2d_here(q.y), qz = f2d_here(q.z);
+                if (b0) in0 = sq_euclid(qx, qy, qz, (double)p0.x, (double)p0.y, (double)p0.z) <= r2;
+                if (b1) in1 = sq_euclid(qx, qy, qz, (double)p1.x, (double)p1.y, (double)p1.z) <= r2;
+            }
+            if (in0 || in1) {
+                const uint32_t m0 = __float_as_uint(p0.w), m1 = __float_as_uint(p1.w);
+                const float c0 = oct_dot(m0, n);
+                const float c1 = TWO ? oct_dot(m1, n) : 0.0f;
+                float w0 = (in0 && c0 < 0.0f) ? -c0 : 0.0f, w1 = (in1 && c1 < 0.0f) ? -c1 : 0.0f;
+                if (pfilter != PF_NONE) {
+                    w0 *= filter_wt_f(pfilter, d0, r2f);
+                    if (TWO) w1 *= filter_wt_f(pfilter, d1, r2f);
+                }
+                const uint32_t l0 = m0 >> 30, l1 = m1 >> 30;
+                if constexpr (TWO) {
+                    k0 += (l0 == 0u ? w0 : 0.0f) + (l1 == 0u ? w1 : 0.0f);
+                    k1 += (l0 == 1u ? w0 : 0.0f) + (l1 == 1u ? w1 : 0.0f);
+                    k2 += (l0 >= 2u ? w0 : 0.0f) + (l1 >= 2u ? w1 : 0.0f);
+                } else {
+                    k0 += l0 == 0u ? w0 : 0.0f;
+                    k1 += l0 == 1u ? w0 : 0.0f;
+                    k2 += l0 >= 2u ? w0 : 0.0f;
+                }
+                if (COUNT) c_hits += (int)in0 + (int)in1;
+                if (DUMP) {
+                    d_in += (in0 ? 1u : 0u) + (in1 ? 1u : 0u);
+                    d_hash += (in0 ? slot_mix(i0) : 0ull) + (in1 ? slot_mix(i1) : 0ull);
+                }
+            }
+        });
+    }
+    const float s0 = warp_sum(k0), s1 = warp_sum(k1), s2 = warp_sum(k2);
+    if (COUNT) {
+        for (int o = 16; o > 0; o >>= 1) {
+            c_slots += __shfl_xor_sync(0xffffffffu, c_slots, o);
+            c_valid += __shfl_xor_sync(0xffffffffu, c_valid, o);
+            c_hits += __shfl_xor_sync(0xffffffffu, c_hits, o);
+        }
+        if (lane == 0) {
+            atomicAdd(out.count + 0, c_valid);
+            atomicAdd(out.count + 1, c_hits);
+            atomicAdd(out.count + 2, c_slots);
+        }
+    }
+    if constexpr (DUMP) {
+        for (int o = 16; o > 0; o >>= 1) {
+            d_in += __shfl_xor_sync(0xffffffffu, d_in, o);
+            d_hash += __shfl_xor_sync(0xffffffffu, d_hash, o);
+        }
+        if (lane == 0) out.dump[qi] = GatherDump{{s0, s1, s2}, d_in, d_hash};
+    }
+    if (lane == 0) {
+        // FP32 only here: an FP64 instruction costs a warp-wide slot of
+        // the narrow FP64 pipe even with one active lane
+        float *px = out.gathered + 3 * (size_t)h.pixel;
+        atomicAdd(px, h.w[0] * s0);
+        atomicAdd(px + 1, h.w[1] * s1);
+        atomicAdd(px + 2, h.w[2] * s2);
+    }
+    return 1u;
+}
+
 template <bool COUNT, bool DUMP = false>
 __global__ void __launch_bounds__(256, 5) k_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed,
                                                      const float4 *smap, const uint32_t *start, int pfilter,
@@ -1178,107 +1298,7 @@ __global__ void __launch_bounds__(256, 5) k_gather_f(const HitPoint<float> *hits
             qi = c;
             qend = c + CHUNK < nq ? c + CHUNK : nq;
         }
-        if (qend - qi == 2 && gather_pair<COUNT, DUMP>(g, st->r2, hits + qi, start, smap, pfilter, out, qi)) {
-            qi += 2;
-            continue;
-        }
-        const HitPoint<float> h = load_hit(hits + qi);
-        const double r2 = st->r2;
-        const float r2_lo = g.r2_lo, r2_hi = g.r2_hi, r2f = g.r2f;
-        V3<float> q = ld3(h.pos), n = ld3(h.nrm);
-        int c[3], lo[3], hi[3];
-        query_cells(g, q, g.ext, g.extx, c, lo, hi);
-        // Per-lane sums: a lane adds a few dozen terms (relative error <
-        // 1e-6), and the three sums take the photon's value or zero without
-        // a branch on its wavelength.
-        float k0 = 0.f, k1 = 0.f, k2 = 0.f;
-        unsigned long long c_slots = 0, c_valid = 0, c_hits = 0;
-        uint32_t d_in = 0;             // export only
-        unsigned long long d_hash = 0;   // export only
-        {
-            for_each_candidate_two(g, start, q, r2f, lo, hi, smap,
-                                   [&](auto two, float4 p0, bool v0, uint32_t i0, float4 p1, bool v1, uint32_t i1) {
-                constexpr bool TWO = decltype(two)::value;
-                if (COUNT) {
-                    c_slots += TWO ? 2 : 1;
-                    c_valid += (int)v0 + (int)v1;
-                }
-                float dx = q.x - p0.x, dy = q.y - p0.y, dz = q.z - p0.z;
-                const float d0 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                float d1 = 0.0f;
-                if constexpr (TWO) {
-                    dx = q.x - p1.x;
-                    dy = q.y - p1.y;
-                    dz = q.z - p1.z;
-                    d1 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                }
-                // in_radius_f32 on both: below r2_lo in, above r2_hi out, between in FP64.
-                // The vote keeps the FP64 recheck a branch that warps almost never
-                // take; left to the compiler it was predicated into every step,
-                // which costs issue slots on this GPU's narrow FP64 pipe.
-                bool in0 = v0 && d0 < r2_lo, in1 = TWO && v1 && d1 < r2_lo;
-                const bool b0 = v0 && !in0 && d0 <= r2_hi, b1 = TWO && v1 && !in1 && d1 <= r2_hi;
-                if (__any_sync(0xffffffffu, b0 || b1)) {
-                    const double qx = f2d_here(q.x), qy = f2d_here(q.y), qz = f2d_here(q.z);
-                    if (b0) in0 = sq_euclid(qx, qy, qz, (double)p0.x, (double)p0.y, (double)p0.z) <= r2;
-                    if (b1) in1 = sq_euclid(qx, qy, qz, (double)p1.x, (double)p1.y, (double)p1.z) <= r2;
-                }
-                if (in0 || in1) {
-                    const uint32_t m0 = __float_as_uint(p0.w), m1 = __float_as_uint(p1.w);
-                    const float c0 = oct_dot(m0, n);
-                    const float c1 = TWO ? oct_dot(m1, n) : 0.0f;
-                    float w0 = (in0 && c0 < 0.0f) ? -c0 : 0.0f, w1 = (in1 && c1 < 0.0f) ? -c1 : 0.0f;
-                    if (pfilter != PF_NONE) {
-                        w0 *= filter_wt_f(pfilter, d0, r2f);
-                        if (TWO) w1 *= filter_wt_f(pfilter, d1, r2f);
-                    }
-                    const uint32_t l0 = m0 >> 30, l1 = m1 >> 30;
-                    if constexpr (TWO) {
-                        k0 += (l0 == 0u ? w0 : 0.0f) + (l1 == 0u ? w1 : 0.0f);
-                        k1 += (l0 == 1u ? w0 : 0.0f) + (l1 == 1u ? w1 : 0.0f);
-                        k2 += (l0 >= 2u ? w0 : 0.0f) + (l1 >= 2u ? w1 : 0.0f);
-                    } else {
-                        k0 += l0 == 0u ? w0 : 0.0f;
-                        k1 += l0 == 1u ? w0 : 0.0f;
-                        k2 += l0 >= 2u ? w0 : 0.0f;
-                    }
-                    if (COUNT) c_hits += (int)in0 + (int)in1;
-                    if (DUMP) {
-                        d_in += (in0 ? 1u : 0u) + (in1 ? 1u : 0u);
-                        d_hash += (in0 ? slot_mix(i0) : 0ull) + (in1 ? slot_mix(i1) : 0ull);
-                    }
-                }
-            });
-        }
-        const float s0 = warp_sum(k0), s1 = warp_sum(k1), s2 = warp_sum(k2);
-        if (COUNT) {
-            for (int o = 16; o > 0; o >>= 1) {
-                c_slots += __shfl_xor_sync(0xffffffffu, c_slots, o);
-                c_valid += __shfl_xor_sync(0xffffffffu, c_valid, o);
-                c_hits += __shfl_xor_sync(0xffffffffu, c_hits, o);
-            }
-            if (lane == 0) {
-                atomicAdd(out.count + 0, c_valid);
-                atomicAdd(out.count + 1, c_hits);
-                atomicAdd(out.count + 2, c_slots);
-            }
-        }
-        if constexpr (DUMP) {
-            for (int o = 16; o > 0; o >>= 1) {
-                d_in += __shfl_xor_sync(0xffffffffu, d_in, o);
-                d_hash += __shfl_xor_sync(0xffffffffu, d_hash, o);
-            }
-            if (lane == 0) out.dump[qi] = GatherDump{{s0, s1, s2}, d_in, d_hash};
-        }
-        if (lane == 0) {
-            // FP32 only here: an FP64 instruction costs a warp-wide slot of
-            // the narrow FP64 pipe even with one active lane
-            float *px = out.gathered + 3 * (size_t)h.pixel;
-            atomicAdd(px, h.w[0] * s0);
-            atomicAdd(px + 1, h.w[1] * s1);
-            atomicAdd(px + 2, h.w[2] * s2);
-        }
-        qi += 1ull;
+        qi += gather_step<COUNT, DUMP>(g, st->r2, hits, qi, qend - qi, start, smap, pfilter, out);
     }
 }
 
