@@ -393,6 +393,22 @@ int         ppm_batch_destroy(ppm_batch *b);
 const char *ppm_batch_last_error(const ppm_batch *b);
 int         ppm_batch_render(ppm_batch *b, const ppm_job *jobs, int32_t njobs, double *device_ms);
 
+/* How a batch runs its passes.  PPM_BATCH_STAGED: one launch per stage of the
+ * pass (eye levels, photon trace, map build, gather, accumulate) covers every
+ * job -- 22 launches per pass whatever the number of jobs, each stage taking
+ * its work items (job, element) from the concatenation of the jobs' work --
+ * for 1 to 256 jobs that are all mixed-precision photon-mapping renders with
+ * the default gather.  PPM_BATCH_GRAPHS: each job's own pass graph, the
+ * jobs' graphs side by side in one parent graph per pass (any jobs).
+ * PPM_BATCH_AUTO (default): staged when the jobs allow it.  tile: photons per
+ * work item of the staged map-build stages; 0 (default) times 1024, 4096 and
+ * 16384 on one pass of the batch before the render and keeps the fastest.
+ * No reference counterpart. */
+enum { PPM_BATCH_AUTO = 0, PPM_BATCH_STAGED = 1, PPM_BATCH_GRAPHS = 2 };
+int         ppm_batch_set_mode(ppm_batch *b, int32_t mode, int32_t tile);
+/* how the last render ran: staged (1) or graphs (0), and the tile it used */
+int         ppm_batch_info(const ppm_batch *b, int32_t *staged, int32_t *tile);
+
 #ifdef __cplusplus
 }
 #endif

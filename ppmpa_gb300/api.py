@@ -33,6 +33,9 @@ RENDER_TUNE_CELLS = 1   # time cells per radius 1 and 2 before the render, keep 
 RENDER_CLASSIC = 2      # the classic ray tracer (trace_ray_classic) instead of photon mapping
 RENDER_TILE_GATHER = 4  # mixed render: the tile gather (32 hit points per warp) instead of the row walk
 
+# Batch.set_mode modes (include/ppm_api.h)
+BATCH_AUTO, BATCH_STAGED, BATCH_GRAPHS = 0, 1, 2
+
 
 @dataclass
 class RenderConfig:
@@ -340,6 +343,19 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+    def set_mode(self, mode: int = 0, tile: int = 0):
+        """BATCH_AUTO / BATCH_STAGED (one launch per stage over every job) /
+        BATCH_GRAPHS (the jobs' pass graphs side by side); tile: photons per
+        map-build work item of the staged passes (0: tuned per render)."""
+        st = self.lib.ppm_batch_set_mode(self.h, int(mode), int(tile))
+        if st != 0:
+            raise PPMError(st, "bad batch mode")
+
+    def info(self) -> dict:
+        staged, tile = C.c_int32(), C.c_int32()
+        self.lib.ppm_batch_info(self.h, C.byref(staged), C.byref(tile))
+        return dict(staged=bool(staged.value), tile=tile.value)
 
     def render(self, jobs):
         """jobs: [(scene, camera, RenderConfig)]; returns ([images], device ms of the passes)."""

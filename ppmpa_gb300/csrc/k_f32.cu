@@ -139,3 +139,6 @@ void launch_pack_photons_f(const float *pos, const float *dir, const uint8_t *wl
 }
 
 }  // namespace ppm
+
+// batched passes over many jobs (the same element bodies)
+#include "ppm_batch.cuh"

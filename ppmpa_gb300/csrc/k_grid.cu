@@ -8,8 +8,7 @@
 
 namespace ppm {
 
-__global__ void k_pass_begin(PassState *st) {
-    if (threadIdx.x != 0) return;
+__device__ __forceinline__ void pass_begin_state(PassState *st) {
     st->n_stored = 0;
     st->n_hits = 0;
     st->candidates = 0;
@@ -31,12 +30,16 @@ __global__ void k_pass_begin(PassState *st) {
     }
 }
 
+__global__ void k_pass_begin(PassState *st) {
+    if (threadIdx.x != 0) return;
+    pass_begin_state(st);
+}
+
 // Grid over the photon bounds with cells of c = r/k * (1 + 1/128) in y and z
 // (k = cells per radius) and c / sx in x.  The margin keeps |p - q| <= r  =>
 // |cell(p) - cell(q)| <= ext (extx in x) under FP32 rounding of the cell
 // coordinate (<= 3 ulp of <= 8192 cells per axis).
-__global__ void k_grid_setup(PassState *st, double r2_override) {
-    if (threadIdx.x != 0) return;
+__device__ __forceinline__ void grid_setup_state(PassState *st, double r2_override) {
     double r2 = r2_override > 0.0 ? r2_override : st->r2;
     double r = sqrt(r2);
     double lo[3], hi[3];
@@ -98,6 +101,11 @@ __global__ void k_grid_setup(PassState *st, double r2_override) {
     st->grid = g;
 }
 
+__global__ void k_grid_setup(PassState *st, double r2_override) {
+    if (threadIdx.x != 0) return;
+    grid_setup_state(st, r2_override);
+}
+
 // Exclusive scan of the per-key counts into start[] (the photon map's cell
 // starts) in tiles of SCAN_TILE keys: per-tile sums, a one-block scan of the
 // tile sums, then each tile scanned from its offset.  The tile kernels loop
@@ -121,36 +129,30 @@ __device__ __forceinline__ long long scan_keys(const PassState *st, long long fi
     return fixed >= 0 ? fixed : st->grid.nkeys;
 }
 
-__global__ void __launch_bounds__(256) k_scan_reduce(const uint32_t *count, const PassState *st, long long fixed,
-                                                     uint32_t *block_sums) {
-    const long long n = scan_keys(st, fixed);
-    const long long ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
-    __shared__ uint32_t ws[8];
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const long long base = tile * SCAN_TILE;
-        uint32_t s = 0;
+// the sum of one tile's counts into block_sums[tile]
+__device__ __forceinline__ void scan_reduce_tile(const uint32_t *count, long long n, long long tile,
+                                                 uint32_t *block_sums, uint32_t *ws) {
+    const long long base = tile * SCAN_TILE;
+    uint32_t s = 0;
 #pragma unroll
-        for (int k = 0; k < SCAN_TILE / SCAN_ROUND; k++) {
-            const uint4 v = load_counts(count, base + (long long)k * SCAN_ROUND + 4 * threadIdx.x, n);
-            s += (v.x + v.y) + (v.z + v.w);
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t t = 0;
-            for (int w = 0; w < 8; w++) t += ws[w];
-            block_sums[tile] = t;
-        }
-        __syncthreads();
+    for (int k = 0; k < SCAN_TILE / SCAN_ROUND; k++) {
+        const uint4 v = load_counts(count, base + (long long)k * SCAN_ROUND + 4 * threadIdx.x, n);
+        s += (v.x + v.y) + (v.z + v.w);
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < 8; w++) t += ws[w];
+        block_sums[tile] = t;
+    }
+    __syncthreads();
 }
 
-__global__ void __launch_bounds__(1024) k_scan_top(uint32_t *block_sums, const PassState *st, long long fixed) {
-    const long long n = scan_keys(st, fixed);
-    const int nb = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
-    __shared__ uint32_t sh[1024];
+// exclusive scan of nb <= 4096 tile sums by a block of 1024 threads
+__device__ __forceinline__ void scan_top_block(uint32_t *block_sums, int nb, uint32_t *sh) {
     // each thread owns up to 4 consecutive tile sums
     uint32_t v[4], t = 0;
     for (int j = 0; j < 4; j++) {
@@ -174,56 +176,75 @@ __global__ void __launch_bounds__(1024) k_scan_top(uint32_t *block_sums, const P
     }
 }
 
+// one tile of the exclusive scan into start[], counts cleared behind it
+__device__ __forceinline__ void scan_down_tile(uint32_t *count, long long n, long long tile,
+                                               const uint32_t *block_sums, uint32_t *start, uint32_t *ws) {
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long base = tile * SCAN_TILE;
+    uint32_t run = block_sums[tile];   // keys before this tile
+#pragma unroll 1
+    for (int k = 0; k < SCAN_TILE / SCAN_ROUND; k++) {
+        const long long i = base + (long long)k * SCAN_ROUND + 4 * threadIdx.x;
+        const uint4 v = load_counts(count, i, n);
+        const uint32_t t = (v.x + v.y) + (v.z + v.w);
+        uint32_t incl = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (unsigned)o) incl += u;
+        }
+        if (lane == 31) ws[warp] = incl;
+        __syncthreads();
+        uint32_t woff = 0, total = 0;
+#pragma unroll
+        for (int w = 0; w < 8; w++) {
+            const uint32_t x = ws[w];
+            woff += (unsigned)w < warp ? x : 0u;
+            total += x;
+        }
+        uint4 o;
+        o.x = run + woff + incl - t;
+        o.y = o.x + v.x;
+        o.z = o.y + v.y;
+        o.w = o.z + v.z;
+        if (i + 3 < n) {
+            *reinterpret_cast<uint4 *>(start + i) = o;
+            *reinterpret_cast<uint4 *>(count + i) = make_uint4(0u, 0u, 0u, 0u);
+        } else {
+            const uint32_t ov[4] = {o.x, o.y, o.z, o.w};
+            for (int j = 0; j < 4; j++)
+                if (i + j < n) {
+                    start[i + j] = ov[j];
+                    count[i + j] = 0u;
+                }
+        }
+        run += total;
+        __syncthreads();   // ws is rewritten by the next round
+    }
+    if (threadIdx.x == 0 && base + SCAN_TILE >= n) start[n] = run;   // the tile holding the last key
+}
+
+__global__ void __launch_bounds__(256) k_scan_reduce(const uint32_t *count, const PassState *st, long long fixed,
+                                                     uint32_t *block_sums) {
+    const long long n = scan_keys(st, fixed);
+    const long long ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    __shared__ uint32_t ws[8];
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) scan_reduce_tile(count, n, tile, block_sums, ws);
+}
+
+__global__ void __launch_bounds__(1024) k_scan_top(uint32_t *block_sums, const PassState *st, long long fixed) {
+    const long long n = scan_keys(st, fixed);
+    __shared__ uint32_t sh[1024];
+    scan_top_block(block_sums, (int)((n + SCAN_TILE - 1) / SCAN_TILE), sh);
+}
+
 __global__ void __launch_bounds__(256) k_scan_down(uint32_t *count, const PassState *st, long long fixed,
                                                    const uint32_t *block_sums, uint32_t *start) {
     const long long n = scan_keys(st, fixed);
     const long long ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
-    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ uint32_t ws[8];
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const long long base = tile * SCAN_TILE;
-        uint32_t run = block_sums[tile];   // keys before this tile
-#pragma unroll 1
-        for (int k = 0; k < SCAN_TILE / SCAN_ROUND; k++) {
-            const long long i = base + (long long)k * SCAN_ROUND + 4 * threadIdx.x;
-            const uint4 v = load_counts(count, i, n);
-            const uint32_t t = (v.x + v.y) + (v.z + v.w);
-            uint32_t incl = t;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= (unsigned)o) incl += u;
-            }
-            if (lane == 31) ws[warp] = incl;
-            __syncthreads();
-            uint32_t woff = 0, total = 0;
-#pragma unroll
-            for (int w = 0; w < 8; w++) {
-                const uint32_t x = ws[w];
-                woff += (unsigned)w < warp ? x : 0u;
-                total += x;
-            }
-            uint4 o;
-            o.x = run + woff + incl - t;
-            o.y = o.x + v.x;
-            o.z = o.y + v.y;
-            o.w = o.z + v.z;
-            if (i + 3 < n) {
-                *reinterpret_cast<uint4 *>(start + i) = o;
-                *reinterpret_cast<uint4 *>(count + i) = make_uint4(0u, 0u, 0u, 0u);
-            } else {
-                const uint32_t ov[4] = {o.x, o.y, o.z, o.w};
-                for (int j = 0; j < 4; j++)
-                    if (i + j < n) {
-                        start[i + j] = ov[j];
-                        count[i + j] = 0u;
-                    }
-            }
-            run += total;
-            __syncthreads();   // ws is rewritten by the next round
-        }
-        if (threadIdx.x == 0 && base + SCAN_TILE >= n) start[n] = run;   // the tile holding the last key
-    }
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+        scan_down_tile(count, n, tile, block_sums, start, ws);
 }
 
 __global__ void k_accum(const double *pass_img, double *sum, long long n) {
@@ -231,11 +252,78 @@ __global__ void k_accum(const double *pass_img, double *sum, long long n) {
         sum[i] += pass_img[i];
 }
 
-__global__ void k_pass_end(PassState *st) {
-    if (threadIdx.x != 0) return;
+__device__ __forceinline__ void pass_end_state(PassState *st) {
     double i = (double)(st->pass + st->offset);
     st->r2 = st->r2 * ((i + st->alpha) / (i + 1.0));
     st->pass += 1;
+}
+
+__global__ void k_pass_end(PassState *st) {
+    if (threadIdx.x != 0) return;
+    pass_end_state(st);
+}
+
+// ---- batched passes: per-job bookkeeping and the per-job scan ---------------
+__global__ void k_bt_begin(const JobDev *jobs, int njobs, BatchState *bs) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j == 0) {
+        bs->emit_next = 0;
+        bs->gather_next = 0;
+    }
+    if (j < njobs) pass_begin_state(jobs[j].st);
+}
+__global__ void k_bt_grid(const JobDev *jobs, int njobs) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < njobs) grid_setup_state(jobs[j].st, -1.0);
+}
+__global__ void k_bt_end(const JobDev *jobs, int njobs) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < njobs) pass_end_state(jobs[j].st);
+}
+
+// work items (job, scan tile) over every job's key counts
+__device__ __forceinline__ long long bt_scan_tiles(const JobDev *jobs, int njobs, long long *off) {
+    return batch_prefix(off, njobs, [&](int j) { return (jobs[j].st->grid.nkeys + SCAN_TILE - 1) / SCAN_TILE; });
+}
+__global__ void __launch_bounds__(256) k_bt_scan_reduce(const JobDev *jobs, int njobs) {
+    __shared__ long long off[BATCH_MAX_JOBS + 1];
+    __shared__ uint32_t ws[8];
+    const long long total = bt_scan_tiles(jobs, njobs, off);
+    for (long long it = blockIdx.x; it < total; it += gridDim.x) {
+        const int j = batch_job(off, njobs, it);
+        const JobDev &jd = jobs[j];
+        scan_reduce_tile(jd.count, jd.st->grid.nkeys, it - off[j], jd.block_sums, ws);
+    }
+}
+__global__ void __launch_bounds__(1024) k_bt_scan_top(const JobDev *jobs) {   // one block per job
+    __shared__ uint32_t sh[1024];
+    const JobDev &jd = jobs[blockIdx.x];
+    scan_top_block(jd.block_sums, (int)((jd.st->grid.nkeys + SCAN_TILE - 1) / SCAN_TILE), sh);
+}
+__global__ void __launch_bounds__(256) k_bt_scan_down(const JobDev *jobs, int njobs) {
+    __shared__ long long off[BATCH_MAX_JOBS + 1];
+    __shared__ uint32_t ws[8];
+    const long long total = bt_scan_tiles(jobs, njobs, off);
+    for (long long it = blockIdx.x; it < total; it += gridDim.x) {
+        const int j = batch_job(off, njobs, it);
+        const JobDev &jd = jobs[j];
+        scan_down_tile(jd.count, jd.st->grid.nkeys, it - off[j], jd.block_sums, jd.start, ws);
+    }
+}
+
+void launch_bt_begin(const JobDev *jobs, int njobs, BatchState *bs, cudaStream_t s) {
+    k_bt_begin<<<(njobs + 127) / 128, 128, 0, s>>>(jobs, njobs, bs);
+}
+void launch_bt_grid(const JobDev *jobs, int njobs, cudaStream_t s) {
+    k_bt_grid<<<(njobs + 127) / 128, 128, 0, s>>>(jobs, njobs);
+}
+void launch_bt_end(const JobDev *jobs, int njobs, cudaStream_t s) {
+    k_bt_end<<<(njobs + 127) / 128, 128, 0, s>>>(jobs, njobs);
+}
+void launch_bt_scan(const JobDev *jobs, int njobs, int grid, cudaStream_t s) {
+    k_bt_scan_reduce<<<grid, 256, 0, s>>>(jobs, njobs);
+    k_bt_scan_top<<<njobs, 1024, 0, s>>>(jobs);
+    k_bt_scan_down<<<grid, 256, 0, s>>>(jobs, njobs);
 }
 
 void launch_pass_begin(PassState *st, cudaStream_t s) { k_pass_begin<<<1, 32, 0, s>>>(st); }

@@ -1778,6 +1778,15 @@ struct ppm_batch {
     cudaStream_t s = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     std::string err;
+    // staged passes: one launch per stage over every job
+    int mode = PPM_BATCH_AUTO;
+    int sm_count = 0;
+    cudaStream_t s2 = nullptr;                 // the eye stages, beside the photon stages
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    void *jobs_d = nullptr, *offs_d = nullptr, *state_d = nullptr;   // job table, prefixes, counters
+    size_t jobs_cap = 0;
+    int tile = 0;                              // photons per map work item (0: tune)
+    int last_staged = 0, last_tile = 0;
 };
 
 static int batch_err(ppm_batch *b, int code, const char *fmt, ...) {
@@ -1800,7 +1809,11 @@ extern "C" int ppm_batch_create(ppm_batch **out, int device, uint64_t seed) {
     b->device = device;
     b->seed = seed;
     b->ctxs.push_back(probe);
+    b->sm_count = probe->sm_count;
     if (cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&b->s2, cudaStreamNonBlocking, eye_priority()) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreate(&b->e0) != cudaSuccess || cudaEventCreate(&b->e1) != cudaSuccess) {
         ppm_batch_destroy(b);
         return PPM_ERR_CUDA;
@@ -1813,15 +1826,236 @@ extern "C" int ppm_batch_destroy(ppm_batch *b) {
     if (!b) return PPM_OK;
     cudaSetDevice(b->device);
     if (b->s) cudaStreamSynchronize(b->s);
+    if (b->s2) cudaStreamSynchronize(b->s2);
     for (ppm_ctx *c : b->ctxs) ppm_ctx_destroy(c);
+    for (void *p : {b->jobs_d, b->offs_d, b->state_d})
+        if (p) cudaFree(p);
     if (b->e0) cudaEventDestroy(b->e0);
     if (b->e1) cudaEventDestroy(b->e1);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_join) cudaEventDestroy(b->ev_join);
     if (b->s) cudaStreamDestroy(b->s);
+    if (b->s2) cudaStreamDestroy(b->s2);
     delete b;
     return PPM_OK;
 }
 
+extern "C" int ppm_batch_set_mode(ppm_batch *b, int32_t mode, int32_t tile) {
+    if (!b || mode < PPM_BATCH_AUTO || mode > PPM_BATCH_GRAPHS || tile < 0 || tile > (1 << 20))
+        return PPM_ERR_INVALID_ARG;
+    b->mode = mode;
+    b->tile = tile;
+    return PPM_OK;
+}
+
+extern "C" int ppm_batch_info(const ppm_batch *b, int32_t *staged, int32_t *tile) {
+    if (!b) return PPM_ERR_INVALID_ARG;
+    if (staged) *staged = b->last_staged;
+    if (tile) *tile = b->last_tile;
+    return PPM_OK;
+}
+
 extern "C" const char *ppm_batch_last_error(const ppm_batch *b) { return b ? b->err.c_str() : ""; }
+
+// ---------------------------------------------------------------------------
+// Staged batched passes: every job keeps its own context (scene, camera,
+// buffers, pass state, cell tuning), and one pass of the whole batch is one
+// launch per stage over all jobs (ppm_batch.cuh): begin, the ten eye levels
+// (on a second stream), photon trace, map build (bounds, grid, histogram,
+// scan, scatter), gather, accumulate, end -- 22 launches for any number of
+// jobs, captured once as a CUDA graph.  Jobs that have rendered all their
+// passes leave the table (the graph is captured again for the rest).
+// ---------------------------------------------------------------------------
+namespace {
+
+// photons per work item of the map-build stages tried by the batch's tuner
+const int BATCH_TILES[] = {1024, 4096, 16384};
+
+JobDev job_dev(ppm_ctx *c) {
+    JobDev d{};
+    d.sv = c->sv_f;
+    d.cam = c->cam_f;
+    d.plan = c->plan;
+    d.st = c->st;
+    d.seed = c->cfg.seed;
+    d.raw = as<float4>(c->raw_f);
+    d.sorted = as<float4>(c->sorted_f);
+    d.count = as<uint32_t>(c->count);
+    d.start = as<uint32_t>(c->start);
+    d.block_sums = as<uint32_t>(c->block_sums);
+    d.keyrank = as<uint2>(c->keyrank);
+    d.hits = as<HitPoint<float>>(c->hits_f);
+    d.qa = EyeQueue<float>{as<float4>(c->eqb[0]), as<float4>(c->eqb[1]), as<float4>(c->eqb[2])};
+    d.qb = EyeQueue<float>{as<float4>(c->eqb[3]), as<float4>(c->eqb[4]), as<float4>(c->eqb[5])};
+    d.eq_cap = (unsigned long long)c->eq_cap;
+    d.direct = as<float>(c->pass_direct32);
+    d.gathered = as<float>(c->pass_gather32);
+    d.pass_img = as<double>(c->pass_img);
+    d.sum_img = as<double>(c->sum_img);
+    d.pw = c->pw;
+    d.npx = c->npx;
+    d.uc = c->cfg.use_classic ? 1 : 0;
+    d.pfilter = c->cam.pfilter;
+    return d;
+}
+
+}  // namespace
+
+// the job table and prefixes of the jobs in `act` to the device (nothing of
+// the batch may be running)
+static int batch_upload_table(ppm_batch *b, const std::vector<int> &act) {
+    const int nj = (int)act.size();
+    std::vector<JobDev> tab((size_t)nj);
+    std::vector<long long> offs(3 * (size_t)(nj + 1), 0);
+    long long *emit = offs.data(), *slots = emit + nj + 1, *px = slots + nj + 1;
+    for (int k = 0; k < nj; k++) {
+        ppm_ctx *c = b->ctxs[act[k]];
+        tab[k] = job_dev(c);
+        emit[k + 1] = emit[k] + c->plan.first[c->plan.n_lights];
+        slots[k + 1] = slots[k] + eye_slots(c->cam.xreso, c->cam.yreso);
+        px[k + 1] = px[k] + 3 * c->npx;
+    }
+    if (b->jobs_cap < (size_t)nj) {
+        for (void **p : {&b->jobs_d, &b->offs_d})
+            if (*p) { cudaFree(*p); *p = nullptr; }
+        b->jobs_cap = 0;
+        if (cudaMalloc(&b->jobs_d, sizeof(JobDev) * nj) != cudaSuccess ||
+            cudaMalloc(&b->offs_d, sizeof(long long) * 3 * (nj + 1)) != cudaSuccess)
+            return batch_err(b, PPM_ERR_OOM, "no device memory for the job table of %d jobs", nj);
+        b->jobs_cap = (size_t)nj;
+    }
+    if (!b->state_d && cudaMalloc(&b->state_d, sizeof(BatchState)) != cudaSuccess)
+        return batch_err(b, PPM_ERR_OOM, "no device memory for the batch counters");
+    CK_B(cudaMemcpyAsync(b->jobs_d, tab.data(), sizeof(JobDev) * nj, cudaMemcpyHostToDevice, b->s));
+    CK_B(cudaMemcpyAsync(b->offs_d, offs.data(), sizeof(long long) * offs.size(), cudaMemcpyHostToDevice, b->s));
+    CK_B(cudaStreamSynchronize(b->s));
+    return PPM_OK;
+}
+
+// one pass of the jobs in the uploaded table, captured as a graph
+static int batch_capture(ppm_batch *b, int nj, int tile, cudaGraphExec_t *exec) {
+    const JobDev *jd = static_cast<const JobDev *>(b->jobs_d);
+    const long long *emit = static_cast<const long long *>(b->offs_d), *slots = emit + nj + 1, *px = slots + nj + 1;
+    BatchState *bs = static_cast<BatchState *>(b->state_d);
+    const int sm = b->sm_count;
+    CK_B(cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal));
+    launch_bt_begin(jd, nj, bs, b->s);
+    cudaEventRecord(b->ev_fork, b->s);
+    cudaStreamWaitEvent(b->s2, b->ev_fork, 0);
+    for (int l = 0; l < MAX_TRACE; l++) launch_bt_eye(jd, nj, l, slots, sm * 4, b->s2);
+    cudaEventRecord(b->ev_join, b->s2);
+    launch_bt_trace(jd, nj, emit, bs, sm * 3, b->s);
+    launch_bt_map(jd, nj, tile, sm * 8, b->s);
+    cudaStreamWaitEvent(b->s, b->ev_join, 0);
+    launch_bt_gather(jd, nj, bs, sm * 4, b->s);
+    launch_bt_accum(jd, nj, px, sm * 8, b->s);
+    launch_bt_end(jd, nj, b->s);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(b->s, &g);
+    const cudaError_t le = cudaGetLastError();
+    if (e != cudaSuccess || le != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return batch_err(b, PPM_ERR_CUDA, "batch pass capture: %s",
+                         cudaGetErrorString(e != cudaSuccess ? e : le));
+    }
+    const cudaError_t ie = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return batch_err(b, PPM_ERR_CUDA, "batch pass graph: %s", cudaGetErrorString(ie));
+    return PPM_OK;
+}
+
+// every job's render begun (buffers, state, cells) with its cell size fixed
+static int batch_begin_jobs(ppm_batch *b, const ppm_job *jobs, int njobs, bool first) {
+    for (int j = 0; j < njobs; j++) {
+        ppm_ctx *c = b->ctxs[j];
+        ppm_render_cfg cfg = jobs[j].cfg;
+        cfg.use_graph = 0;
+        if (!first) {   // keep the cell size the first begin tuned
+            cfg.cell_factor = c->cell_factor;
+            cfg.flags &= ~PPM_RENDER_TUNE_CELLS;
+        }
+        int st = PPM_OK;
+        if (first) {
+            st = ppm_scene_upload(c, jobs[j].objs, jobs[j].n_objs, jobs[j].mats, jobs[j].n_mats, jobs[j].lights,
+                                  jobs[j].n_lights);
+            if (st == PPM_OK) st = ppm_camera_set(c, jobs[j].cam);
+        }
+        if (st == PPM_OK) st = ppm_render_begin(c, &cfg);
+        if (st != PPM_OK) return batch_err(b, st, "job %d: %s", j, c->err.c_str());
+    }
+    for (int j = 0; j < njobs; j++) CK_B(cudaStreamSynchronize(b->ctxs[j]->s));
+    return PPM_OK;
+}
+
+static int batch_render_staged(ppm_batch *b, const ppm_job *jobs, int njobs, double *device_ms) {
+    TRY(batch_begin_jobs(b, jobs, njobs, true));
+    std::vector<int> all((size_t)njobs);
+    for (int j = 0; j < njobs; j++) all[j] = j;
+    int tile = b->tile;
+    if (tile == 0) {
+        // tile tuner: one pass of the whole batch with each work-item size
+        // (one untimed, two timed), then every job begun again
+        TRY(batch_upload_table(b, all));
+        float best = 1e30f;
+        tile = BATCH_TILES[0];
+        for (int cand : BATCH_TILES) {
+            cudaGraphExec_t ex = nullptr;
+            TRY(batch_capture(b, njobs, cand, &ex));
+            float ms = 0.0f;
+            cudaError_t e = cudaGraphLaunch(ex, b->s);
+            if (e == cudaSuccess) e = cudaEventRecord(b->e0, b->s);
+            for (int r = 0; r < 2 && e == cudaSuccess; r++) e = cudaGraphLaunch(ex, b->s);
+            if (e == cudaSuccess) e = cudaEventRecord(b->e1, b->s);
+            if (e == cudaSuccess) e = cudaEventSynchronize(b->e1);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, b->e0, b->e1);
+            cudaGraphExecDestroy(ex);
+            if (e != cudaSuccess) return batch_err(b, PPM_ERR_CUDA, "batch tile tuner: %s", cudaGetErrorString(e));
+            if (ms < best) { best = ms; tile = cand; }
+        }
+        TRY(batch_begin_jobs(b, jobs, njobs, false));
+    }
+    int max_passes = 0;
+    for (int j = 0; j < njobs; j++) max_passes = std::max(max_passes, jobs[j].cfg.passes);
+    CK_B(cudaEventRecord(b->e0, b->s));
+    int p = 0;
+    while (p < max_passes) {
+        // the jobs still rendering, and the pass at which the next one is done
+        std::vector<int> act;
+        int until = max_passes;
+        for (int j = 0; j < njobs; j++)
+            if (jobs[j].cfg.passes > p) {
+                act.push_back(j);
+                until = std::min(until, jobs[j].cfg.passes);
+            }
+        TRY(batch_upload_table(b, act));
+        cudaGraphExec_t ex = nullptr;
+        TRY(batch_capture(b, (int)act.size(), tile, &ex));
+        int rc = PPM_OK;
+        for (; rc == PPM_OK && p < until; p++) {
+            cudaError_t e = cudaGraphLaunch(ex, b->s);
+            if (e != cudaSuccess) rc = batch_err(b, PPM_ERR_CUDA, "batch pass %d: %s", p, cudaGetErrorString(e));
+        }
+        CK_B(cudaStreamSynchronize(b->s));   // the table is rewritten for the next set of jobs
+        cudaGraphExecDestroy(ex);
+        if (rc != PPM_OK) return rc;
+    }
+    CK_B(cudaEventRecord(b->e1, b->s));
+    CK_B(cudaStreamSynchronize(b->s));
+    if (device_ms) {
+        float ms = 0.0f;
+        CK_B(cudaEventElapsedTime(&ms, b->e0, b->e1));
+        *device_ms = ms;
+    }
+    b->last_staged = 1;
+    b->last_tile = tile;
+    for (int j = 0; j < njobs; j++) {
+        ppm_ctx *c = b->ctxs[j];
+        c->passes_done = jobs[j].cfg.passes;
+        int st = ppm_render_image(c, jobs[j].image_out);
+        if (st != PPM_OK) return batch_err(b, st, "job %d: %s", j, c->err.c_str());
+    }
+    return PPM_OK;
+}
 
 extern "C" int ppm_batch_render(ppm_batch *b, const ppm_job *jobs, int32_t njobs, double *device_ms) {
     if (!b || njobs < 0 || (njobs && !jobs)) return PPM_ERR_INVALID_ARG;
@@ -1836,6 +2070,18 @@ extern "C" int ppm_batch_render(ppm_batch *b, const ppm_job *jobs, int32_t njobs
         if (st != PPM_OK) return batch_err(b, st, "context for job %zu: %s", b->ctxs.size(), ppm_last_error(nullptr));
         b->ctxs.push_back(c);
     }
+    // staged passes need every job to be a mixed-precision photon-mapping
+    // render with the default gather
+    bool staged = b->mode != PPM_BATCH_GRAPHS && njobs > 0 && njobs <= BATCH_MAX_JOBS;
+    for (int j = 0; j < njobs && staged; j++)
+        staged = jobs[j].cfg.precision == PPM_PRECISION_MIXED &&
+                 !(jobs[j].cfg.flags & (PPM_RENDER_CLASSIC | PPM_RENDER_TILE_GATHER));
+    if (b->mode == PPM_BATCH_STAGED && !staged)
+        return batch_err(b, PPM_ERR_INVALID_ARG, "staged batch passes take 1 to %d mixed-precision photon-mapping "
+                         "jobs with the default gather", BATCH_MAX_JOBS);
+    if (staged) return batch_render_staged(b, jobs, njobs, device_ms);
+    b->last_staged = 0;
+    b->last_tile = 0;
     int max_passes = 0;
     for (int j = 0; j < njobs; j++) {
         const ppm_job &jb = jobs[j];

@@ -2019,16 +2019,18 @@ __global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_estimate_tile(const 
                     if (__any_sync(0xffffffffu, bd))
                         if (bd) in = sq_euclid(f2d_here(q.x), f2d_here(q.y), f2d_here(q.z), (double)p.x, (double)p.y,
                                                (double)p.z) <= r2l;
-                    const uint32_t m = __float_as_uint(p.w);
-                    float inv;
-                    const V3<float> d = oct_raw(m, inv);
-                    const float bx = -d.x * inv, by = -d.y * inv, bz = -d.z * inv;
-                    const float cc = __fmaf_rn(nl.z, bz, __fmaf_rn(nl.y, by, nl.x * bx));
-                    const uint32_t term = fix_bits(in ? fmaxf(cc, 0.0f) : 0.0f) - FIX_BIAS;
-                    const uint32_t w = m >> 30;
-                    u0 += w == 0u ? term : 0u;
-                    u1 += w == 1u ? term : 0u;
-                    u2 += w >= 2u ? term : 0u;
+                    if (in) {   // the term of a photon in radius (most candidates are not)
+                        const uint32_t m = __float_as_uint(p.w);
+                        float inv;
+                        const V3<float> d = oct_raw(m, inv);
+                        const float bx = -d.x * inv, by = -d.y * inv, bz = -d.z * inv;
+                        const float cc = __fmaf_rn(nl.z, bz, __fmaf_rn(nl.y, by, nl.x * bx));
+                        const uint32_t term = fix_bits(fmaxf(cc, 0.0f)) - FIX_BIAS;
+                        const uint32_t w = m >> 30;
+                        u0 += w == 0u ? term : 0u;
+                        u1 += w == 1u ? term : 0u;
+                        u2 += w >= 2u ? term : 0u;
+                    }
                     if (COUNT) {
                         c_slots += 1;
                         c_tests += valid2 ? 1 : 0;
@@ -2179,6 +2181,73 @@ __global__ void k_intersect(SceneView<T, B> sc, const double *rays, long long n,
         t[i] = 0.0; obj[i] = -1;
         if (nrm) { nrm[3 * i] = 0.0; nrm[3 * i + 1] = 0.0; nrm[3 * i + 2] = 0.0; }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Batched passes: one launch per stage runs that stage for every job of a
+// batch (k_batch.cu, and the per-job bookkeeping in k_grid.cu).  A job is a
+// mixed-precision render with its own scene, camera, buffers and pass state;
+// the stage kernels map their work items -- (job, element) -- onto the
+// concatenation of the jobs' work, through a prefix of the jobs' counts.
+// ---------------------------------------------------------------------------
+constexpr int BATCH_MAX_JOBS = 256;   // the prefix of job counts lives in one block's shared memory
+
+struct JobDev {
+    SceneView<float> sv;          // bvh != nullptr: rays walk the hierarchy
+    DCamera<float> cam;
+    EmitPlan plan;
+    PassState *st;
+    uint64_t seed;
+    float4 *raw, *sorted;         // stored photons and the photon map
+    uint32_t *count, *start, *block_sums;
+    uint2 *keyrank;
+    HitPoint<float> *hits;
+    EyeQueue<float> qa, qb;
+    unsigned long long eq_cap;
+    float *direct, *gathered;
+    double *pass_img, *sum_img;
+    double pw;
+    long long npx;
+    int32_t uc, pfilter;
+};
+
+// counters the stages take their work from (reset by the batch's first stage)
+struct BatchState {
+    unsigned long long emit_next, gather_next;
+};
+
+// prefix[j] = sum of count(k) for k < j, prefix[njobs] = total, in shared
+// memory; the block's threads (at least njobs of them) load one count each
+template <typename F>
+__device__ __forceinline__ long long batch_prefix(long long *prefix, int njobs, F count) {
+    __shared__ long long wsum[32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    long long v = t < njobs ? count(t) : 0;
+    long long incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    long long before = 0;
+    for (int k = 0; k < w; k++) before += wsum[k];
+    if (t < njobs) prefix[t] = before + incl - v;
+    if (t == (int)blockDim.x - 1) prefix[njobs] = before + incl;
+    __syncthreads();
+    return prefix[njobs];
+}
+
+// the job of flattened index x: the last j with prefix[j] <= x
+__device__ __forceinline__ int batch_job(const long long *prefix, int njobs, long long x) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
 }  // namespace ppm

@@ -109,4 +109,19 @@ void launch_accum_mixed(const float *direct, const float *gathered, const PassSt
 void launch_pass_end(PassState *st, cudaStream_t s);
 int kernels_per_scan();
 
+// ---- batched passes (ppm_batch.cuh in k_f32.cu; per-job bookkeeping and scan in k_grid.cu) ----
+// one launch per stage over every job of the table (njobs <= BATCH_MAX_JOBS);
+// tile is the photons per work item of the map-build stages
+void launch_bt_begin(const JobDev *jobs, int njobs, BatchState *bs, cudaStream_t s);
+void launch_bt_grid(const JobDev *jobs, int njobs, cudaStream_t s);
+void launch_bt_end(const JobDev *jobs, int njobs, cudaStream_t s);
+void launch_bt_scan(const JobDev *jobs, int njobs, int grid, cudaStream_t s);
+void launch_bt_trace(const JobDev *jobs, int njobs, const long long *emit_off, BatchState *bs, int grid,
+                     cudaStream_t s);
+void launch_bt_map(const JobDev *jobs, int njobs, int tile, int grid, cudaStream_t s);
+void launch_bt_eye(const JobDev *jobs, int njobs, int level, const long long *slot_off, int grid, cudaStream_t s);
+void launch_bt_gather(const JobDev *jobs, int njobs, BatchState *bs, int grid, cudaStream_t s);
+void launch_bt_accum(const JobDev *jobs, int njobs, const long long *px_off, int grid, cudaStream_t s);
+int kernels_per_bt_map();
+
 }  // namespace ppm

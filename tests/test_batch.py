@@ -39,6 +39,64 @@ def test_batch_images_equal_single_renders():
             assert want.max() > 0
 
 
+def _mixed_jobs():
+    """Mixed-precision photon-mapping jobs of every kind a staged batch takes:
+    small and large images, a mesh walked through its BVH, a parallelogram
+    light, uneven photon budgets and pass counts."""
+    rng = np.random.default_rng(5)
+    return [
+        (S.box_scene("c1"), S.box_camera(64), RenderConfig(nphoton=30000, passes=4, radius0=0.08, seed=21)),
+        (S.box_scene("c2"), S.box_camera(96), RenderConfig(nphoton=50000, passes=2, radius0=0.06, alpha=0.5,
+                                                           seed=22)),
+        (M.mesh_scene(3), S.box_camera(80), RenderConfig(nphoton=40000, passes=3, radius0=0.07, seed=23)),
+        (W.batch_scene(rng, 3000), S.box_camera(72), RenderConfig(nphoton=20000, passes=5, radius0=0.05, seed=24)),
+        (W.batch_scene(rng, 40), S.box_camera(40), RenderConfig(nphoton=60000, passes=1, radius0=0.09, seed=25,
+                                                               flags=1)),
+    ]
+
+
+def test_staged_batch_images_equal_single_renders():
+    """One launch per stage over all jobs gives each job the image of its own
+    render (the same paths and neighbour sets; FP32 sums in another order)."""
+    from ppmpa_gb300.api import BATCH_STAGED
+    jobs = _mixed_jobs()
+    with Batch(0, seed=1) as b:
+        b.set_mode(BATCH_STAGED)
+        imgs, ms = b.render(jobs)
+        info = b.info()
+    assert info["staged"] and info["tile"] > 0 and ms > 0
+    with Context(0, seed=1) as ctx:
+        for (sc, cam, cfg), img in zip(jobs, imgs):
+            ctx.upload_scene(sc)
+            ctx.set_camera(cam)
+            want = ctx.render(cfg)
+            assert img.shape == want.shape
+            assert np.allclose(img, want, rtol=1e-5, atol=1e-5 * want.max()), cfg
+            assert want.max() > 0
+
+
+def test_staged_and_graph_batches_agree():
+    from ppmpa_gb300.api import BATCH_GRAPHS, BATCH_STAGED
+    jobs = _mixed_jobs()[:3]
+    out = {}
+    with Batch(0, seed=1) as b:
+        for mode in (BATCH_STAGED, BATCH_GRAPHS):
+            b.set_mode(mode, tile=4096)
+            out[mode], _ = b.render(jobs)
+            assert b.info()["staged"] == (mode == BATCH_STAGED)
+    for a, g in zip(out[BATCH_STAGED], out[BATCH_GRAPHS]):
+        assert np.allclose(a, g, rtol=1e-5, atol=1e-5 * g.max())
+
+
+def test_staged_batch_refuses_plain_jobs():
+    from ppmpa_gb300 import PPMError
+    from ppmpa_gb300.api import BATCH_STAGED
+    with Batch(0, seed=1) as b:
+        b.set_mode(BATCH_STAGED)
+        with pytest.raises(PPMError, match="staged batch passes"):
+            b.render(_jobs()[:2])
+
+
 def test_cell_tuning_changes_only_speed():
     sc, cam = S.box_scene("c2"), S.box_camera(96)
     with Context(0, seed=1) as ctx:
