@@ -747,6 +747,78 @@ __device__ __forceinline__ RowSet make_rows(const GridParams &g, const uint32_t 
     return rs;
 }
 
+// Packed rows: a group's non-empty rows laid end to end, walked in windows
+// of 32 positions, so that a row of 9 candidates and the next of 40 fill
+// two windows rather than three mostly idle ones.  Position p of the
+// concatenation is in the row whose start is the last one at or before p:
+// a window ORs the bits (start - window base) of the starts that fall in
+// it (one reduction), and lane i counts the bits at or below i.  Lane k of
+// the warp holds, for the k-th non-empty row, the map slot of its first
+// candidate minus its start, so the slot of position p is one shuffle and
+// one add away.  No search, no shared memory.
+struct PackedRows {
+    uint32_t total;   // candidates in the group's rows
+    uint32_t first;   // this lane's row's start in the concatenation (0x80000000: empty row)
+    uint32_t delta;   // lane k: k-th non-empty row's first slot minus its start
+};
+
+__device__ __forceinline__ unsigned lanemask_le() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_le;" : "=r"(m));
+    return m;
+}
+
+// position of the k-th (from 0) set bit of m; any value in [0, 31] when m
+// has k or fewer set bits
+__device__ __forceinline__ int kth_set_bit(unsigned m, int k) {
+    int pos = 0;
+#pragma unroll
+    for (int w = 16; w > 0; w >>= 1) {
+        const int c = __popc(m & ((1u << w) - 1u));
+        if (k >= c) {
+            k -= c;
+            m >>= w;
+            pos += w;
+        }
+    }
+    return pos;
+}
+
+// lane i holds row i of the group (first slot rbeg, rlen candidates);
+// nonempty is the ballot of rlen > 0
+__device__ __forceinline__ PackedRows pack_rows(uint32_t rbeg, uint32_t rlen, unsigned nonempty) {
+    const unsigned lane = lane_id();
+    uint32_t incl = rlen;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (unsigned)o) incl += t;
+    }
+    PackedRows pr;
+    pr.total = __shfl_sync(0xffffffffu, incl, 31);
+    const uint32_t s = incl - rlen;
+    pr.first = rlen > 0u ? s : 0x80000000u;
+    pr.delta = __shfl_sync(0xffffffffu, rbeg - s, kth_set_bit(nonempty, (int)lane));
+    return pr;
+}
+
+// map slot of position wb + lane (the window at wb; windows in increasing
+// order, kbase = -1 before the first); valid = the position holds a
+// candidate.  Past the end the slot is the last candidate's, so loads stay
+// in bounds.  All lanes must call it.
+__device__ __forceinline__ uint32_t packed_slot(const PackedRows &pr, uint32_t wb, unsigned le, int &kbase,
+                                                bool &valid) {
+    unsigned bit;
+    // PTX clamps shift counts above 31: starts outside the window give 0
+    asm("shl.b32 %0, %1, %2;" : "=r"(bit) : "r"(1u), "r"(pr.first - wb));
+    const unsigned m = __reduce_or_sync(0xffffffffu, bit);
+    const int k = kbase + __popc(m & le);
+    kbase += __popc(m);
+    const uint32_t p = wb + lane_id();
+    valid = p < pr.total;
+    return min(p, pr.total - 1u) + __shfl_sync(0xffffffffu, pr.delta, k);
+}
+
 // calls f(photon_index, valid) for every candidate of the query, lanes in
 // parallel; all lanes of the warp must enter (warp-uniform query)
 template <typename T, typename F>
@@ -772,38 +844,58 @@ __device__ __forceinline__ void for_each_candidate(const GridParams &g, const ui
     }
 }
 
-// The render row walk: the steps of for_each_candidate, two candidates per
-// lane per step (both loaded before either is used), handed to one call, use(two, p0, valid0, slot0,
-// p1, valid1, slot1), so that their radius tests and direction decodes form
-// two independent instruction chains in one block (one branch per step
-// instead of two).  A step over a row's last 32 or fewer candidates passes
-// two = std::false_type and no second photon, so that the body compiled for
-// it does one candidate's work.  Every lane makes every call, so use() may
-// hold warp votes.  The slots (map positions) are used by the parity export
-// only; the production body ignores them.
+// for_each_candidate over packed rows: f(slot, valid) once per window of 32
+// positions of the group's rows laid end to end (slots of invalid lanes are
+// in bounds); all lanes of the warp must enter
+template <typename T, typename F>
+__device__ __forceinline__ void for_each_candidate_packed(const GridParams &g, const uint32_t *start, V3<T> q, T r2,
+                                                          const int lo[3], const int hi[3], F &&f) {
+    const int nrows = (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+    const unsigned le = lanemask_le();
+    for (int row0 = 0; row0 < nrows; row0 += 32) {
+        const RowSet rs = make_rows(g, start, q, r2, lo, hi, row0);
+        if (rs.nonempty == 0u) continue;
+        const PackedRows pr = pack_rows(rs.begin, rs.len, rs.nonempty);
+        int kbase = -1;
+        for (uint32_t win = 0; win < pr.total; win += 32) {
+            bool v;
+            const uint32_t slot = packed_slot(pr, win, le, kbase, v);
+            f(slot, v);
+        }
+    }
+}
+
+// The render row walk: the group's rows packed end to end (pack_rows), two
+// windows per step (both candidates loaded before either is used), handed
+// to one call, use(two, p0, valid0, slot0, p1, valid1, slot1), so that
+// their radius tests and direction decodes form two independent
+// instruction chains in one block (one branch per step instead of two).  A
+// step over the last 32 or fewer positions passes two = std::false_type
+// and no second photon, so that the body compiled for it does one
+// candidate's work.  Every lane makes every call, so use() may hold warp
+// votes.  The slots (map positions) are used by the parity export only;
+// the production body ignores them.
 template <typename U>
 __device__ __forceinline__ void for_each_candidate_two(const GridParams &g, const uint32_t *start, V3<float> q,
                                                        float r2, const int lo[3], const int hi[3],
                                                        const float4 *smap, U &&use) {
     const int nrows = (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+    const unsigned le = lanemask_le();
     for (int row0 = 0; row0 < nrows; row0 += 32) {
-        RowSet rs = make_rows(g, start, q, r2, lo, hi, row0);
-        unsigned m = rs.nonempty;
-        while (m) {
-            int r = __ffs(m) - 1;
-            m &= m - 1;
-            const uint32_t b = __shfl_sync(0xffffffffu, rs.begin, r);
-            const uint32_t n = __shfl_sync(0xffffffffu, rs.len, r);
-            for (uint32_t base = 0; base < n; base += 64) {
-                const uint32_t o0 = base + lane_id(), o1 = o0 + 32;
-                const bool v0 = o0 < n, v1 = o1 < n;
-                const float4 p0 = __ldg(&smap[v0 ? b + o0 : b]);
-                if (base + 32 < n) {
-                    const float4 p1 = __ldg(&smap[v1 ? b + o1 : b]);
-                    use(std::true_type{}, p0, v0, b + o0, p1, v1, b + o1);
-                } else {
-                    use(std::false_type{}, p0, v0, b + o0, p0, false, b);   // the row's last 32 or fewer
-                }
+        const RowSet rs = make_rows(g, start, q, r2, lo, hi, row0);
+        if (rs.nonempty == 0u) continue;
+        const PackedRows pr = pack_rows(rs.begin, rs.len, rs.nonempty);
+        int kbase = -1;
+        for (uint32_t wb = 0; wb < pr.total; wb += 64) {
+            bool v0, v1;
+            const uint32_t i0 = packed_slot(pr, wb, le, kbase, v0);
+            const float4 p0 = __ldg(&smap[i0]);
+            if (wb + 32 < pr.total) {
+                const uint32_t i1 = packed_slot(pr, wb + 32, le, kbase, v1);
+                const float4 p1 = __ldg(&smap[i1]);
+                use(std::true_type{}, p0, v0, i0, p1, v1, i1);
+            } else {
+                use(std::false_type{}, p0, v0, i0, p0, false, i0);   // the last 32 or fewer
             }
         }
     }
@@ -1047,6 +1139,7 @@ __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, cons
     uint32_t na_in = 0, nb_in = 0;             // export only
     unsigned long long ha_in = 0, hb_in = 0;   // export only
     const int ny = hi[1] - lo[1] + 1, nrows = ny * (hi[2] - lo[2] + 1);
+    const unsigned le = lanemask_le();
     for (int row0 = 0; row0 < nrows; row0 += 32) {
         // lane's row: the union of the two queries' chord ranges
         uint32_t rbeg = 0, rlen = 0;
@@ -1065,16 +1158,15 @@ __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, cons
                 rlen = start[3 * (base + x1 + 1)] - rbeg;
             }
         }
-        unsigned m = __ballot_sync(0xffffffffu, rlen > 0);
-        while (m) {
-            const int r = __ffs(m) - 1;
-            m &= m - 1;
-            const uint32_t b = __shfl_sync(0xffffffffu, rbeg, r);
-            const uint32_t n = __shfl_sync(0xffffffffu, rlen, r);
-            for (uint32_t base = 0; base < n; base += 32) {
-                const uint32_t o = base + lane;
-                const bool v = o < n;
-                const float4 p = __ldg(&smap[v ? b + o : b]);
+        const unsigned nonempty = __ballot_sync(0xffffffffu, rlen > 0);
+        if (nonempty == 0u) continue;
+        const PackedRows pr = pack_rows(rbeg, rlen, nonempty);
+        int kbase = -1;
+        {
+            for (uint32_t win = 0; win < pr.total; win += 32) {
+                bool v;
+                const uint32_t slot = packed_slot(pr, win, le, kbase, v);
+                const float4 p = __ldg(&smap[slot]);
                 float dx = qa.x - p.x, dy = qa.y - p.y, dz = qa.z - p.z;
                 const float da = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
                 dx = qb.x - p.x;
@@ -1094,7 +1186,7 @@ __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, cons
                     c_hits += (int)ia + (int)ib;
                 }
                 if (DUMP && (ia || ib)) {
-                    const unsigned long long hm = slot_mix(b + o);
+                    const unsigned long long hm = slot_mix(slot);
                     na_in += ia ? 1u : 0u;
                     nb_in += ib ? 1u : 0u;
                     ha_in += ia ? hm : 0ull;
@@ -1814,7 +1906,7 @@ __global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_estimate_tile(const 
     const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
     float4 *const sp = s_pos[wid], *const sd = s_dir[wid];
     TileBox &box = s_box[wid];
-    const unsigned lt = (1u << lane) - 1u;
+    const unsigned lt = (1u << lane) - 1u, le = lanemask_le();
     const GridParams g = st->grid;
     constexpr float FAR = 1e30f;
     unsigned long long c_tests = 0, c_slots = 0, c_hits = 0;
@@ -1914,26 +2006,16 @@ __global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_estimate_tile(const 
                             rlen = start[3 * (base + x1 + 1)] - rbeg;
                         }
                     }
-                    uint32_t incl = rlen;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
-                        if (lane >= (unsigned)o) incl += u;
-                    }
-                    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-                    const uint32_t excl = incl - rlen;
-                    for (uint32_t b0 = 0; b0 < total; b0 += 32) {
-                        const uint32_t j = b0 + lane;
-                        int r = 0;
-#pragma unroll
-                        for (int step = 16; step > 0; step >>= 1)
-                            if (__shfl_sync(0xffffffffu, incl, r + step - 1) <= j) r += step;
-                        const uint32_t rb = __shfl_sync(0xffffffffu, rbeg, r), rx = __shfl_sync(0xffffffffu, excl, r);
-                        const bool v = j < total;
+                    const unsigned nonempty = __ballot_sync(0xffffffffu, rlen > 0);
+                    if (nonempty == 0u) continue;
+                    const PackedRows pr = pack_rows(rbeg, rlen, nonempty);
+                    int kbase = -1;
+                    for (uint32_t b0 = 0; b0 < pr.total; b0 += 32) {
+                        bool v;
+                        const uint32_t slot = packed_slot(pr, b0, le, kbase, v);
                         uint32_t wl = 3u;
                         float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pd = pa;
                         if (v) {
-                            const uint32_t slot = rb + (j - rx);
                             const float4 p = __ldg(&smap[slot]);
                             const uint32_t m = __float_as_uint(p.w);
                             float inv;
@@ -2010,7 +2092,7 @@ __global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_estimate_tile(const 
                 int c[3], lo[3], hi[3];
                 query_cells(g, q, ext, extx, c, lo, hi);
                 unsigned long long u0 = 0, u1 = 0, u2 = 0;
-                for_each_candidate(g, start, q, rl * rl, lo, hi, [&](uint32_t idx, bool valid2) {
+                for_each_candidate_packed(g, start, q, rl * rl, lo, hi, [&](uint32_t idx, bool valid2) {
                     const float4 p = __ldg(&smap[idx]);
                     const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
                     const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));

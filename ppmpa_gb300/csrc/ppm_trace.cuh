@@ -56,6 +56,35 @@ __device__ __forceinline__ bool method_moller(T l, V3<T> p0, V3<T> d1, V3<T> d2,
     return true;
 }
 
+// FP32: every product and sum rounded as written.  Left to the compiler,
+// a cross product x*y - z*w contracts to fma(x, y, -z*w) or fma(-z, w, x*y)
+// depending on the code around it, so two kernels that inline the test (a
+// single render's trace and a batch's) could disagree in the last bit near
+// an edge and send a ray to a neighbouring triangle.
+__device__ __forceinline__ float dot_rn(V3<float> a, V3<float> b) {
+    return __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, __fmul_rn(a.x, b.x)));
+}
+__device__ __forceinline__ V3<float> cross_rn(V3<float> a, V3<float> b) {
+    return mk3(__fmaf_rn(a.y, b.z, -__fmul_rn(a.z, b.y)), __fmaf_rn(a.z, b.x, -__fmul_rn(a.x, b.z)),
+               __fmaf_rn(a.x, b.y, -__fmul_rn(a.y, b.x)));
+}
+template <>
+__device__ __forceinline__ bool method_moller<float>(float l, V3<float> p0, V3<float> d1, V3<float> d2, V3<float> p,
+                                                     V3<float> d, float &t) {
+    const V3<float> re2 = cross_rn(d, d2);
+    const float det_a = dot_rn(re2, d1);
+    if (det_a == 0.0f) return false;
+    const float inv = __frcp_rn(det_a);
+    const V3<float> pp = mk3(__fsub_rn(p.x, p0.x), __fsub_rn(p.y, p0.y), __fsub_rn(p.z, p0.z));
+    const float u = __fmul_rn(dot_rn(re2, pp), inv);
+    if (u < 0.0f || u > 1.0f) return false;
+    const V3<float> te1 = cross_rn(pp, d1);
+    const float v = __fmul_rn(dot_rn(te1, d), inv);
+    if (v < 0.0f || v > 1.0f || __fadd_rn(u, v) > l) return false;
+    t = __fmul_rn(dot_rn(te1, d2), inv);
+    return true;
+}
+
 template <typename T>
 __device__ __forceinline__ int shape_distance(const DObject<T> &o, V3<T> rp, V3<T> rd, T &ta, T &tb) {
     switch (o.shape) {
