@@ -57,9 +57,12 @@ SWEEPS = {"gather_sweep_uniform": "uniform", "gather_sweep_clustered": "clustere
 SWEEP_MAX_STEPS = {"uniform": 10, "clustered": 3}
 # 64 seeded render jobs of uneven sizes (ppmpa_gb300/workloads.py batch_jobs),
 # 8 passes each, rendered as one batch (one graph launch per pass for all jobs)
-BATCHES = {"batch_64": dict(n_jobs=64, passes=8)}
+BATCHES = {"batch_64": dict(n_jobs=64, passes=8),
+           # many small jobs: per-job graphs cost 22 kernel nodes each per pass
+           "batch_256_small": dict(n_jobs=256, passes=8, prims=(10, 2000), reso=(48, 128),
+                                   photons=(20_000, 100_000))}
 # the configurations measured beside the headline, in this order
-SECONDARY = ["box_256", "mesh_1024", "gather_sweep_uniform", "gather_sweep_clustered", "batch_64"]
+SECONDARY = ["box_256", "mesh_1024", "gather_sweep_uniform", "gather_sweep_clustered", "batch_64", "batch_256_small"]
 L2_BYTES = 129 * 1024 * 1024
 
 
@@ -92,6 +95,8 @@ def parse():
     p.add_argument("--cell-factor", type=int, default=0, help="grid cells per radius (0: tuned per render)")
     p.add_argument("--nphoton", type=int, default=0, help="photons per pass (0: the workload's); for profiling")
     p.add_argument("--tile-gather", action="store_true", help="mixed render: the tile gather (comparison)")
+    p.add_argument("--batch-legs", default="staged,graphs,sequential",
+                   help="batch workloads: which of the staged, graphs and sequential legs to run (staged always runs)")
     return p.parse_args()
 
 
@@ -403,7 +408,8 @@ def measure_render(args, name, w, ctx, stream, flush, world, rank, local, headli
     peak, peak_src = hbm_peak()
     ab = algorithmic_bytes(dominant, st_t, npx)
     achieved = ab / (stage_avg[dominant] / 1e3) / 1e9
-    summary = profile_summary(f"{dominant}:{name}")
+    # the gather's counts depend on the grid: its summaries are keyed by cells per radius
+    summary = profile_summary(f"{dominant}:{name}" + (f":k{cells}" if dominant == "gather" else ""))
 
     stage_roof = {}
     for k, t in stage_avg.items():
@@ -710,31 +716,42 @@ def run_sweep_reference(args, kind):
 # ---------------------------------------------------------------------------
 def measure_batch(args, name, bw):
     """A step = one pass of every job.  value: photons of all jobs per second
-    of batch device time; sequential: the same jobs rendered one after
-    another, each with its own pass graph; e2e: Batch.render wall time
-    (scene uploads, BVH builds, cell tuning, graph capture, passes, images)."""
+    of batch device time, in the mode PPM_BATCH_AUTO picked (its trial, on
+    the warm-up render, times one pass of staged passes and one of the jobs'
+    graphs side by side, and keeps the faster); the other mode and the jobs
+    rendered one after another are timed beside it; e2e: Batch.render wall
+    time (scene uploads, BVH builds, cell tuning, graph capture, passes,
+    images)."""
     import torch
     from ppmpa_gb300 import Batch, Context, workloads as W
-    from ppmpa_gb300.api import BATCH_GRAPHS, BATCH_STAGED
-    jobs = W.batch_jobs(bw["n_jobs"], seed=args.seed + 6, passes=bw["passes"])
+    from ppmpa_gb300.api import BATCH_AUTO, BATCH_GRAPHS, BATCH_STAGED
+    jobs = W.batch_jobs(bw["n_jobs"], seed=args.seed + 6, passes=bw["passes"],
+                        **{k: bw[k] for k in ("prims", "reso", "photons") if k in bw})
     photons = sum(cfg.nphoton for _, _, cfg in jobs) * bw["passes"]
+    legs = args.batch_legs.split(",")
     with Batch(0, seed=args.seed) as b:
-        b.set_mode(BATCH_STAGED)
-        b.render(jobs)                                   # warm-up: allocations, module loads, tile tuning
-        tile = b.info()["tile"]
-        b.set_mode(BATCH_STAGED, tile)                   # the tuned tile, as a repeat caller passes it
+        b.set_mode(BATCH_AUTO)
+        b.render(jobs)                                   # warm-up: allocations, module loads, AUTO's trial
+        info = b.info()
+        picked = "staged" if info["staged"] else "graphs"
         clocks = Clocks(0)
         clocks.start()
         t0 = time.perf_counter()
-        imgs, dev_ms = b.render(jobs)
+        imgs, dev_ms = b.render(jobs)                    # AUTO keeps its pick
         wall = time.perf_counter() - t0
         clk = clocks.stop()
-        b.set_mode(BATCH_GRAPHS)                         # the jobs' own pass graphs side by side
-        b.render(jobs)
-        _, graphs_ms = b.render(jobs)
-    seq_ms = 0.0
+        mode_ms = {picked: dev_ms}
+        if "staged" in legs and picked != "staged":
+            b.set_mode(BATCH_STAGED, info["tile"])
+            b.render(jobs)
+            _, mode_ms["staged"] = b.render(jobs)
+        if "graphs" in legs and picked != "graphs":
+            b.set_mode(BATCH_GRAPHS)
+            b.render(jobs)
+            _, mode_ms["graphs"] = b.render(jobs)
+    seq_ms = None if "sequential" not in legs else 0.0
     with Context(0, seed=args.seed) as ctx:
-        for sc, cam, cfg in jobs:
+        for sc, cam, cfg in (jobs if seq_ms is not None else []):
             ctx.upload_scene(sc)
             ctx.set_camera(cam)
             ctx.render_begin(cfg)
@@ -748,8 +765,14 @@ def measure_batch(args, name, bw):
             torch.cuda.synchronize()
             seq_ms += a.elapsed_time(e)
     prims = [sc.n_objects for sc, _, _ in jobs]
+
+    def rate(ms):
+        return None if ms is None else {"value": photons / (ms / 1e3) / 1e6, "unit": "Mphotons/s", "ms": ms}
+    # kernels of this library launched in the timed render: 22 per staged pass
+    # of the batch, or 22 per pass of every job inside the parent graphs
+    launches = 22 * bw["passes"] if picked == "staged" else 22 * sum(cfg.passes for _, _, cfg in jobs)
     return {
-        "metric": f"batched render Mphotons/s ({len(jobs)} uneven jobs, one launch per stage per pass over all jobs)",
+        "metric": f"batched render Mphotons/s ({len(jobs)} uneven jobs, all passes of every job)",
         "value": photons / (dev_ms / 1e3) / 1e6, "unit": "Mphotons/s", "steps": bw["passes"],
         "warmup": 1, "ms_per_step": dev_ms / bw["passes"], "higher_is_better": True,
         "dtype": "f32 trace/gather, f64 radius/average", "data": "synthetic (seeded scenes)",
@@ -757,23 +780,27 @@ def measure_batch(args, name, bw):
                    "primitives": [min(prims), max(prims), sum(prims)],
                    "photons_per_pass": [min(c.nphoton for _, _, c in jobs), max(c.nphoton for _, _, c in jobs)],
                    "reso": [min(c.xreso for _, c, _ in jobs), max(c.xreso for _, c, _ in jobs)],
-                   "cell_tuning": True, "staged_tile": tile},
-        "graphs": {"value": photons / (graphs_ms / 1e3) / 1e6, "unit": "Mphotons/s", "ms": graphs_ms,
-                   "note": "each job's pass graph, all jobs' graphs in one parent graph per pass"},
-        "staged_over_graphs": graphs_ms / dev_ms,
-        "gpu_launches": 22 * bw["passes"],
-        "sequential": {"value": photons / (seq_ms / 1e3) / 1e6, "unit": "Mphotons/s", "ms": seq_ms},
-        "batch_over_sequential": seq_ms / dev_ms,
+                   "cell_tuning": True, "mode": picked, "staged_tile": info["tile"],
+                   "auto_trial_ms_per_pass": info.get("trial_ms")},
+        "staged": rate(mode_ms.get("staged")),
+        "graphs": dict(rate(mode_ms.get("graphs")) or {},
+                       note="each job's pass graph, all jobs' graphs in one parent graph per pass")
+        if mode_ms.get("graphs") is not None else None,
+        "staged_over_graphs": (mode_ms["graphs"] / mode_ms["staged"]
+                               if mode_ms.get("staged") and mode_ms.get("graphs") else None),
+        "gpu_launches": launches,
+        "sequential": rate(seq_ms),
+        "batch_over_sequential": None if seq_ms is None else seq_ms / dev_ms,
         "e2e": {"value": photons / wall / 1e6, "unit": "Mphotons/s",
                 "h2d_bytes_per_step": sum(120 * sc.n_objects + 168 * len(sc.materials) + 160 * len(sc.lights) + 336
                                           for sc, _, _ in jobs),
                 "d2h_bytes_per_step": sum(i.nbytes for i in imgs),
                 "step": "Batch.render: uploads, BVH builds, cell tuning, capture, all passes, images"},
         "cpu_baseline": None,
-        "cpu_baseline_note": ("no CPU leg: the reference tests every object per ray (up to 200k here) and renders "
-                              "one scene per process; the per-configuration CPU rates are under box_256 and "
-                              "mesh_1024"),
-        "mean_radiance": float(np.mean([i.mean() for i in imgs])), "clocks": clk,
+        "cpu_baseline_note": ("no CPU leg: the reference tests every object per ray and renders one scene per "
+                              "process; the per-configuration CPU rates are under box_256 and mesh_1024"),
+        "nonfinite_pixels": int(sum(int((~np.isfinite(i)).any(axis=-1).sum()) for i in imgs)),
+        "mean_radiance": float(np.mean([np.nanmean(i) for i in imgs])), "clocks": clk,
     }
 
 

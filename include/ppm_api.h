@@ -400,14 +400,20 @@ int         ppm_batch_render(ppm_batch *b, const ppm_job *jobs, int32_t njobs, d
  * for 1 to 256 jobs that are all mixed-precision photon-mapping renders with
  * the default gather.  PPM_BATCH_GRAPHS: each job's own pass graph, the
  * jobs' graphs side by side in one parent graph per pass (any jobs).
- * PPM_BATCH_AUTO (default): staged when the jobs allow it.  tile: photons per
- * work item of the staged map-build stages; 0 (default) times 1024, 4096 and
- * 16384 on one pass of the batch before the render and keeps the fastest.
+ * PPM_BATCH_AUTO (default): when the jobs allow staged passes, the first
+ * render times one pass of each mode on its jobs (the staged one after the
+ * tile tuner) and keeps the faster for this and later renders, until the
+ * next ppm_batch_set_mode; otherwise graphs.  tile: photons per work item of
+ * the staged map-build stages; 0 (default) times 1024, 4096 and 16384 on one
+ * pass of the batch before the render and keeps the fastest.
  * No reference counterpart. */
 enum { PPM_BATCH_AUTO = 0, PPM_BATCH_STAGED = 1, PPM_BATCH_GRAPHS = 2 };
 int         ppm_batch_set_mode(ppm_batch *b, int32_t mode, int32_t tile);
 /* how the last render ran: staged (1) or graphs (0), and the tile it used */
 int         ppm_batch_info(const ppm_batch *b, int32_t *staged, int32_t *tile);
+/* AUTO's trial: ms per pass of the staged and graph modes it measured
+ * (PPM_ERR_NOT_READY before the first AUTO render of staged-capable jobs) */
+int         ppm_batch_trial_ms(const ppm_batch *b, double *staged_ms, double *graphs_ms);
 
 #ifdef __cplusplus
 }

@@ -370,7 +370,9 @@ static int specular_refraction(V3 n, V3 v, double eta, V3 *t_out, double *cos2) 
     double sq_eta = eta * eta;
     double sq_cos = cos1 * cos1;
     double g0 = sq_eta + sq_cos - 1.0;
-    if (g0 < 0.0) { *cos2 = 0.0; return 0; }
+    /* eta = 0: the reference's g / eta is 0/0 or x/0 where rounding makes
+     * |cos1| reach 1 (NaN weights); no refraction, as the GPU paths */
+    if (g0 < 0.0 || eta == 0.0) { *cos2 = 0.0; return 0; }
     double g = sqrt(g0);
     *cos2 = g / eta;
     return vnormalize(smul(1.0 / eta, vadd(v, smul(cos1 - g, n))), t_out);
@@ -383,6 +385,7 @@ static V3 reflection_glossy(rng_t *rg, V3 n, V3 r, double pw) {
         vnormalize(vcross(v3(1.0, 0.00424, 0.00764), r), &u);
     V3 v = vcross(u, r);
     double c0 = vdot(n, r);
+    if (c0 < 0.0) c0 = 0.0;   /* rounding at grazing incidence; NaN below otherwise (as the GPU paths) */
     double xi0 = gen_range(rg, 0.0, 1.0);
     double xi1 = m_pow(xi0, pw * c0);
     double xi2 = 2.0 * PI_D * gen_range(rg, 0.0, 1.0);

@@ -59,6 +59,7 @@ SIGNATURES = {
     "ppm_batch_render": (C.c_int, [_P, _P, C.c_int32, _dp]),
     "ppm_batch_set_mode": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "ppm_batch_info": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "ppm_batch_trial_ms": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "ppm_scene_parse": (C.c_int, [C.c_char_p, C.c_void_p, C.POINTER(C.c_int32), C.c_void_p, C.POINTER(C.c_int32),
                                   C.c_void_p, C.POINTER(C.c_int32)]),
     "ppm_camera_parse": (C.c_int, [C.c_char_p, C.c_void_p, C.POINTER(C.c_int64)]),

@@ -29,7 +29,7 @@ def _ptr(a: np.ndarray, ctype):
 
 
 # RenderConfig.flags bits (include/ppm_api.h)
-RENDER_TUNE_CELLS = 1   # time cells per radius 1 and 2 before the render, keep the faster
+RENDER_TUNE_CELLS = 1   # time 1 to 4 cells per radius before the render, keep the fastest
 RENDER_CLASSIC = 2      # the classic ray tracer (trace_ray_classic) instead of photon mapping
 RENDER_TILE_GATHER = 4  # mixed render: the tile gather (32 hit points per warp) instead of the row walk
 
@@ -353,9 +353,15 @@ class Batch:
             raise PPMError(st, "bad batch mode")
 
     def info(self) -> dict:
+        """How the last render ran (staged or graphs, the tile) and, after
+        an AUTO render, the ms per pass its trial measured for each mode."""
         staged, tile = C.c_int32(), C.c_int32()
         self.lib.ppm_batch_info(self.h, C.byref(staged), C.byref(tile))
-        return dict(staged=bool(staged.value), tile=tile.value)
+        out = dict(staged=bool(staged.value), tile=tile.value)
+        s_ms, g_ms = C.c_double(), C.c_double()
+        if self.lib.ppm_batch_trial_ms(self.h, C.byref(s_ms), C.byref(g_ms)) == 0:
+            out["trial_ms"] = dict(staged=s_ms.value, graphs=g_ms.value)
+        return out
 
     def render(self, jobs):
         """jobs: [(scene, camera, RenderConfig)]; returns ([images], device ms of the passes)."""

@@ -113,7 +113,7 @@ void launch_query_sort_f(const float *pos, const float *nrm, const double *r2, l
     if (n <= 0) return;
     // radius classes: r below r_max / 4, below r_max / 2, the rest
     k_query_hist<<<grid, 256, 0, s>>>(pos, r2, n, st, r2max / 16.0, r2max / 4.0, count, keyrank);
-    launch_scan(count, st, block_sums, qstart, cell_cap, s, grid);
+    launch_scan(count, st, block_sums, qstart, cell_cap, s, grid, SCAN_QUERY_KEYS);
     k_query_place<<<grid, 256, 0, s>>>(pos, nrm, r2, n, qstart, keyrank, hits, r2_sorted);
 }
 void launch_intersect_f(const SceneView<float> &sc, const double *rays, long long n, double *t, int32_t *obj,

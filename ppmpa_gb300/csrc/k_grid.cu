@@ -70,7 +70,7 @@ __device__ __forceinline__ void grid_setup_state(PassState *st, double r2_overri
             else dim[a] = (long long)f + 1;
             tot *= dim[a];
         }
-        if (ok && 3 * tot <= st->cell_cap) break;
+        if (ok && tot <= st->cell_cap) break;
         c *= 1.25;
         inv = 1.0 / c;
         if (it == 399) { dim[0] = dim[1] = dim[2] = 1; c = 1e30; inv = 1e-30; }
@@ -93,7 +93,7 @@ __device__ __forceinline__ void grid_setup_state(PassState *st, double r2_overri
     double efx = ceil(r * invx + 3e-3);
     g.extx = efx >= 1.0 && efx <= 64.0 ? (int)efx : (efx > 64.0 ? 64 : 1);
     g.ncell = dim[0] * dim[1] * dim[2];
-    g.nkeys = 3 * g.ncell;
+    g.nkeys = g.ncell;
     g.r2f = (float)r2;
     g.r2_lo = __double2float_rd(r2 * (1.0 - 1e-6));
     g.r2_hi = __double2float_ru(r2 * (1.0 + 1e-6));
@@ -124,9 +124,11 @@ __device__ __forceinline__ uint4 load_counts(const uint32_t *count, long long i,
     return v;
 }
 
-// key count of a scan: the pass grid's (fixed < 0) or a fixed one
+// key count of a scan: a fixed one (fixed >= 0), the pass grid's map keys
+// (one per cell), or the query sort's (SCAN_QUERY_KEYS: three radius
+// classes per cell)
 __device__ __forceinline__ long long scan_keys(const PassState *st, long long fixed) {
-    return fixed >= 0 ? fixed : st->grid.nkeys;
+    return fixed >= 0 ? fixed : (fixed == SCAN_QUERY_KEYS ? 3 * st->grid.ncell : st->grid.nkeys);
 }
 
 // the sum of one tile's counts into block_sums[tile]

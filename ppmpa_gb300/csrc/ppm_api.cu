@@ -33,7 +33,7 @@ constexpr int N_STAGES = 6;
 const char *STAGE_NAMES[N_STAGES] = {"photon_trace", "map_build", "eye_trace", "gather", "accumulate", "query_sort"};
 constexpr int TIMING_SLOTS = 256;
 constexpr int HITS_PER_PIXEL = 8;
-constexpr long long CELL_CAP = 1LL << 24;
+constexpr long long CELL_CAP = 1LL << 24;   // map keys (one per cell), the most one scan takes
 constexpr int BVH_MIN_OBJECTS = 32;   // below this a loop over the objects is faster
 constexpr int MAX_CELL_FACTOR = 4;    // render grids: 1 to 4 cells per radius (the tuner tries each)
 
@@ -334,8 +334,11 @@ static double make_plan(const std::vector<ppm_light> &lights, long long nphoton,
     return pw;
 }
 
+// cell_cap: cells a grid may have (map keys are cells; the FP32 estimate
+// maps pass CELL_CAP / 3, so that their query sort's three radius classes
+// per cell fit one scan)
 static int upload_state(ppm_ctx *ctx, double r2, int pass, double alpha, int offset, double cell_factor,
-                        long long photon_cap, long long hit_cap, int cell_sx = 1) {
+                        long long photon_cap, long long hit_cap, int cell_sx = 1, long long cell_cap = CELL_CAP) {
     PassState h;
     std::memset(&h, 0, sizeof h);
     h.photon_cap = (unsigned long long)photon_cap;
@@ -346,7 +349,7 @@ static int upload_state(ppm_ctx *ctx, double r2, int pass, double alpha, int off
     h.offset = offset;
     h.cell_factor = cell_factor;
     h.cell_sx = cell_sx;
-    h.cell_cap = CELL_CAP;
+    h.cell_cap = cell_cap;
     CK(cudaMemcpyAsync(ctx->st, &h, sizeof h, cudaMemcpyHostToDevice, ctx->s));
     return PPM_OK;
 }
@@ -1124,7 +1127,7 @@ extern "C" int ppm_eye_pass(ppm_ctx *ctx, int32_t use_classic, uint64_t seed, in
 // grid can be rebuilt with another k without the host arrays.
 static int grid_map_f32(ppm_ctx *ctx, long long n, double r2max, double k) {
     PhotonBuf<float> pb{as<float4>(ctx->raw_f), as<float4>(ctx->sorted_f), as<int32_t>(ctx->sidx)};
-    TRY(upload_state(ctx, r2max, 0, 0.0, 1, k, n, 0));
+    TRY(upload_state(ctx, r2max, 0, 0.0, 1, k, n, 0, 1, CELL_CAP / 3));
     launch_pass_begin(ctx->st, ctx->s);
     int g = grid_blocks(ctx, 4);
     launch_bbox_f(pb, ctx->st, n, g, ctx->s);
@@ -1787,6 +1790,10 @@ struct ppm_batch {
     size_t jobs_cap = 0;
     int tile = 0;                              // photons per map work item (0: tune)
     int last_staged = 0, last_tile = 0;
+    // AUTO: the mode the first eligible render measured as faster (0: not
+    // measured yet, 1: staged, 2: graphs) and its trial times per pass
+    int auto_pick = 0;
+    double trial_ms[2] = {0.0, 0.0};
 };
 
 static int batch_err(ppm_batch *b, int code, const char *fmt, ...) {
@@ -1845,6 +1852,7 @@ extern "C" int ppm_batch_set_mode(ppm_batch *b, int32_t mode, int32_t tile) {
         return PPM_ERR_INVALID_ARG;
     b->mode = mode;
     b->tile = tile;
+    b->auto_pick = 0;
     return PPM_OK;
 }
 
@@ -1852,6 +1860,14 @@ extern "C" int ppm_batch_info(const ppm_batch *b, int32_t *staged, int32_t *tile
     if (!b) return PPM_ERR_INVALID_ARG;
     if (staged) *staged = b->last_staged;
     if (tile) *tile = b->last_tile;
+    return PPM_OK;
+}
+
+extern "C" int ppm_batch_trial_ms(const ppm_batch *b, double *staged_ms, double *graphs_ms) {
+    if (!b) return PPM_ERR_INVALID_ARG;
+    if (!b->auto_pick) return PPM_ERR_NOT_READY;
+    if (staged_ms) *staged_ms = b->trial_ms[0];
+    if (graphs_ms) *graphs_ms = b->trial_ms[1];
     return PPM_OK;
 }
 
@@ -1987,32 +2003,97 @@ static int batch_begin_jobs(ppm_batch *b, const ppm_job *jobs, int njobs, bool f
     return PPM_OK;
 }
 
-static int batch_render_staged(ppm_batch *b, const ppm_job *jobs, int njobs, double *device_ms) {
-    TRY(batch_begin_jobs(b, jobs, njobs, true));
+// Tile tuner: one staged pass of the whole batch with each work-item size
+// (one untimed, two timed; the jobs must be begun), then every job begun
+// again.  Returns the best tile and its time per pass.
+static int batch_tune_tile(ppm_batch *b, const ppm_job *jobs, int njobs, int *tile, double *ms_per_pass) {
     std::vector<int> all((size_t)njobs);
     for (int j = 0; j < njobs; j++) all[j] = j;
+    TRY(batch_upload_table(b, all));
+    float best = 1e30f;
+    *tile = BATCH_TILES[0];
+    for (int cand : BATCH_TILES) {
+        cudaGraphExec_t ex = nullptr;
+        TRY(batch_capture(b, njobs, cand, &ex));
+        float ms = 0.0f;
+        cudaError_t e = cudaGraphLaunch(ex, b->s);
+        if (e == cudaSuccess) e = cudaEventRecord(b->e0, b->s);
+        for (int r = 0; r < 2 && e == cudaSuccess; r++) e = cudaGraphLaunch(ex, b->s);
+        if (e == cudaSuccess) e = cudaEventRecord(b->e1, b->s);
+        if (e == cudaSuccess) e = cudaEventSynchronize(b->e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, b->e0, b->e1);
+        cudaGraphExecDestroy(ex);
+        if (e != cudaSuccess) return batch_err(b, PPM_ERR_CUDA, "batch tile tuner: %s", cudaGetErrorString(e));
+        if (ms < best) { best = ms; *tile = cand; }
+    }
+    *ms_per_pass = best / 2.0;
+    return batch_begin_jobs(b, jobs, njobs, false);
+}
+
+// One launch of a parent graph holding every job's own pass graph (the
+// jobs in `act`, begun with use_graph) -- one pass of those jobs.
+static int batch_parent_graph(ppm_batch *b, const std::vector<int> &act, cudaGraphExec_t *exec) {
+    cudaGraph_t parent = nullptr;
+    CK_B(cudaGraphCreate(&parent, 0));
+    int rc = PPM_OK;
+    for (int j : act) {
+        cudaGraphNode_t node;
+        cudaError_t e = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, b->ctxs[j]->graph);
+        if (e != cudaSuccess) { rc = batch_err(b, PPM_ERR_CUDA, "job %d graph: %s", j, cudaGetErrorString(e)); break; }
+    }
+    if (rc == PPM_OK) {
+        cudaError_t e = cudaGraphInstantiate(exec, parent, 0);
+        if (e != cudaSuccess) rc = batch_err(b, PPM_ERR_CUDA, "batch graph: %s", cudaGetErrorString(e));
+    }
+    cudaGraphDestroy(parent);
+    return rc;
+}
+
+// AUTO's measurement, on the first eligible render of a batch: the staged
+// tile tuner's best pass, then one pass of the jobs' graphs side by side
+// (one untimed, two timed, the jobs begun with the cells already tuned);
+// the faster mode is kept for this and later renders.
+static int batch_auto_trial(ppm_batch *b, const ppm_job *jobs, int njobs) {
+    TRY(batch_begin_jobs(b, jobs, njobs, true));
+    int tile = 0;
+    double staged_ms = 0.0;
+    TRY(batch_tune_tile(b, jobs, njobs, &tile, &staged_ms));
+    std::vector<int> all((size_t)njobs);
+    for (int j = 0; j < njobs; j++) {
+        all[j] = j;
+        ppm_ctx *c = b->ctxs[j];
+        ppm_render_cfg cfg = jobs[j].cfg;
+        cfg.use_graph = 1;
+        cfg.cell_factor = c->cell_factor;
+        cfg.flags &= ~PPM_RENDER_TUNE_CELLS;
+        int st = ppm_render_begin(c, &cfg);
+        if (st != PPM_OK) return batch_err(b, st, "job %d: %s", j, c->err.c_str());
+    }
+    for (int j = 0; j < njobs; j++) CK_B(cudaStreamSynchronize(b->ctxs[j]->s));
+    cudaGraphExec_t ex = nullptr;
+    TRY(batch_parent_graph(b, all, &ex));
+    float ms = 0.0f;
+    cudaError_t e = cudaGraphLaunch(ex, b->s);
+    if (e == cudaSuccess) e = cudaEventRecord(b->e0, b->s);
+    for (int r = 0; r < 2 && e == cudaSuccess; r++) e = cudaGraphLaunch(ex, b->s);
+    if (e == cudaSuccess) e = cudaEventRecord(b->e1, b->s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b->e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, b->e0, b->e1);
+    cudaGraphExecDestroy(ex);
+    if (e != cudaSuccess) return batch_err(b, PPM_ERR_CUDA, "batch mode trial: %s", cudaGetErrorString(e));
+    b->trial_ms[0] = staged_ms;
+    b->trial_ms[1] = ms / 2.0;
+    b->auto_pick = staged_ms <= ms / 2.0 ? 1 : 2;
+    b->tile = tile;
+    return PPM_OK;
+}
+
+static int batch_render_staged(ppm_batch *b, const ppm_job *jobs, int njobs, double *device_ms) {
+    TRY(batch_begin_jobs(b, jobs, njobs, true));
     int tile = b->tile;
     if (tile == 0) {
-        // tile tuner: one pass of the whole batch with each work-item size
-        // (one untimed, two timed), then every job begun again
-        TRY(batch_upload_table(b, all));
-        float best = 1e30f;
-        tile = BATCH_TILES[0];
-        for (int cand : BATCH_TILES) {
-            cudaGraphExec_t ex = nullptr;
-            TRY(batch_capture(b, njobs, cand, &ex));
-            float ms = 0.0f;
-            cudaError_t e = cudaGraphLaunch(ex, b->s);
-            if (e == cudaSuccess) e = cudaEventRecord(b->e0, b->s);
-            for (int r = 0; r < 2 && e == cudaSuccess; r++) e = cudaGraphLaunch(ex, b->s);
-            if (e == cudaSuccess) e = cudaEventRecord(b->e1, b->s);
-            if (e == cudaSuccess) e = cudaEventSynchronize(b->e1);
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, b->e0, b->e1);
-            cudaGraphExecDestroy(ex);
-            if (e != cudaSuccess) return batch_err(b, PPM_ERR_CUDA, "batch tile tuner: %s", cudaGetErrorString(e));
-            if (ms < best) { best = ms; tile = cand; }
-        }
-        TRY(batch_begin_jobs(b, jobs, njobs, false));
+        double ms = 0.0;
+        TRY(batch_tune_tile(b, jobs, njobs, &tile, &ms));
     }
     int max_passes = 0;
     for (int j = 0; j < njobs; j++) max_passes = std::max(max_passes, jobs[j].cfg.passes);
@@ -2079,6 +2160,10 @@ extern "C" int ppm_batch_render(ppm_batch *b, const ppm_job *jobs, int32_t njobs
     if (b->mode == PPM_BATCH_STAGED && !staged)
         return batch_err(b, PPM_ERR_INVALID_ARG, "staged batch passes take 1 to %d mixed-precision photon-mapping "
                          "jobs with the default gather", BATCH_MAX_JOBS);
+    if (staged && b->mode == PPM_BATCH_AUTO) {
+        if (!b->auto_pick) TRY(batch_auto_trial(b, jobs, njobs));
+        staged = b->auto_pick == 1;
+    }
     if (staged) return batch_render_staged(b, jobs, njobs, device_ms);
     b->last_staged = 0;
     b->last_tile = 0;
@@ -2100,29 +2185,20 @@ extern "C" int ppm_batch_render(ppm_batch *b, const ppm_job *jobs, int32_t njobs
     int p = 0;
     while (p < max_passes) {
         // jobs still running, and the pass at which the next one finishes
-        cudaGraph_t parent = nullptr;
-        CK_B(cudaGraphCreate(&parent, 0));
+        std::vector<int> act;
         int until = max_passes;
-        int rc = PPM_OK;
-        for (int j = 0; j < njobs && rc == PPM_OK; j++) {
-            const int pj = jobs[j].cfg.passes;
-            if (pj <= p) continue;
-            until = std::min(until, pj);
-            cudaGraphNode_t node;
-            cudaError_t e = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, b->ctxs[j]->graph);
-            if (e != cudaSuccess) rc = batch_err(b, PPM_ERR_CUDA, "job %d graph: %s", j, cudaGetErrorString(e));
-        }
+        for (int j = 0; j < njobs; j++)
+            if (jobs[j].cfg.passes > p) {
+                act.push_back(j);
+                until = std::min(until, jobs[j].cfg.passes);
+            }
         cudaGraphExec_t exec = nullptr;
-        if (rc == PPM_OK) {
-            cudaError_t e = cudaGraphInstantiate(&exec, parent, 0);
-            if (e != cudaSuccess) rc = batch_err(b, PPM_ERR_CUDA, "batch graph: %s", cudaGetErrorString(e));
-        }
+        int rc = batch_parent_graph(b, act, &exec);
         for (; rc == PPM_OK && p < until; p++) {
             cudaError_t e = cudaGraphLaunch(exec, b->s);
             if (e != cudaSuccess) rc = batch_err(b, PPM_ERR_CUDA, "batch pass %d: %s", p, cudaGetErrorString(e));
         }
         if (exec) cudaGraphExecDestroy(exec);
-        cudaGraphDestroy(parent);
         if (rc != PPM_OK) return rc;
     }
     CK_B(cudaEventRecord(b->e1, b->s));

@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(256) k_bt_hist(const JobDev *jobs, int njobs, 
         const long long b1 = b0 + tile < n ? b0 + tile : n;
         for (long long i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
             const float4 r = jd.raw[i];
-            const uint32_t c = 3u * cell_of(g, mk3(r.x, r.y, r.z)) + (__float_as_uint(r.w) >> 30);
+            const uint32_t c = cell_of(g, mk3(r.x, r.y, r.z));
             jd.keyrank[i] = make_uint2(c, atomicAdd(&jd.count[c], 1u));
         }
     }

@@ -37,7 +37,7 @@ struct GridParams {
     int32_t dim[3];
     int32_t ext, extx;        // cells a radius can span: y/z, x
     int64_t ncell;
-    int64_t nkeys;            // 3 * ncell
+    int64_t nkeys;            // map keys: one per cell
     float r2f, r2_lo, r2_hi;  // pass radius^2 in FP32 and its rounding band
     float cellf;              // cell size in FP32
 };
@@ -382,10 +382,8 @@ __global__ void __launch_bounds__(256) k_cell_hist(PhotonBuf<T> buf, PassState *
     const GridParams g = st->grid;
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
-        int wl;
-        const V3<T> pos = buf.raw_pos_wl(i, wl);
-        uint32_t c = 3u * cell_of(g, pos) + (uint32_t)wl;
-        uint32_t r = atomicAdd(&count[c], 1u);
+        const uint32_t c = cell_of(g, buf.raw_pos(i));
+        const uint32_t r = atomicAdd(&count[c], 1u);
         keyrank[i] = make_uint2(c, r);
     }
 }
@@ -739,8 +737,8 @@ __device__ __forceinline__ RowSet make_rows(const GridParams &g, const uint32_t 
         int yy = lo[1] + (row - zi * ny), zz = lo[2] + zi;
         if (RowCull<T>::range(g, q, r2, yy, zz, lo[0], hi[0], x0, x1)) {
             int base = (zz * g.dim[1] + yy) * g.dim[0];
-            rs.begin = start[3 * (base + x0)];
-            rs.len = start[3 * (base + x1 + 1)] - rs.begin;
+            rs.begin = start[base + x0];
+            rs.len = start[base + x1 + 1] - rs.begin;
         }
     }
     rs.nonempty = __ballot_sync(0xffffffffu, rs.len > 0);
@@ -840,27 +838,6 @@ __device__ __forceinline__ void for_each_candidate(const GridParams &g, const ui
                 uint32_t o = base + lane_id();
                 f(o < n ? b + o : 0u, o < n);
             }
-        }
-    }
-}
-
-// for_each_candidate over packed rows: f(slot, valid) once per window of 32
-// positions of the group's rows laid end to end (slots of invalid lanes are
-// in bounds); all lanes of the warp must enter
-template <typename T, typename F>
-__device__ __forceinline__ void for_each_candidate_packed(const GridParams &g, const uint32_t *start, V3<T> q, T r2,
-                                                          const int lo[3], const int hi[3], F &&f) {
-    const int nrows = (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
-    const unsigned le = lanemask_le();
-    for (int row0 = 0; row0 < nrows; row0 += 32) {
-        const RowSet rs = make_rows(g, start, q, r2, lo, hi, row0);
-        if (rs.nonempty == 0u) continue;
-        const PackedRows pr = pack_rows(rs.begin, rs.len, rs.nonempty);
-        int kbase = -1;
-        for (uint32_t win = 0; win < pr.total; win += 32) {
-            bool v;
-            const uint32_t slot = packed_slot(pr, win, le, kbase, v);
-            f(slot, v);
         }
     }
 }
@@ -1154,8 +1131,8 @@ __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, cons
                 const int x0 = ra ? (rb ? min(xa0, xb0) : xa0) : xb0;
                 const int x1 = ra ? (rb ? max(xa1, xb1) : xa1) : xb1;
                 const int base = (zz * g.dim[1] + yy) * g.dim[0];
-                rbeg = start[3 * (base + x0)];
-                rlen = start[3 * (base + x1 + 1)] - rbeg;
+                rbeg = start[base + x0];
+                rlen = start[base + x1 + 1] - rbeg;
             }
         }
         const unsigned nonempty = __ballot_sync(0xffffffffu, rlen > 0);
@@ -1503,8 +1480,8 @@ __device__ __forceinline__ uint32_t tile_walk(const GridParams &g, const TileBox
         if (box_row_range(g, mk3(box.lo[0], box.lo[1], box.lo[2]), mk3(box.hi[0], box.hi[1], box.hi[2]), r2f, yy, zz,
                           box.cx0, box.cx1, x0, x1)) {
             const int base = (zz * g.dim[1] + yy) * g.dim[0];
-            rbeg = start[3 * (base + x0)];
-            rlen = start[3 * (base + x1 + 1)] - rbeg;
+            rbeg = start[base + x0];
+            rlen = start[base + x1 + 1] - rbeg;
         }
     }
     uint32_t incl = rlen;
@@ -1895,7 +1872,7 @@ constexpr float EST_TILE_RATIO = 0.5f;                // tile mode: union box <=
 __device__ __forceinline__ uint32_t fix_bits(float w) { return __float_as_uint(__fmaf_rn(w, FIX_ONE, FIX_ONE)); }
 
 template <bool COUNT>
-__global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_estimate_tile(const HitPoint<float> *hits, const double *r2s,
+__global__ void __launch_bounds__(32 * GATHER_TILE_WARPS, 4) k_estimate_tile(const HitPoint<float> *hits, const double *r2s,
                                                                           long long nq, PassState *st,
                                                                           const float4 *smap, const uint32_t *start,
                                                                           double pw, GatherOutF out) {
@@ -2002,8 +1979,8 @@ __global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_estimate_tile(const 
                         if (box_row_range(g, mk3(box.lo[0], box.lo[1], box.lo[2]), mk3(box.hi[0], box.hi[1], box.hi[2]),
                                           box.r2, yy, zz, box.cx0, box.cx1, x0, x1)) {
                             const int base = (zz * g.dim[1] + yy) * g.dim[0];
-                            rbeg = start[3 * (base + x0)];
-                            rlen = start[3 * (base + x1 + 1)] - rbeg;
+                            rbeg = start[base + x0];
+                            rlen = start[base + x1 + 1] - rbeg;
                         }
                     }
                     const unsigned nonempty = __ballot_sync(0xffffffffu, rlen > 0);
@@ -2092,7 +2069,12 @@ __global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_estimate_tile(const 
                 int c[3], lo[3], hi[3];
                 query_cells(g, q, ext, extx, c, lo, hi);
                 unsigned long long u0 = 0, u1 = 0, u2 = 0;
-                for_each_candidate_packed(g, start, q, rl * rl, lo, hi, [&](uint32_t idx, bool valid2) {
+                // a lane adds at most one term (<= 2^23) per step: 32-bit lane
+                // sums, folded into the 64-bit ones every 256 steps, cannot wrap
+                uint32_t v0 = 0u, v1 = 0u, v2 = 0u, steps = 0u;
+                // row by row: these rows already fill most lanes, and a packed
+                // walk's lane placement costs more than it saves here
+                for_each_candidate(g, start, q, rl * rl, lo, hi, [&](uint32_t idx, bool valid2) {
                     const float4 p = __ldg(&smap[idx]);
                     const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
                     const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
@@ -2109,9 +2091,13 @@ __global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_estimate_tile(const 
                         const float cc = __fmaf_rn(nl.z, bz, __fmaf_rn(nl.y, by, nl.x * bx));
                         const uint32_t term = fix_bits(fmaxf(cc, 0.0f)) - FIX_BIAS;
                         const uint32_t w = m >> 30;
-                        u0 += w == 0u ? term : 0u;
-                        u1 += w == 1u ? term : 0u;
-                        u2 += w >= 2u ? term : 0u;
+                        v0 += w == 0u ? term : 0u;
+                        v1 += w == 1u ? term : 0u;
+                        v2 += w >= 2u ? term : 0u;
+                    }
+                    if ((++steps & 255u) == 0u) {
+                        u0 += v0; u1 += v1; u2 += v2;
+                        v0 = v1 = v2 = 0u;
                     }
                     if (COUNT) {
                         c_slots += 1;
@@ -2119,6 +2105,7 @@ __global__ void __launch_bounds__(32 * GATHER_TILE_WARPS) k_estimate_tile(const 
                         c_hits += in ? 1 : 0;
                     }
                 });
+                u0 += v0; u1 += v1; u2 += v2;
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
                     u0 += __shfl_xor_sync(0xffffffffu, u0, o);

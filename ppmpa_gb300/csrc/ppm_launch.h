@@ -99,8 +99,10 @@ constexpr int SCAN_TILE = 4096;
 void launch_pass_begin(PassState *st, cudaStream_t s);
 void launch_grid_setup(PassState *st, double r2_override, cudaStream_t s);
 // grid: blocks of the two tile kernels (each loops over the pass's tiles)
-// fixed_keys >= 0: scan that many keys instead of the pass grid's (at most
-// 4096 * SCAN_TILE keys: k_scan_top holds 4096 tile sums)
+// fixed_keys >= 0: scan that many keys instead of the pass grid's map keys;
+// SCAN_QUERY_KEYS: the query sort's three radius classes per cell.  At most
+// 4096 * SCAN_TILE keys: k_scan_top holds 4096 tile sums.
+constexpr long long SCAN_QUERY_KEYS = -2;
 void launch_scan(uint32_t *count, const PassState *st, uint32_t *block_sums, uint32_t *start, long long cell_cap,
                  cudaStream_t s, int grid, long long fixed_keys = -1);
 void launch_accum(const double *pass_img, double *sum, long long n, cudaStream_t s);

@@ -211,7 +211,10 @@ __device__ __forceinline__ bool specular_refraction(V3<T> n, V3<T> v, T eta, V3<
     T sq_eta = eta * eta;
     T sq_cos = cos1 * cos1;
     T g0 = sq_eta + sq_cos - T(1);
-    if (g0 < T(0)) { cos2 = T(0); return false; }
+    // eta = 0 (a surface without an IOR) leaves g0 <= 0 except where
+    // rounding makes |cos1| reach 1: there the reference divides g by 0
+    // (0/0 or x/0) and the weights become NaN; no refraction instead
+    if (g0 < T(0) || eta == T(0)) { cos2 = T(0); return false; }
     T g = dsqrt(g0);
     cos2 = g / eta;
     return normalize((T(1) / eta) * (v + (cos1 - g) * n), t_out);
@@ -224,7 +227,11 @@ __device__ __forceinline__ V3<T> reflection_glossy(Rng &rg, V3<T> n, V3<T> r, T 
     if (!normalize(cross(mk3(T(0.00424), T(1), T(0.00764)), r), u))
         normalize(cross(mk3(T(1), T(0.00424), T(0.00764)), r), u);
     V3<T> v = cross(u, r);
+    // r is a reflection about n, so n.r >= 0; at grazing incidence rounding
+    // can make it a hair negative, where xi0^(pw n.r) > 1 and the square
+    // root below is NaN (in the reference too): clamped to 0
     T c0 = dot(n, r);
+    if (c0 < T(0)) c0 = T(0);
     T xi0 = gen_range<T>(rg, T(0), T(1));
     T xi1 = Math<T>::pow_(xi0, pw * c0);
     T xi2 = T(2.0 * PI_D) * gen_range<T>(rg, T(0), T(1));

@@ -138,21 +138,22 @@ def batch_scene(rng, n_prims: int):
     return sc
 
 
-def batch_jobs(n_jobs: int = 64, seed: int = 7, passes: int = 8, precision: int = 1, flags: int = 1):
+def batch_jobs(n_jobs: int = 64, seed: int = 7, passes: int = 8, precision: int = 1, flags: int = 1,
+               prims=(10, 200_000), reso=(64, 512), photons=(50_000, 2_000_000)):
     """[(scene, camera, RenderConfig)]: primitive counts log-uniform over
-    10..200k, square images 64..512 pixels wide, photons per pass
-    log-uniform over 50k..2M, alpha uniform in [0.5, 0.9]."""
+    `prims`, square images `reso` pixels wide (log-uniform), photons per
+    pass log-uniform over `photons`, alpha uniform in [0.5, 0.9]."""
     from . import scene as S
     from .api import RenderConfig
     rng = np.random.default_rng([seed, 404])
     jobs = []
     for j in range(n_jobs):
-        n_prims = int(round(_log_uniform(rng, 10, 200_000)))
-        reso = int(round(_log_uniform(rng, 64, 512)))
-        nphoton = int(round(_log_uniform(rng, 50_000, 2_000_000)))
+        n_prims = int(round(_log_uniform(rng, *prims)))
+        w = int(round(_log_uniform(rng, *reso)))
+        nphoton = int(round(_log_uniform(rng, *photons)))
         alpha = float(rng.uniform(0.5, 0.9))
         sc = batch_scene(rng, n_prims)
         cfg = RenderConfig(nphoton=nphoton, passes=passes, radius0=0.05, alpha=alpha, precision=precision,
                            seed=seed * 1000 + j, flags=flags)
-        jobs.append((sc, S.box_camera(reso), cfg))
+        jobs.append((sc, S.box_camera(w), cfg))
     return jobs

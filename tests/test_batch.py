@@ -129,3 +129,19 @@ def test_pass_shards_reassemble_the_full_render(precision, tol):
         total = sum(run(*shard_passes(6, r, 2)) for r in range(2)) / 6.0
     assert np.allclose(total, full, rtol=tol, atol=tol * full.max())
     assert parts[1] is None
+
+
+def test_auto_mode_times_both_modes_and_keeps_the_faster():
+    """PPM_BATCH_AUTO times one pass of each mode on the first render and
+    keeps the faster one; either way every job gets its own image."""
+    jobs = _mixed_jobs()[:3]
+    with Batch(0, seed=1) as b:
+        imgs, _ = b.render(jobs)
+        info = b.info()
+        t = info["trial_ms"]
+        assert t["staged"] > 0 and t["graphs"] > 0
+        assert info["staged"] == (t["staged"] <= t["graphs"])
+        again, _ = b.render(jobs)
+        assert b.info()["staged"] == info["staged"]
+    for a, c in zip(imgs, again):
+        assert np.allclose(a, c, rtol=1e-5, atol=1e-5 * c.max())

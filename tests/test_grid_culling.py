@@ -19,7 +19,7 @@ def grid(lo, hi, r2, k=1.0, sx=4, cell_cap=1 << 24):
     inv = 1.0 / c
     while True:
         dim = [int(np.floor((hi[a] - lo[a]) * (inv * sx if a == 0 else inv))) + 1 for a in range(3)]
-        if all(d <= 8192 for d in dim) and 3 * dim[0] * dim[1] * dim[2] <= cell_cap:
+        if all(d <= 8192 for d in dim) and dim[0] * dim[1] * dim[2] <= cell_cap:
             break
         c *= 1.25
         inv = 1.0 / c
