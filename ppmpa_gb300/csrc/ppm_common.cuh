@@ -88,7 +88,11 @@ __host__ __device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1,
 }
 
 // Sequential draws of one event.  FP64: 52-bit uniforms (rand 0.6 float
-// construction: (u64 >> 12) * 2^-52); FP32: 24-bit uniforms.
+// construction: (u64 >> 12) * 2^-52); FP32: 24-bit uniforms.  The first
+// Philox block (the same for both precisions) is computed by init, where
+// the lanes of a warp are still together: an event's draws are taken in
+// branches that differ per lane (diffuse, specular, glass), and a lazily
+// computed first block would be computed once per branch a warp runs.
 struct Rng {
     uint32_t k0, k1, item, pass, tag;
     uint32_t buf[4];
@@ -96,10 +100,11 @@ struct Rng {
     __device__ __forceinline__ void init(uint64_t seed, uint32_t it, uint32_t ps, uint32_t tg) {
         k0 = (uint32_t)seed; k1 = (uint32_t)(seed >> 32);
         item = it; pass = ps; tag = tg; k = 0;
+        philox4x32_10(item, pass, tag, 0u, k0, k1, buf);
     }
     __device__ __forceinline__ uint64_t next64() {
         int w = k & 1;
-        if (w == 0) philox4x32_10(item, pass, tag, (uint32_t)(k >> 1), k0, k1, buf);
+        if (w == 0 && k > 0) philox4x32_10(item, pass, tag, (uint32_t)(k >> 1), k0, k1, buf);
         uint64_t v = w ? ((uint64_t)buf[2] | ((uint64_t)buf[3] << 32)) : ((uint64_t)buf[0] | ((uint64_t)buf[1] << 32));
         k++;
         return v;
@@ -109,7 +114,7 @@ struct Rng {
     // an Rng instance serves one precision only
     __device__ __forceinline__ float u32f() {
         int w = k & 3;
-        if (w == 0) philox4x32_10(item, pass, tag, (uint32_t)(k >> 2), k0, k1, buf);
+        if (w == 0 && k > 0) philox4x32_10(item, pass, tag, (uint32_t)(k >> 2), k0, k1, buf);
         uint32_t v = w == 0 ? buf[0] : (w == 1 ? buf[1] : (w == 2 ? buf[2] : buf[3]));
         k++;
         return (float)(v >> 8) * 0x1p-24f;

@@ -1106,9 +1106,14 @@ __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, cons
     }
     int c[3], lo[3], hi[3];
     query_cells(g, qa, g.ext, g.extx, c, lo, hi);
-    if (CellMath<float>::coord(g, qb.x, 0) != c[0] || CellMath<float>::coord(g, qb.y, 1) != c[1] ||
-        CellMath<float>::coord(g, qb.z, 2) != c[2])
+    // one set of rows: the same y/z cell; x cells at most a radius apart,
+    // the rows' x bounds widened to both queries' ranges
+    const int cbx = CellMath<float>::coord(g, qb.x, 0);
+    if (CellMath<float>::coord(g, qb.y, 1) != c[1] || CellMath<float>::coord(g, qb.z, 2) != c[2] ||
+        abs(cbx - c[0]) > g.extx)
         return false;
+    lo[0] = max(min(c[0], cbx) - g.extx, 0);
+    hi[0] = min(max(c[0], cbx) + g.extx, g.dim[0] - 1);
     const float r2f = g.r2f, r2_lo = g.r2_lo, r2_hi = g.r2_hi;
     const unsigned lane = lane_id();
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, b0 = 0.f, b1 = 0.f, b2 = 0.f;
@@ -1883,7 +1888,7 @@ __global__ void __launch_bounds__(32 * GATHER_TILE_WARPS, 4) k_estimate_tile(con
     const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
     float4 *const sp = s_pos[wid], *const sd = s_dir[wid];
     TileBox &box = s_box[wid];
-    const unsigned lt = (1u << lane) - 1u, le = lanemask_le();
+    const unsigned lt = (1u << lane) - 1u;
     const GridParams g = st->grid;
     constexpr float FAR = 1e30f;
     unsigned long long c_tests = 0, c_slots = 0, c_hits = 0;
@@ -1983,16 +1988,28 @@ __global__ void __launch_bounds__(32 * GATHER_TILE_WARPS, 4) k_estimate_tile(con
                             rlen = start[base + x1 + 1] - rbeg;
                         }
                     }
-                    const unsigned nonempty = __ballot_sync(0xffffffffu, rlen > 0);
-                    if (nonempty == 0u) continue;
-                    const PackedRows pr = pack_rows(rbeg, rlen, nonempty);
-                    int kbase = -1;
-                    for (uint32_t b0 = 0; b0 < pr.total; b0 += 32) {
-                        bool v;
-                        const uint32_t slot = packed_slot(pr, b0, le, kbase, v);
+                    uint32_t incl = rlen;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= (unsigned)o) incl += u;
+                    }
+                    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+                    const uint32_t excl = incl - rlen;
+                    // rows end to end; a lane's row by a 5-step search (the
+                    // sweep over the staged batch below dwarfs it)
+                    for (uint32_t b0 = 0; b0 < total; b0 += 32) {
+                        const uint32_t j = b0 + lane;
+                        int r = 0;
+#pragma unroll
+                        for (int step = 16; step > 0; step >>= 1)
+                            if (__shfl_sync(0xffffffffu, incl, r + step - 1) <= j) r += step;
+                        const uint32_t rb = __shfl_sync(0xffffffffu, rbeg, r), rx = __shfl_sync(0xffffffffu, excl, r);
+                        const bool v = j < total;
                         uint32_t wl = 3u;
                         float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pd = pa;
                         if (v) {
+                            const uint32_t slot = rb + (j - rx);
                             const float4 p = __ldg(&smap[slot]);
                             const uint32_t m = __float_as_uint(p.w);
                             float inv;
