@@ -2039,7 +2039,25 @@ static int batch_parent_graph(ppm_batch *b, const std::vector<int> &act, cudaGra
     for (int j : act) {
         cudaGraphNode_t node;
         cudaError_t e = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, b->ctxs[j]->graph);
-        if (e != cudaSuccess) { rc = batch_err(b, PPM_ERR_CUDA, "job %d graph: %s", j, cudaGetErrorString(e)); break; }
+        if (e != cudaSuccess) {
+            // name the node types of the job's graph, for the error
+            size_t n = 0;
+            int types[16] = {0};
+            if (cudaGraphGetNodes(b->ctxs[j]->graph, nullptr, &n) == cudaSuccess && n) {
+                std::vector<cudaGraphNode_t> nodes(n);
+                if (cudaGraphGetNodes(b->ctxs[j]->graph, nodes.data(), &n) == cudaSuccess)
+                    for (cudaGraphNode_t nd : nodes) {
+                        cudaGraphNodeType t;
+                        if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && (int)t >= 0 && (int)t < 16) types[(int)t]++;
+                    }
+            }
+            std::string census;
+            for (int t = 0; t < 16; t++)
+                if (types[t]) census += " type" + std::to_string(t) + "x" + std::to_string(types[t]);
+            rc = batch_err(b, PPM_ERR_CUDA, "job %d graph (%zu nodes:%s): %s", j, n, census.c_str(),
+                           cudaGetErrorString(e));
+            break;
+        }
     }
     if (rc == PPM_OK) {
         cudaError_t e = cudaGraphInstantiate(exec, parent, 0);

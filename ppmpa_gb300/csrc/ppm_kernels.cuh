@@ -1106,14 +1106,18 @@ __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, cons
     }
     int c[3], lo[3], hi[3];
     query_cells(g, qa, g.ext, g.extx, c, lo, hi);
-    // one set of rows: the same y/z cell; x cells at most a radius apart,
-    // the rows' x bounds widened to both queries' ranges
-    const int cbx = CellMath<float>::coord(g, qb.x, 0);
-    if (CellMath<float>::coord(g, qb.y, 1) != c[1] || CellMath<float>::coord(g, qb.z, 2) != c[2] ||
-        abs(cbx - c[0]) > g.extx)
-        return false;
-    lo[0] = max(min(c[0], cbx) - g.extx, 0);
-    hi[0] = min(max(c[0], cbx) + g.extx, g.dim[0] - 1);
+    // One set of rows over both queries' cell ranges: y and z cells at most
+    // one apart (one more row or column of rows), x cells at most a
+    // radius apart.  Each query still culls every row to its own chord.
+    const int cb[3] = {CellMath<float>::coord(g, qb.x, 0), CellMath<float>::coord(g, qb.y, 1),
+                       CellMath<float>::coord(g, qb.z, 2)};
+    if (abs(cb[0] - c[0]) > g.extx || abs(cb[1] - c[1]) > 1 || abs(cb[2] - c[2]) > 1) return false;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int e = a == 0 ? g.extx : g.ext;
+        lo[a] = max(min(c[a], cb[a]) - e, 0);
+        hi[a] = min(max(c[a], cb[a]) + e, g.dim[a] - 1);
+    }
     const float r2f = g.r2f, r2_lo = g.r2_lo, r2_hi = g.r2_hi;
     const unsigned lane = lane_id();
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, b0 = 0.f, b1 = 0.f, b2 = 0.f;
