@@ -27,14 +27,24 @@ void launch_scatter_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, co
 void launch_eye_level_f(const SceneView<float> &sc, const DCamera<float> &cam, uint64_t seed, PassState *st, int uc,
                         int level, EyeQueue<float> in, EyeQueue<float> out, unsigned long long qcap,
                         HitPoint<float> *hits, EyeOut<float> pix, int grid, cudaStream_t s, bool classic) {
+    // levels after 0 launch as programmatic dependents of the level before
+    cudaLaunchConfig_t c = {};
+    c.gridDim = dim3((unsigned)grid);
+    c.blockDim = dim3(128);
+    c.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    c.attrs = at;
+    c.numAttrs = level > 0 ? 1 : 0;
     if (sc.bvh && classic)
-        k_eye_level_bvh<float, true><<<grid, 128, 0, s>>>(with_bvh(sc), cam, seed, st, uc, level, in, out, qcap, hits, pix);
+        cudaLaunchKernelEx(&c, k_eye_level_bvh<float, true>, with_bvh(sc), cam, seed, st, uc, level, in, out, qcap, hits, pix);
     else if (sc.bvh)
-        k_eye_level_bvh<float, false><<<grid, 128, 0, s>>>(with_bvh(sc), cam, seed, st, uc, level, in, out, qcap, hits, pix);
+        cudaLaunchKernelEx(&c, k_eye_level_bvh<float, false>, with_bvh(sc), cam, seed, st, uc, level, in, out, qcap, hits, pix);
     else if (classic)
-        k_eye_level<float, true><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
+        cudaLaunchKernelEx(&c, k_eye_level<float, true>, sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
     else
-        k_eye_level<float, false><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
+        cudaLaunchKernelEx(&c, k_eye_level<float, false>, sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
 }
 void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
                      const uint32_t *start, int pfilter, GatherOutF out, int grid, cudaStream_t s) {

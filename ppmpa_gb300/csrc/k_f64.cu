@@ -27,14 +27,24 @@ void launch_scatter_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, c
 void launch_eye_level_d(const SceneView<double> &sc, const DCamera<double> &cam, uint64_t seed, PassState *st, int uc,
                         int level, EyeQueue<double> in, EyeQueue<double> out, unsigned long long qcap,
                         HitPoint<double> *hits, EyeOut<double> pix, int grid, cudaStream_t s, bool classic) {
+    // levels after 0 launch as programmatic dependents of the level before
+    cudaLaunchConfig_t c = {};
+    c.gridDim = dim3((unsigned)grid);
+    c.blockDim = dim3(128);
+    c.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    c.attrs = at;
+    c.numAttrs = level > 0 ? 1 : 0;
     if (sc.bvh && classic)
-        k_eye_level_bvh<double, true><<<grid, 128, 0, s>>>(with_bvh(sc), cam, seed, st, uc, level, in, out, qcap, hits, pix);
+        cudaLaunchKernelEx(&c, k_eye_level_bvh<double, true>, with_bvh(sc), cam, seed, st, uc, level, in, out, qcap, hits, pix);
     else if (sc.bvh)
-        k_eye_level_bvh<double, false><<<grid, 128, 0, s>>>(with_bvh(sc), cam, seed, st, uc, level, in, out, qcap, hits, pix);
+        cudaLaunchKernelEx(&c, k_eye_level_bvh<double, false>, with_bvh(sc), cam, seed, st, uc, level, in, out, qcap, hits, pix);
     else if (classic)
-        k_eye_level<double, true><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
+        cudaLaunchKernelEx(&c, k_eye_level<double, true>, sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
     else
-        k_eye_level<double, false><<<grid, 128, 0, s>>>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
+        cudaLaunchKernelEx(&c, k_eye_level<double, false>, sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
 }
 void launch_gather_d(const HitPoint<double> *hits, PassState *st, long long n_fixed, const double4 *spos,
                      const double4 *sdir, const uint32_t *start, double pw, int pfilter, int mode, GatherOutD out,

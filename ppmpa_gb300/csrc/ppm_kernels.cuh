@@ -121,6 +121,11 @@ constexpr long long HIT_KEYS = 1LL << (3 * HIT_MORTON_BITS);
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
+// programmatic dependent launch (sm_90+): wait for the prerequisite grid to
+// finish and flush, and let the dependent grid be scheduled
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dependents_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // warp-aggregated append: returns this lane's slot (called by the lanes that append)
 __device__ __forceinline__ unsigned long long agg_append(unsigned long long *ctr) {
     unsigned active = __activemask();
@@ -625,6 +630,10 @@ template <typename T, bool B, bool CLASSIC = false>
 __device__ __forceinline__ void eye_level(const SceneView<T, B> &sc, const DCamera<T> &cam, uint64_t seed,
                                           PassState *st, int uc, int level, EyeQueue<T> in, EyeQueue<T> out,
                                           unsigned long long qcap, HitPoint<T> *hits, EyeOut<T> pix) {
+    // Levels after 0 are programmatic dependents of the level before: their
+    // blocks may be scheduled before it ends and wait here until it has
+    // finished and its queue appends are visible (a no-op for a plain launch)
+    grid_dependency_wait();
     const uint32_t pass = (uint32_t)st->pass;
     const unsigned long long hit_cap = st->hit_cap;
     const long long ntx = eye_tiles_x(cam.xreso);
@@ -633,6 +642,10 @@ __device__ __forceinline__ void eye_level(const SceneView<T, B> &sc, const DCame
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x)
         eye_vertex<T, B, CLASSIC>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix, i, pass, hit_cap, ntx);
+    // this block's work is done: the next level may be scheduled once every
+    // block has said so, i.e. once every block of this level has been
+    // scheduled, so its waiting blocks can never hold slots this level needs
+    grid_dependents_launch();
 }
 
 // Two entry points over the same body: without a hierarchy the compiler's
