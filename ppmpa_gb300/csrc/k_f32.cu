@@ -14,15 +14,15 @@ void launch_trace_f(const SceneView<float> &sc, const EmitPlan &plan, uint64_t s
         k_trace<float, false><<<grid, 256, 0, s>>>(sc, plan, seed, st, uc, photons);
 }
 void launch_bbox_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s) {
-    k_bbox<float><<<grid, 256, 0, s>>>(buf, st, n_fixed);
+    launch_pdl(k_bbox<float>, dim3(grid), dim3(256), s, buf, st, n_fixed);
 }
 void launch_hist_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, uint32_t *count, uint2 *keyrank, int grid,
                    cudaStream_t s) {
-    k_cell_hist<float><<<grid, 256, 0, s>>>(buf, st, n_fixed, count, keyrank);
+    launch_pdl(k_cell_hist<float>, dim3(grid), dim3(256), s, buf, st, n_fixed, count, keyrank);
 }
 void launch_scatter_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, const uint32_t *start,
                       const uint2 *keyrank, int grid, cudaStream_t s) {
-    k_scatter<float><<<grid, 256, 0, s>>>(buf, st, n_fixed, start, keyrank);
+    launch_pdl(k_scatter<float>, dim3(grid), dim3(256), s, buf, st, n_fixed, start, keyrank);
 }
 void launch_eye_level_f(const SceneView<float> &sc, const DCamera<float> &cam, uint64_t seed, PassState *st, int uc,
                         int level, EyeQueue<float> in, EyeQueue<float> out, unsigned long long qcap,
@@ -49,11 +49,11 @@ void launch_eye_level_f(const SceneView<float> &sc, const DCamera<float> &cam, u
 void launch_gather_f(const HitPoint<float> *hits, PassState *st, long long n_fixed, const float4 *smap,
                      const uint32_t *start, int pfilter, GatherOutF out, int grid, cudaStream_t s) {
     if (out.dump)   // the parity export
-        k_gather_f<false, true><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pfilter, out);
+        launch_pdl(k_gather_f<false, true>, dim3(grid), dim3(256), s, hits, st, n_fixed, smap, start, pfilter, out);
     else if (out.count)
-        k_gather_f<true><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pfilter, out);
+        launch_pdl(k_gather_f<true>, dim3(grid), dim3(256), s, hits, st, n_fixed, smap, start, pfilter, out);
     else
-        k_gather_f<false><<<grid, 256, 0, s>>>(hits, st, n_fixed, smap, start, pfilter, out);
+        launch_pdl(k_gather_f<false>, dim3(grid), dim3(256), s, hits, st, n_fixed, smap, start, pfilter, out);
 }
 void launch_gather_tile_f(const HitPoint<float> *hits, PassState *st, const float4 *smap, const uint32_t *start,
                           int pfilter, TileItem *items, unsigned long long cap, GatherOutF out, int grid,

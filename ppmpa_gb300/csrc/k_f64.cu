@@ -14,15 +14,15 @@ void launch_trace_d(const SceneView<double> &sc, const EmitPlan &plan, uint64_t 
         k_trace<double, false><<<grid, 256, 0, s>>>(sc, plan, seed, st, uc, photons);
 }
 void launch_bbox_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s) {
-    k_bbox<double><<<grid, 256, 0, s>>>(buf, st, n_fixed);
+    launch_pdl(k_bbox<double>, dim3(grid), dim3(256), s, buf, st, n_fixed);
 }
 void launch_hist_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, uint32_t *count, uint2 *keyrank, int grid,
                    cudaStream_t s) {
-    k_cell_hist<double><<<grid, 256, 0, s>>>(buf, st, n_fixed, count, keyrank);
+    launch_pdl(k_cell_hist<double>, dim3(grid), dim3(256), s, buf, st, n_fixed, count, keyrank);
 }
 void launch_scatter_d(PhotonBuf<double> buf, PassState *st, long long n_fixed, const uint32_t *start,
                       const uint2 *keyrank, int grid, cudaStream_t s) {
-    k_scatter<double><<<grid, 256, 0, s>>>(buf, st, n_fixed, start, keyrank);
+    launch_pdl(k_scatter<double>, dim3(grid), dim3(256), s, buf, st, n_fixed, start, keyrank);
 }
 void launch_eye_level_d(const SceneView<double> &sc, const DCamera<double> &cam, uint64_t seed, PassState *st, int uc,
                         int level, EyeQueue<double> in, EyeQueue<double> out, unsigned long long qcap,

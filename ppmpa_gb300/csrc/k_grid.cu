@@ -102,8 +102,10 @@ __device__ __forceinline__ void grid_setup_state(PassState *st, double r2_overri
 }
 
 __global__ void k_grid_setup(PassState *st, double r2_override) {
+    grid_dependency_wait();
     if (threadIdx.x != 0) return;
     grid_setup_state(st, r2_override);
+    grid_dependents_launch();
 }
 
 // Exclusive scan of the per-key counts into start[] (the photon map's cell
@@ -228,25 +230,31 @@ __device__ __forceinline__ void scan_down_tile(uint32_t *count, long long n, lon
 
 __global__ void __launch_bounds__(256) k_scan_reduce(const uint32_t *count, const PassState *st, long long fixed,
                                                      uint32_t *block_sums) {
+    grid_dependency_wait();
     const long long n = scan_keys(st, fixed);
     const long long ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     __shared__ uint32_t ws[8];
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) scan_reduce_tile(count, n, tile, block_sums, ws);
+    grid_dependents_launch();
 }
 
 __global__ void __launch_bounds__(1024) k_scan_top(uint32_t *block_sums, const PassState *st, long long fixed) {
+    grid_dependency_wait();
     const long long n = scan_keys(st, fixed);
     __shared__ uint32_t sh[1024];
     scan_top_block(block_sums, (int)((n + SCAN_TILE - 1) / SCAN_TILE), sh);
+    grid_dependents_launch();
 }
 
 __global__ void __launch_bounds__(256) k_scan_down(uint32_t *count, const PassState *st, long long fixed,
                                                    const uint32_t *block_sums, uint32_t *start) {
+    grid_dependency_wait();
     const long long n = scan_keys(st, fixed);
     const long long ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     __shared__ uint32_t ws[8];
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
         scan_down_tile(count, n, tile, block_sums, start, ws);
+    grid_dependents_launch();
 }
 
 __global__ void k_accum(const double *pass_img, double *sum, long long n) {
@@ -329,15 +337,17 @@ void launch_bt_scan(const JobDev *jobs, int njobs, int grid, cudaStream_t s) {
 }
 
 void launch_pass_begin(PassState *st, cudaStream_t s) { k_pass_begin<<<1, 32, 0, s>>>(st); }
-void launch_grid_setup(PassState *st, double r2_override, cudaStream_t s) { k_grid_setup<<<1, 32, 0, s>>>(st, r2_override); }
+void launch_grid_setup(PassState *st, double r2_override, cudaStream_t s) {
+    launch_pdl(k_grid_setup, dim3(1), dim3(32), s, st, r2_override);
+}
 void launch_scan(uint32_t *count, const PassState *st, uint32_t *block_sums, uint32_t *start, long long cell_cap,
                  cudaStream_t s, int grid, long long fixed_keys) {
     const long long cap = fixed_keys >= 0 ? fixed_keys : cell_cap;
     const long long tiles = (cap + SCAN_TILE - 1) / SCAN_TILE;
     const int nb = (int)(tiles < grid ? tiles : grid);
-    k_scan_reduce<<<nb, 256, 0, s>>>(count, st, fixed_keys, block_sums);
-    k_scan_top<<<1, 1024, 0, s>>>(block_sums, st, fixed_keys);
-    k_scan_down<<<nb, 256, 0, s>>>(count, st, fixed_keys, block_sums, start);
+    launch_pdl(k_scan_reduce, dim3(nb), dim3(256), s, count, st, fixed_keys, block_sums);
+    launch_pdl(k_scan_top, dim3(1), dim3(1024), s, block_sums, st, fixed_keys);
+    launch_pdl(k_scan_down, dim3(nb), dim3(256), s, count, st, fixed_keys, block_sums, start);
 }
 int kernels_per_scan() { return 3; }
 void launch_accum(const double *pass_img, double *sum, long long n, cudaStream_t s) {
@@ -353,17 +363,17 @@ void launch_pass_end(PassState *st, cudaStream_t s) { k_pass_end<<<1, 32, 0, s>>
 // multiply-add and the running-sum add.)
 __global__ void k_accum_mixed(const float *direct, const float *gathered, const PassState *st, double pw,
                               double *pass_img, double *sum, long long n) {
+    grid_dependency_wait();
     const double kk = pw * st->inv_pi_r2;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         double v = (double)direct[i] + (double)gathered[i] * kk;
         pass_img[i] = v;
         sum[i] += v;
-    }
-}
+    }}
 void launch_accum_mixed(const float *direct, const float *gathered, const PassState *st, double pw, double *pass_img,
                         double *sum, long long n, cudaStream_t s) {
-    k_accum_mixed<<<(unsigned)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024), 256, 0, s>>>(direct, gathered, st, pw,
-                                                                                             pass_img, sum, n);
+    launch_pdl(k_accum_mixed, dim3((unsigned)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024)), dim3(256), s, direct,
+               gathered, st, pw, pass_img, sum, n);
 }
 
 }  // namespace ppm

@@ -313,10 +313,12 @@ __global__ void __launch_bounds__(256, TraceBlocks<T>::value) k_trace(SceneView<
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) rays += __shfl_xor_sync(0xffffffffu, rays, o);
     if (lane == 0 && rays) atomicAdd(&st->photon_rays, (unsigned long long)rays);
+    grid_dependents_launch();   // the map build may be scheduled once every block is here
 }
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_bbox(PhotonBuf<T> buf, PassState *st, long long n_fixed) {
+    grid_dependency_wait();
     unsigned long long n = n_photons(st, n_fixed);
     // reduced in the photons' own precision; converted once per block
     T lo[3] = {T(1e30), T(1e30), T(1e30)}, hi[3] = {T(-1e30), T(-1e30), T(-1e30)};
@@ -355,6 +357,7 @@ __global__ void __launch_bounds__(256) k_bbox(PhotonBuf<T> buf, PassState *st, l
             atomicMax(&st->bb_hi[a], ord_enc((double)h));
         }
     }
+    grid_dependents_launch();
 }
 
 // cell coordinate, clamped to the grid
@@ -383,6 +386,7 @@ __device__ __forceinline__ uint32_t cell_of(const GridParams &g, V3<T> p) {
 template <typename T>
 __global__ void __launch_bounds__(256) k_cell_hist(PhotonBuf<T> buf, PassState *st, long long n_fixed,
                                                    uint32_t *count, uint2 *keyrank) {
+    grid_dependency_wait();
     unsigned long long n = n_photons(st, n_fixed);
     const GridParams g = st->grid;
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -391,6 +395,7 @@ __global__ void __launch_bounds__(256) k_cell_hist(PhotonBuf<T> buf, PassState *
         const uint32_t r = atomicAdd(&count[c], 1u);
         keyrank[i] = make_uint2(c, r);
     }
+    grid_dependents_launch();
 }
 
 template <typename T> __global__ void k_scatter(PhotonBuf<T> buf, PassState *st, long long n_fixed,
@@ -400,6 +405,7 @@ template <typename T> __global__ void k_scatter(PhotonBuf<T> buf, PassState *st,
 template <>
 __global__ void __launch_bounds__(256) k_scatter<double>(PhotonBuf<double> buf, PassState *st, long long n_fixed,
                                                          const uint32_t *start, const uint2 *keyrank) {
+    grid_dependency_wait();
     unsigned long long n = n_photons(st, n_fixed);
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
@@ -410,6 +416,7 @@ __global__ void __launch_bounds__(256) k_scatter<double>(PhotonBuf<double> buf, 
         buf.spos[dst] = make_double4(r.pos[0], r.pos[1], r.pos[2], __longlong_as_double((long long)meta));
         buf.sdir[dst] = make_double4(r.dir[0], r.dir[1], r.dir[2], 0.0);
     }
+    grid_dependents_launch();
 }
 
 #endif
@@ -418,6 +425,7 @@ __global__ void __launch_bounds__(256) k_scatter<double>(PhotonBuf<double> buf, 
 template <>
 __global__ void __launch_bounds__(256) k_scatter<float>(PhotonBuf<float> buf, PassState *st, long long n_fixed,
                                                         const uint32_t *start, const uint2 *keyrank) {
+    grid_dependency_wait();
     unsigned long long n = n_photons(st, n_fixed);
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
@@ -426,6 +434,7 @@ __global__ void __launch_bounds__(256) k_scatter<float>(PhotonBuf<float> buf, Pa
         buf.sorted[dst] = buf.raw[i];
         if (buf.sidx) buf.sidx[dst] = (int32_t)i;
     }
+    grid_dependents_launch();
 }
 
 #endif
@@ -1376,6 +1385,7 @@ __global__ void __launch_bounds__(256, 5) k_gather_f(const HitPoint<float> *hits
                                                      const float4 *smap, const uint32_t *start, int pfilter,
                                                      GatherOutF out) {
     constexpr unsigned CHUNK = 2u;
+    grid_dependency_wait();   // a programmatic dependent of the map's scatter
     const unsigned long long nq = n_hitpoints(st, n_fixed);
     const GridParams g = st->grid;
     const unsigned lane = lane_id();
@@ -1391,6 +1401,7 @@ __global__ void __launch_bounds__(256, 5) k_gather_f(const HitPoint<float> *hits
         }
         qi += gather_step<COUNT, DUMP>(g, st->r2, hits, qi, qend - qi, start, smap, pfilter, out);
     }
+    grid_dependents_launch();
 }
 
 // ---------------------------------------------------------------------------

@@ -94,6 +94,25 @@ int bvh_scratch_words(int m, int n_objs);
 int launch_bvh_build(const DObject<double> *objs, const int32_t *bounded, int m, int n_objs, int leaf_max,
                      BvhNode *nodes, int32_t *order, uint32_t *scratch, cudaStream_t s);
 
+// A launch that may begin before the previous kernel in the stream ends
+// (programmatic dependent launch): the kernel waits (griddepcontrol.wait)
+// before it reads what that kernel wrote, and the previous kernel's blocks
+// signal when their work is done, so a chain of dependent launches loses
+// no launch latency between its kernels.
+template <typename... K, typename... A>
+inline void launch_pdl(void (*kernel)(K...), dim3 grid, dim3 block, cudaStream_t s, A &&...args) {
+    cudaLaunchConfig_t c = {};
+    c.gridDim = grid;
+    c.blockDim = block;
+    c.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    c.attrs = at;
+    c.numAttrs = 1;
+    cudaLaunchKernelEx(&c, kernel, std::forward<A>(args)...);
+}
+
 // ---- grid / scan / pass bookkeeping ------------------------------------------------
 constexpr int SCAN_TILE = 4096;
 void launch_pass_begin(PassState *st, cudaStream_t s);
