@@ -23,17 +23,15 @@ __device__ __forceinline__ void pass_begin_state(PassState *st) {
     for (int l = 0; l < MAX_TRACE + 2; l++) st->eq[l] = 0;
     st->inv_pi_r2 = ONE_PI_D / st->r2;
     for (int a = 0; a < 3; a++) {
-        st->bb_lo[a] = ord_enc(1e300);
-        st->bb_hi[a] = ord_enc(-1e300);
+        // a scene of bounded objects gives the grid its box; otherwise the
+        // pass's photons do (k_bbox)
+        st->bb_lo[a] = ord_enc(st->scene_box ? st->scene_lo[a] : 1e300);
+        st->bb_hi[a] = ord_enc(st->scene_box ? st->scene_hi[a] : -1e300);
         st->hb_lo[a] = ordf_enc(0x7f7fffffu);   // +FLT_MAX
         st->hb_hi[a] = ordf_enc(0xff7fffffu);   // -FLT_MAX
     }
 }
 
-__global__ void k_pass_begin(PassState *st) {
-    if (threadIdx.x != 0) return;
-    pass_begin_state(st);
-}
 
 // Grid over the photon bounds with cells of c = r/k * (1 + 1/128) in y and z
 // (k = cells per radius) and c / sx in x.  The margin keeps |p - q| <= r  =>
@@ -99,6 +97,16 @@ __device__ __forceinline__ void grid_setup_state(PassState *st, double r2_overri
     g.r2_hi = __double2float_ru(r2 * (1.0 + 1e-6));
     g.cellf = (float)c;
     st->grid = g;
+}
+
+// Pass set-up.  With a scene box the bounds the grid spans are the box
+// (the photons and hit points lie on the scene's objects), and the pass
+// launches no k_bbox; k_grid_setup still follows the photon trace, off the
+// eye branch's path.  Photons a rounding step outside the box go to the
+// edge cells, which only shrinks their cell distance to any query.
+__global__ void k_pass_begin(PassState *st) {
+    if (threadIdx.x != 0) return;
+    pass_begin_state(st);
 }
 
 __global__ void k_grid_setup(PassState *st, double r2_override) {

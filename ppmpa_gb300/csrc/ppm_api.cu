@@ -49,6 +49,10 @@ struct ppm_ctx {
     cudaStream_t s = nullptr, s2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::string err;
+    // every object bounded: the box the render's grids span (set at upload);
+    // render_scene_box: the begun render uses it
+    bool scene_box = false, render_scene_box = false;
+    double scene_lo[3] = {0, 0, 0}, scene_hi[3] = {0, 0, 0};
     uint64_t seed = 0;
 
     // scene
@@ -334,11 +338,58 @@ static double make_plan(const std::vector<ppm_light> &lights, long long nphoton,
     return pw;
 }
 
+// The box of the scene's objects, when every object that can be hit is
+// bounded (spheres, triangles, parallelograms; a point object is never hit):
+// the render's photons and hit points lie on them, so its grids span this
+// box without a bounds pass.  An infinite plane leaves scene_box false.
+static void scene_bounds(ppm_ctx *ctx) {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    bool ok = false;
+    auto add = [&](const double *p, double dx, double dy, double dz) {
+        const double v[3] = {p[0] + dx, p[1] + dy, p[2] + dz};
+        for (int a = 0; a < 3; a++) {
+            lo[a] = std::min(lo[a], v[a]);
+            hi[a] = std::max(hi[a], v[a]);
+        }
+    };
+    for (const ppm_object &o : ctx->objs) {
+        const double *p = o.position, *d1 = o.dir1, *d2 = o.dir2;
+        switch (o.shape) {
+        case SH_SPHERE:
+            add(p, -o.radius, -o.radius, -o.radius);
+            add(p, o.radius, o.radius, o.radius);
+            ok = true;
+            break;
+        case SH_POLYGON:
+        case SH_PARALLELOGRAM:
+            add(p, 0.0, 0.0, 0.0);
+            add(p, d1[0], d1[1], d1[2]);
+            add(p, d2[0], d2[1], d2[2]);
+            if (o.shape == SH_PARALLELOGRAM) add(p, d1[0] + d2[0], d1[1] + d2[1], d1[2] + d2[2]);
+            ok = true;
+            break;
+        case SH_PLAIN:
+            ctx->scene_box = false;
+            return;
+        default:
+            break;
+        }
+    }
+    bool finite = ok;
+    for (int a = 0; a < 3; a++) finite = finite && lo[a] <= hi[a] && hi[a] - lo[a] < 1e30;
+    ctx->scene_box = finite;
+    for (int a = 0; a < 3; a++) {
+        ctx->scene_lo[a] = finite ? lo[a] : 0.0;
+        ctx->scene_hi[a] = finite ? hi[a] : 0.0;
+    }
+}
+
 // cell_cap: cells a grid may have (map keys are cells; the FP32 estimate
 // maps pass CELL_CAP / 3, so that their query sort's three radius classes
 // per cell fit one scan)
 static int upload_state(ppm_ctx *ctx, double r2, int pass, double alpha, int offset, double cell_factor,
-                        long long photon_cap, long long hit_cap, int cell_sx = 1, long long cell_cap = CELL_CAP) {
+                        long long photon_cap, long long hit_cap, int cell_sx = 1, long long cell_cap = CELL_CAP,
+                        bool use_scene_box = false) {
     PassState h;
     std::memset(&h, 0, sizeof h);
     h.photon_cap = (unsigned long long)photon_cap;
@@ -350,6 +401,11 @@ static int upload_state(ppm_ctx *ctx, double r2, int pass, double alpha, int off
     h.cell_factor = cell_factor;
     h.cell_sx = cell_sx;
     h.cell_cap = cell_cap;
+    h.scene_box = use_scene_box && ctx->scene_box ? 1 : 0;
+    for (int a = 0; a < 3; a++) {
+        h.scene_lo[a] = ctx->scene_lo[a];
+        h.scene_hi[a] = ctx->scene_hi[a];
+    }
     CK(cudaMemcpyAsync(ctx->st, &h, sizeof h, cudaMemcpyHostToDevice, ctx->s));
     return PPM_OK;
 }
@@ -631,6 +687,7 @@ extern "C" int ppm_scene_upload(ppm_ctx *ctx, const ppm_object *objs, int32_t n_
     ctx->objs.assign(objs, objs + n_objs);
     ctx->mats.assign(mats, mats + n_mats);
     ctx->lights.assign(lights, lights + n_lights);
+    scene_bounds(ctx);
     std::vector<DObject<double>> od;
     std::vector<DObject<float>> of;
     std::vector<DMaterial<double>> md;
@@ -1447,11 +1504,12 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
     }
     if (ev) CK(cudaEventRecord(ev[6], s2));
     CK(cudaEventRecord(ctx->ev_join, s2));
-    // photons
+    // photons; the pass's grid over the scene's box or the photons' bounds
+    const bool box = ctx->render_scene_box;
     if (mixed) {
         PhotonBuf<float> pb{as<float4>(ctx->raw_f), as<float4>(ctx->sorted_f), nullptr};
         kernels += enqueue_photon_trace<float>(ctx, ctx->plan, ctx->cfg.seed, uc, pb, s);
-        launch_bbox_f(pb, ctx->st, -1, g4, s);
+        if (!box) launch_bbox_f(pb, ctx->st, -1, g4, s);
         if (ev) CK(cudaEventRecord(ev[1], s));
         launch_grid_setup(ctx->st, -1.0, s);
         launch_hist_f(pb, ctx->st, -1, as<uint32_t>(ctx->count), as<uint2>(ctx->keyrank), g8, s);
@@ -1461,7 +1519,7 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
     } else {
         PhotonBuf<double> pb{as<PhotonD>(ctx->raw_d), as<double4>(ctx->spos), as<double4>(ctx->sdir)};
         kernels += enqueue_photon_trace<double>(ctx, ctx->plan, ctx->cfg.seed, uc, pb, s);
-        launch_bbox_d(pb, ctx->st, -1, g4, s);
+        if (!box) launch_bbox_d(pb, ctx->st, -1, g4, s);
         if (ev) CK(cudaEventRecord(ev[1], s));
         launch_grid_setup(ctx->st, -1.0, s);
         launch_hist_d(pb, ctx->st, -1, as<uint32_t>(ctx->count), as<uint2>(ctx->keyrank), g8, s);
@@ -1469,7 +1527,7 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
                     grid_blocks(ctx, 8));
         launch_scatter_d(pb, ctx->st, -1, as<uint32_t>(ctx->start), as<uint2>(ctx->keyrank), g8, s);
     }
-    kernels += 4 + kernels_per_scan();
+    kernels += (box ? 3 : 4) + kernels_per_scan();
     if (ev) CK(cudaEventRecord(ev[2], s));
     CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
     if (ev) CK(cudaEventRecord(ev[7], s));
@@ -1535,7 +1593,7 @@ static int tune_cells(ppm_ctx *ctx, const ppm_render_cfg &cfg, long long cap, in
         float total = 0.0f;
         for (int rep = 0; rep < 3 && rc == PPM_OK; rep++) {   // one warm-up, two timed passes
             rc = upload_state(ctx, schedule_r2(cfg, trial), trial, cfg.alpha, cfg.schedule_offset, (double)k, cap,
-                              ctx->hit_cap, ctx->render_sx);
+                              ctx->hit_cap, ctx->render_sx, CELL_CAP, ctx->render_scene_box);
             if (rc == PPM_OK && cudaEventRecord(e0, ctx->s) != cudaSuccess) rc = set_err(ctx, PPM_ERR_CUDA, "event");
             if (rc == PPM_OK) {
                 if (ctx->graph_exec) {   // time the pass the render will replay
@@ -1571,6 +1629,7 @@ extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
         return set_err(ctx, PPM_ERR_INVALID_ARG, "bad render configuration");
     cudaSetDevice(ctx->device);
     drop_graph(ctx);
+    ctx->render_scene_box = ctx->scene_box;
     ctx->cfg = *cfg;
     ctx->pw = make_plan(ctx->lights, cfg->nphoton, ctx->plan);
     long long nem = ctx->plan.first[ctx->plan.n_lights];
@@ -1599,7 +1658,7 @@ extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
     CK(cudaMemsetAsync(ctx->pass_img.p, 0, sizeof(double) * 3 * ctx->npx, ctx->s));
     int cf = cfg->cell_factor ? cfg->cell_factor : 1;
     TRY(upload_state(ctx, schedule_r2(*cfg, cfg->first_pass), cfg->first_pass, cfg->alpha, cfg->schedule_offset, (double)cf,
-                     cap, ctx->hit_cap, ctx->render_sx));
+                     cap, ctx->hit_cap, ctx->render_sx, CELL_CAP, ctx->render_scene_box));
     CK(cudaStreamSynchronize(ctx->s));
     ctx->cell_factor = cf;
     ctx->passes_done = 0;
@@ -1619,7 +1678,7 @@ extern "C" int ppm_render_begin(ppm_ctx *ctx, const ppm_render_cfg *cfg) {
     if ((cfg->flags & PPM_RENDER_TUNE_CELLS) && !(cfg->flags & PPM_RENDER_CLASSIC)) {
         TRY(tune_cells(ctx, *cfg, cap, cf));
         TRY(upload_state(ctx, schedule_r2(*cfg, cfg->first_pass), cfg->first_pass, cfg->alpha, cfg->schedule_offset,
-                         (double)cf, cap, ctx->hit_cap, ctx->render_sx));
+                         (double)cf, cap, ctx->hit_cap, ctx->render_sx, CELL_CAP, ctx->render_scene_box));
         CK(cudaStreamSynchronize(ctx->s));
         ctx->cell_factor = cf;
     }

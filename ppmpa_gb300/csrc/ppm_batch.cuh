@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(256, 3) k_bt_trace(const JobDev *jobs, int njo
                     while (l < jd.plan.n_lights - 1 && li >= jd.plan.first[l + 1]) l++;
                     pass = (uint32_t)jd.st->pass;
                     Rng rg;
-                    rg.init(jd.seed, (uint32_t)li, pass, TAG_EMIT);
+                    rg.init<float>(jd.seed, (uint32_t)li, pass, TAG_EMIT);
                     generate_photon(jd.sv.lights[l], rg, ph);
                     ph.item = (uint32_t)li;
                     active = true;

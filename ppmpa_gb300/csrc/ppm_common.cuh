@@ -66,12 +66,17 @@ __device__ __forceinline__ bool normalize(V3<T> a, V3<T> &out) {
 }
 
 // ---------------------------------------------------------------------------
-// Philox4x32-10 (Salmon et al., SC'11).  key = seed, ctr = {item, pass, tag, block}.
+// Philox4x32-R (Salmon et al., SC'11).  key = seed, ctr = {item, pass, tag, block}.
+// R = 10 for the FP64 path (the oracle's generator, bit for bit); R = 7 for
+// the FP32 path, which is compared statistically: Salmon et al. report that
+// Philox4x32 passes TestU01's BigCrush from 7 rounds on (10 is their margin),
+// and 7 rounds take 4 % off the FP32 photon trace.
 // ---------------------------------------------------------------------------
-__host__ __device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
-                                                      uint32_t k0, uint32_t k1, uint32_t out[4]) {
+template <int R>
+__host__ __device__ __forceinline__ void philox4x32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                                   uint32_t k1, uint32_t out[4]) {
 #pragma unroll
-    for (int i = 0; i < 10; i++) {
+    for (int i = 0; i < R; i++) {
 #ifdef __CUDA_ARCH__
         uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
         uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
@@ -87,34 +92,38 @@ __host__ __device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1,
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
+template <typename T> struct PhiloxRounds { static constexpr int value = 10; };
+template <> struct PhiloxRounds<float> { static constexpr int value = 7; };
+
 // Sequential draws of one event.  FP64: 52-bit uniforms (rand 0.6 float
-// construction: (u64 >> 12) * 2^-52); FP32: 24-bit uniforms.  The first
-// Philox block (the same for both precisions) is computed by init, where
-// the lanes of a warp are still together: an event's draws are taken in
-// branches that differ per lane (diffuse, specular, glass), and a lazily
-// computed first block would be computed once per branch a warp runs.
+// construction: (u64 >> 12) * 2^-52) from Philox4x32-10; FP32: 24-bit
+// uniforms from Philox4x32-7.  An Rng instance serves one precision, named
+// at init.  The first Philox block is computed by init, where the lanes of
+// a warp are still together: an event's draws are taken in branches that
+// differ per lane (diffuse, specular, glass), and a lazily computed first
+// block would be computed once per branch a warp runs.
 struct Rng {
     uint32_t k0, k1, item, pass, tag;
     uint32_t buf[4];
     int k;
+    template <typename T>
     __device__ __forceinline__ void init(uint64_t seed, uint32_t it, uint32_t ps, uint32_t tg) {
         k0 = (uint32_t)seed; k1 = (uint32_t)(seed >> 32);
         item = it; pass = ps; tag = tg; k = 0;
-        philox4x32_10(item, pass, tag, 0u, k0, k1, buf);
+        philox4x32<PhiloxRounds<T>::value>(item, pass, tag, 0u, k0, k1, buf);
     }
     __device__ __forceinline__ uint64_t next64() {
         int w = k & 1;
-        if (w == 0 && k > 0) philox4x32_10(item, pass, tag, (uint32_t)(k >> 1), k0, k1, buf);
+        if (w == 0 && k > 0) philox4x32<10>(item, pass, tag, (uint32_t)(k >> 1), k0, k1, buf);
         uint64_t v = w ? ((uint64_t)buf[2] | ((uint64_t)buf[3] << 32)) : ((uint64_t)buf[0] | ((uint64_t)buf[1] << 32));
         k++;
         return v;
     }
     __device__ __forceinline__ double u64d() { return (double)(next64() >> 12) * 0x1p-52; }
-    // FP32 draws use every 32-bit word of a block (4 draws per Philox call);
-    // an Rng instance serves one precision only
+    // FP32 draws use every 32-bit word of a block (4 draws per Philox call)
     __device__ __forceinline__ float u32f() {
         int w = k & 3;
-        if (w == 0 && k > 0) philox4x32_10(item, pass, tag, (uint32_t)(k >> 2), k0, k1, buf);
+        if (w == 0 && k > 0) philox4x32<7>(item, pass, tag, (uint32_t)(k >> 2), k0, k1, buf);
         uint32_t v = w == 0 ? buf[0] : (w == 1 ? buf[1] : (w == 2 ? buf[2] : buf[3]));
         k++;
         return (float)(v >> 8) * 0x1p-24f;

@@ -69,6 +69,9 @@ struct PassState {
     uint32_t hb_lo[3], hb_hi[3];            // hit point bounds (orderable FP32 encodings)
     unsigned long long tile_items;          // tile gather: items queued this pass
     unsigned long long tile_next;           // and the next one to take
+    int32_t scene_box;                      // 1: every object is bounded; the grid spans their box
+    int32_t pad3;
+    double scene_lo[3], scene_hi[3];        // the scene's box (photons and hit points lie on its objects)
 };
 
 // number of valid photons / hit points (the counters keep counting past the
@@ -287,7 +290,7 @@ __global__ void __launch_bounds__(256, TraceBlocks<T>::value) k_trace(SceneView<
                     int li = 0;
                     while (li < plan.n_lights - 1 && (int64_t)i >= plan.first[li + 1]) li++;
                     Rng rg;
-                    rg.init(seed, (uint32_t)i, pass, TAG_EMIT);
+                    rg.init<T>(seed, (uint32_t)i, pass, TAG_EMIT);
                     generate_photon(sc.lights[li], rg, ph);
                     ph.item = (uint32_t)i;
                     active = true;
@@ -518,7 +521,7 @@ __device__ __forceinline__ void eye_vertex(const SceneView<T, B> &sc, const DCam
             p = py * (uint32_t)cam.xreso + px;
             const T y = (T)py, x = (T)px;
             Rng rg;
-            rg.init(seed, p, pass, TAG_CAMERA);
+            rg.init<T>(seed, p, pass, TAG_CAMERA);
             V3<T> blur = mk3(T(0), T(0), T(0));
             if (cam.blur) {
                 T r1 = gen_range<T>(rg, T(-0.5), T(0.5));
@@ -572,7 +575,7 @@ __device__ __forceinline__ void eye_vertex(const SceneView<T, B> &sc, const DCam
                     cf = bsdf_coef(mate, cos1);
                 } else {
                     Rng rv;
-                    rv.init(seed, p, pass, TAG_EYE | node);
+                    rv.init<T>(seed, p, pass, TAG_EYE | node);
                     rdir = reflection_glossy(rv, is.n, rdir0, sf_power_glossy(mate));
                     V3<T> hvec = is.n;
                     if (!normalize(rdir - rd, hvec)) hvec = is.n;

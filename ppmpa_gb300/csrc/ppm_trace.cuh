@@ -403,7 +403,7 @@ __device__ __forceinline__ bool photon_event(const SceneView<T, B> &sc, uint64_t
     const DMaterial<T> &mate = sc.mats[mid];
     const T air[3] = {T(1), T(1), T(1)};
     Rng rg;
-    rg.init(seed, ph.item, pass, TAG_BOUNCE | (uint32_t)ph.level);
+    rg.init<T>(seed, ph.item, pass, TAG_BOUNCE | (uint32_t)ph.level);
     bool cont = false;
     int nmed = ph.medium;
     V3<T> nd = ph.dir;
