@@ -769,8 +769,14 @@ def measure_batch(args, name, bw):
     def rate(ms):
         return None if ms is None else {"value": photons / (ms / 1e3) / 1e6, "unit": "Mphotons/s", "ms": ms}
     # kernels of this library launched in the timed render: 22 per staged pass
-    # of the batch, or 22 per pass of every job inside the parent graphs
-    launches = 22 * bw["passes"] if picked == "staged" else 22 * sum(cfg.passes for _, _, cfg in jobs)
+    # of the batch, or each job's pass graph per pass inside the parent graphs
+    # (21 kernels, 22 when its scene holds an infinite plane)
+    def per_pass(sc):
+        from ppmpa_gb300 import scene as S
+        plane = any(sh.shape == S.SHAPE_PLAIN for sh, _ in sc.objects) or \
+            any(bool((b["shape"] == S.SHAPE_PLAIN).any()) for b in sc.bulk)
+        return 22 if plane else 21
+    launches = 22 * bw["passes"] if picked == "staged" else sum(per_pass(sc) * cfg.passes for sc, _, cfg in jobs)
     return {
         "metric": f"batched render Mphotons/s ({len(jobs)} uneven jobs, all passes of every job)",
         "value": photons / (dev_ms / 1e3) / 1e6, "unit": "Mphotons/s", "steps": bw["passes"],
