@@ -58,7 +58,7 @@ SWEEP_MAX_STEPS = {"uniform": 10, "clustered": 3}
 # 64 seeded render jobs of uneven sizes (ppmpa_gb300/workloads.py batch_jobs),
 # 8 passes each, rendered as one batch (one graph launch per pass for all jobs)
 BATCHES = {"batch_64": dict(n_jobs=64, passes=8),
-           # many small jobs: per-job graphs cost 22 kernel nodes each per pass
+           # many small jobs: per-job graphs cost 21 kernel nodes each per pass
            "batch_256_small": dict(n_jobs=256, passes=8, prims=(10, 2000), reso=(48, 128),
                                    photons=(20_000, 100_000))}
 # the configurations measured beside the headline, in this order
