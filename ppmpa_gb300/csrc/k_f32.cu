@@ -9,9 +9,9 @@ namespace ppm {
 void launch_trace_f(const SceneView<float> &sc, const EmitPlan &plan, uint64_t seed, PassState *st, int uc,
                     PhotonBuf<float> photons, int grid, cudaStream_t s) {
     if (sc.bvh)
-        k_trace<float, true><<<grid, 256, 0, s>>>(with_bvh(sc), plan, seed, st, uc, photons);
+        k_trace<float, true><<<grid, TRACE_THREADS, 0, s>>>(with_bvh(sc), plan, seed, st, uc, photons);
     else
-        k_trace<float, false><<<grid, 256, 0, s>>>(sc, plan, seed, st, uc, photons);
+        k_trace<float, false><<<grid, TRACE_THREADS, 0, s>>>(sc, plan, seed, st, uc, photons);
 }
 void launch_bbox_f(PhotonBuf<float> buf, PassState *st, long long n_fixed, int grid, cudaStream_t s) {
     launch_pdl(k_bbox<float>, dim3(grid), dim3(256), s, buf, st, n_fixed);

@@ -473,11 +473,22 @@ static void launch_trace(ppm_ctx *ctx, const EmitPlan &plan, uint64_t seed, int 
     launch_trace_f(ctx->sv_f, plan, seed, ctx->st, uc, pb, g, s);
 }
 
-// one persistent launch with as many blocks as stay resident (TraceBlocks)
+// Eye levels after the first beside the photon trace: FP32 box scenes (no
+// hierarchy; the classic tracer has no photon trace).  The trace then leaves
+// room for one eye block per SM, so the levels run while it does instead of
+// after it (the levels are latency-bound: each is a few dependent memory
+// round trips long, whatever its size).
+static bool eye_beside_trace(const ppm_ctx *ctx, bool fp32) {
+    return fp32 && !ctx->sv_f.bvh && !(ctx->cfg.flags & PPM_RENDER_CLASSIC);
+}
+
+// one persistent launch with as many blocks as stay resident (TraceBlocks),
+// or TRACE_BLOCKS_BESIDE_EYE per SM beside the eye levels
 template <typename T>
 static int enqueue_photon_trace(ppm_ctx *ctx, const EmitPlan &plan, uint64_t seed, int uc, PhotonBuf<T> pb,
                                 cudaStream_t s) {
-    launch_trace(ctx, plan, seed, uc, pb, grid_blocks(ctx, TraceBlocks<T>::value), s);
+    const int per_sm = eye_beside_trace(ctx, sizeof(T) == 4) ? TRACE_BLOCKS_BESIDE_EYE : TraceBlocks<T>::value;
+    launch_trace(ctx, plan, seed, uc, pb, grid_blocks(ctx, per_sm), s);
     return 1;
 }
 
@@ -488,12 +499,15 @@ static int enqueue_eye(ppm_ctx *ctx, HitPoint<T> *hits, Level level_fn, cudaStre
     EyeQueue<T> qb{as<V>(ctx->eqb[3]), as<V>(ctx->eqb[4]), as<V>(ctx->eqb[5])};
     // Level 0 has one thread per pixel slot (pixels in tiles of 32, see
     // eye_slots).  The deeper levels' sizes are only known on the device;
-    // their grids stride over the queue.
+    // their grids stride over the queue: two blocks per SM beside the photon
+    // trace (one runs in the room the trace leaves, the other once it ends),
+    // four otherwise.
     const long long slots = eye_slots(ctx->cam.xreso, ctx->cam.yreso);
     const int g0 = (int)std::max(1LL, std::min<long long>((slots + 127) / 128, (long long)ctx->sm_count * 16));
+    const int gl = grid_blocks(ctx, eye_beside_trace(ctx, sizeof(T) == 4) ? 2 : 4);
     for (int l = 0; l < MAX_TRACE; l++)
-        level_fn(l, (l & 1) ? qb : qa, (l & 1) ? qa : qb, (unsigned long long)ctx->eq_cap, hits,
-                 l == 0 ? g0 : grid_blocks(ctx, 4), s);
+        level_fn(l, (l & 1) ? qb : qa, (l & 1) ? qa : qb, (unsigned long long)ctx->eq_cap, hits, l == 0 ? g0 : gl,
+                 s);
     return MAX_TRACE;
 }
 

@@ -289,7 +289,9 @@ static_assert(sizeof(DObject<float>) == 64, "FP32 object = four 16-byte vectors"
 static_assert(sizeof(DObject<double>) == 128, "FP64 object = eight 16-byte vectors");
 
 // object fetch with 16-byte vector loads (the table is read by every lane
-// for every ray, uniformly: each load is one broadcast transaction)
+// for every ray, uniformly: each load is one broadcast transaction).  Plain
+// loads, not __ldg: the eye levels point the table at a copy in shared
+// memory (eye_level), which the non-coherent global path cannot read.
 template <typename T>
 __device__ __forceinline__ DObject<T> load_object(const DObject<T> *objs, int i) {
     constexpr int NV = sizeof(DObject<T>) / 16;
@@ -299,7 +301,7 @@ __device__ __forceinline__ DObject<T> load_object(const DObject<T> *objs, int i)
     } u;
     const uint4 *src = reinterpret_cast<const uint4 *>(objs + i);
 #pragma unroll
-    for (int k = 0; k < NV; k++) u.v[k] = __ldg(src + k);
+    for (int k = 0; k < NV; k++) u.v[k] = src[k];
     return u.o;
 }
 

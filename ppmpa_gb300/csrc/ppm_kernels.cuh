@@ -250,11 +250,46 @@ __device__ __forceinline__ uint32_t tag(double4 v) { return (uint32_t)__double_a
 
 // photon ray queue: a = (pos, emission index), b = (dir, wl | (medium+1) << 8)
 
-// bounds of n photons (block reduction, then one atomic per block and axis)
-// resident blocks of 256 threads asked of the persistent photon trace: 4 in
-// FP32 (fits in 64 registers without spills), 2 in FP64
-template <typename T> struct TraceBlocks { static constexpr int value = 2; };
-template <> struct TraceBlocks<float> { static constexpr int value = 4; };
+// Scene tables of a box scene (no hierarchy) copied to shared memory by each
+// eye-level block: a level after the first has few vertices per SM, and a
+// vertex's intersection is then a chain of object loads from L2 (the table
+// is not yet in this SM's L1), one round trip per object.  Larger tables
+// stay in global memory.
+constexpr int EYE_SMEM_OBJS = 32, EYE_SMEM_MATS = 32;
+
+template <typename T, bool B>
+__device__ __forceinline__ SceneView<T, B> stage_scene(const SceneView<T, B> &sc) {
+    SceneView<T, B> v = sc;
+    if constexpr (!B) {
+        constexpr int OW = (int)(sizeof(DObject<T>) / 4), MW = (int)(sizeof(DMaterial<T>) / 4);
+        static_assert(sizeof(DMaterial<T>) % 4 == 0, "materials copy as 32-bit words");
+        __shared__ __align__(16) uint32_t s_obj[EYE_SMEM_OBJS * OW];
+        __shared__ __align__(16) uint32_t s_mat[EYE_SMEM_MATS * MW];
+        if (sc.n_objs <= EYE_SMEM_OBJS && sc.n_mats <= EYE_SMEM_MATS) {   // uniform over the block
+            const uint32_t *go = reinterpret_cast<const uint32_t *>(sc.objs);
+            const uint32_t *gm = reinterpret_cast<const uint32_t *>(sc.mats);
+            for (int k = threadIdx.x; k < sc.n_objs * OW; k += blockDim.x) s_obj[k] = __ldg(go + k);
+            for (int k = threadIdx.x; k < sc.n_mats * MW; k += blockDim.x) s_mat[k] = __ldg(gm + k);
+            __syncthreads();
+            v.objs = reinterpret_cast<const DObject<T> *>(s_obj);
+            v.mats = reinterpret_cast<const DMaterial<T> *>(s_mat);
+        }
+    }
+    return v;
+}
+
+// The persistent photon trace runs in blocks of TRACE_THREADS; TraceBlocks
+// is the most that stay resident per SM: 16 in FP32 (64 registers, no
+// spills), 8 in FP64.  Box scenes in FP32 launch TRACE_BLOCKS_BESIDE_EYE
+// per SM instead, leaving registers for one block of the eye levels (128
+// threads at 96 registers): 13 x 64 x 64 + 128 x 96 = 65,536, the SM's
+// register file.  Small blocks keep that room small: six of 128 threads
+// leave more, and measured 1 % slower on the glass box; sixteen of 64 leave
+// none, and the deeper eye levels then wait for the trace to end.
+constexpr int TRACE_THREADS = 64;
+template <typename T> struct TraceBlocks { static constexpr int value = 8; };
+template <> struct TraceBlocks<float> { static constexpr int value = 16; };
+constexpr int TRACE_BLOCKS_BESIDE_EYE = 13;
 
 // Persistent photon tracing: one launch per pass (measured faster than an
 // emission kernel plus MAX_TRACE bounce kernels with ray queues between them,
@@ -266,7 +301,7 @@ template <> struct TraceBlocks<float> { static constexpr int value = 4; };
 // (emission index, pass, level) as in the wavefront form, so the stored
 // photons are the same set (their order in the buffer differs).
 template <typename T, bool B>
-__global__ void __launch_bounds__(256, TraceBlocks<T>::value) k_trace(SceneView<T, B> sc, EmitPlan plan, uint64_t seed,
+__global__ void __launch_bounds__(TRACE_THREADS, TraceBlocks<T>::value) k_trace(SceneView<T, B> sc, EmitPlan plan, uint64_t seed,
                                                                        PassState *st, int uc, PhotonBuf<T> photons) {
     const uint32_t pass = (uint32_t)st->pass;
     const unsigned long long n_emit = (unsigned long long)plan.first[plan.n_lights];
@@ -319,6 +354,7 @@ __global__ void __launch_bounds__(256, TraceBlocks<T>::value) k_trace(SceneView<
     grid_dependents_launch();   // the map build may be scheduled once every block is here
 }
 
+// bounds of n photons (block reduction, then one atomic per block and axis)
 template <typename T>
 __global__ void __launch_bounds__(256) k_bbox(PhotonBuf<T> buf, PassState *st, long long n_fixed) {
     grid_dependency_wait();
@@ -639,9 +675,11 @@ __device__ __forceinline__ void eye_vertex(const SceneView<T, B> &sc, const DCam
 }
 
 template <typename T, bool B, bool CLASSIC = false>
-__device__ __forceinline__ void eye_level(const SceneView<T, B> &sc, const DCamera<T> &cam, uint64_t seed,
+__device__ __forceinline__ void eye_level(const SceneView<T, B> &gsc, const DCamera<T> &cam, uint64_t seed,
                                           PassState *st, int uc, int level, EyeQueue<T> in, EyeQueue<T> out,
                                           unsigned long long qcap, HitPoint<T> *hits, EyeOut<T> pix) {
+    // the scene's tables do not change within a pass: staged before the wait
+    const SceneView<T, B> sc = stage_scene(gsc);
     // Levels after 0 are programmatic dependents of the level before: their
     // blocks may be scheduled before it ends and wait here until it has
     // finished and its queue appends are visible (a no-op for a plain launch)
@@ -660,13 +698,15 @@ __device__ __forceinline__ void eye_level(const SceneView<T, B> &sc, const DCame
     grid_dependents_launch();
 }
 
-// Two entry points over the same body: without a hierarchy the compiler's
-// own register choice (no spills, more resident warps); with one, a cap of
-// 128 registers, under which the traversal stack does not spill.
+// Two entry points over the same body: without a hierarchy five blocks per
+// SM (96 registers in FP32: one block fits beside the photon trace's
+// TRACE_BLOCKS_BESIDE_EYE); with one, a cap of 128 registers, under which
+// the traversal stack does not spill.
 template <typename T, bool CLASSIC>
-__global__ void __launch_bounds__(128) k_eye_level(SceneView<T, false> sc, DCamera<T> cam, uint64_t seed,
-                                                   PassState *st, int uc, int level, EyeQueue<T> in, EyeQueue<T> out,
-                                                   unsigned long long qcap, HitPoint<T> *hits, EyeOut<T> pix) {
+__global__ void __launch_bounds__(128, 5) k_eye_level(SceneView<T, false> sc, DCamera<T> cam, uint64_t seed,
+                                                      PassState *st, int uc, int level, EyeQueue<T> in,
+                                                      EyeQueue<T> out, unsigned long long qcap, HitPoint<T> *hits,
+                                                      EyeOut<T> pix) {
     eye_level<T, false, CLASSIC>(sc, cam, seed, st, uc, level, in, out, qcap, hits, pix);
 }
 template <typename T, bool CLASSIC>
