@@ -58,7 +58,7 @@ SWEEP_MAX_STEPS = {"uniform": 10, "clustered": 3}
 # 64 seeded render jobs of uneven sizes (ppmpa_gb300/workloads.py batch_jobs),
 # 8 passes each, rendered as one batch (one graph launch per pass for all jobs)
 BATCHES = {"batch_64": dict(n_jobs=64, passes=8),
-           # many small jobs: per-job graphs cost 21 kernel nodes each per pass
+           # many small jobs: per-job graphs cost 20 kernel nodes each per pass
            "batch_256_small": dict(n_jobs=256, passes=8, prims=(10, 2000), reso=(48, 128),
                                    photons=(20_000, 100_000))}
 # the configurations measured beside the headline, in this order
@@ -770,12 +770,13 @@ def measure_batch(args, name, bw):
         return None if ms is None else {"value": photons / (ms / 1e3) / 1e6, "unit": "Mphotons/s", "ms": ms}
     # kernels of this library launched in the timed render: 22 per staged pass
     # of the batch, or each job's pass graph per pass inside the parent graphs
-    # (21 kernels, 22 when its scene holds an infinite plane)
+    # (20 kernels, 22 when its scene holds an infinite plane: the photon bounds
+    # and the grid set-up, which the photon trace does for bounded scenes)
     def per_pass(sc):
         from ppmpa_gb300 import scene as S
         plane = any(sh.shape == S.SHAPE_PLAIN for sh, _ in sc.objects) or \
             any(bool((b["shape"] == S.SHAPE_PLAIN).any()) for b in sc.bulk)
-        return 22 if plane else 21
+        return 22 if plane else 20
     launches = 22 * bw["passes"] if picked == "staged" else sum(per_pass(sc) * cfg.passes for sc, _, cfg in jobs)
     return {
         "metric": f"batched render Mphotons/s ({len(jobs)} uneven jobs, all passes of every job)",

@@ -32,78 +32,12 @@ __device__ __forceinline__ void pass_begin_state(PassState *st) {
     }
 }
 
-
-// Grid over the photon bounds with cells of c = r/k * (1 + 1/128) in y and z
-// (k = cells per radius) and c / sx in x.  The margin keeps |p - q| <= r  =>
-// |cell(p) - cell(q)| <= ext (extx in x) under FP32 rounding of the cell
-// coordinate (<= 3 ulp of <= 8192 cells per axis).
-__device__ __forceinline__ void grid_setup_state(PassState *st, double r2_override) {
-    double r2 = r2_override > 0.0 ? r2_override : st->r2;
-    double r = sqrt(r2);
-    double lo[3], hi[3];
-    bool empty = false;
-    for (int a = 0; a < 3; a++) {
-        lo[a] = ord_dec(st->bb_lo[a]);
-        hi[a] = ord_dec(st->bb_hi[a]);
-        if (!(lo[a] <= hi[a])) empty = true;
-    }
-    for (int a = 0; a < 3; a++)
-        if (!(hi[a] - lo[a] >= 0.0 && hi[a] - lo[a] < 1e30)) empty = true;
-    if (empty) for (int a = 0; a < 3; a++) { lo[a] = 0.0; hi[a] = 0.0; }
-    double k = st->cell_factor > 0.0 ? st->cell_factor : 1.0;
-    const int sx = st->cell_sx >= 1 ? st->cell_sx : 1;
-    // One thread, and FP64 is a narrow, long-latency pipe on this GPU: two
-    // divisions, the rest multiplications by the reciprocal (the same
-    // product form cell_of uses, so the last cell holds hi exactly).
-    double c = r * ((1.0 + 1.0 / 128.0) / k);
-    if (!(c > 0.0 && c < 1e30)) c = 1.0;
-    double inv = 1.0 / c;
-    long long dim[3] = {1, 1, 1};
-    for (int it = 0; it < 400; it++) {
-        bool ok = true;
-        long long tot = 1;
-        for (int a = 0; a < 3; a++) {
-            double f = floor((hi[a] - lo[a]) * (a == 0 ? inv * sx : inv));
-            if (!(f >= 0.0 && f < 8192.0)) { ok = false; dim[a] = 8193; }
-            else dim[a] = (long long)f + 1;
-            tot *= dim[a];
-        }
-        if (ok && tot <= st->cell_cap) break;
-        c *= 1.25;
-        inv = 1.0 / c;
-        if (it == 399) { dim[0] = dim[1] = dim[2] = 1; c = 1e30; inv = 1e-30; }
-    }
-    GridParams g;
-    for (int a = 0; a < 3; a++) {
-        g.org[a] = lo[a];
-        g.orgf[a] = (float)lo[a];
-        g.dim[a] = (int32_t)dim[a];
-    }
-    const double invx = inv * sx;
-    g.cell = c;
-    g.inv = inv;
-    g.invf = (float)inv;
-    g.invx = invx;
-    g.invxf = (float)invx;
-    double ef = ceil(r * inv + 3e-3);
-    int ext = ef >= 1.0 && ef <= 8.0 ? (int)ef : (ef > 8.0 ? 8 : 1);
-    g.ext = ext < 1 ? 1 : (ext > 8 ? 8 : ext);
-    double efx = ceil(r * invx + 3e-3);
-    g.extx = efx >= 1.0 && efx <= 64.0 ? (int)efx : (efx > 64.0 ? 64 : 1);
-    g.ncell = dim[0] * dim[1] * dim[2];
-    g.nkeys = g.ncell;
-    g.r2f = (float)r2;
-    g.r2_lo = __double2float_rd(r2 * (1.0 - 1e-6));
-    g.r2_hi = __double2float_ru(r2 * (1.0 + 1e-6));
-    g.cellf = (float)c;
-    st->grid = g;
-}
-
 // Pass set-up.  With a scene box the bounds the grid spans are the box
 // (the photons and hit points lie on the scene's objects), and the pass
-// launches no k_bbox; k_grid_setup still follows the photon trace, off the
-// eye branch's path.  Photons a rounding step outside the box go to the
-// edge cells, which only shrinks their cell distance to any query.
+// launches no k_bbox; the FP32 photon trace then sets the grid up itself
+// (one thread, after its loop), the FP64 path in k_grid_setup after the
+// trace.  Photons a rounding step outside the box go to the edge cells,
+// which only shrinks their cell distance to any query.
 __global__ void k_pass_begin(PassState *st) {
     if (threadIdx.x != 0) return;
     pass_begin_state(st);

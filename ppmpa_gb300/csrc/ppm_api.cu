@@ -1525,7 +1525,7 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
         kernels += enqueue_photon_trace<float>(ctx, ctx->plan, ctx->cfg.seed, uc, pb, s);
         if (!box) launch_bbox_f(pb, ctx->st, -1, g4, s);
         if (ev) CK(cudaEventRecord(ev[1], s));
-        launch_grid_setup(ctx->st, -1.0, s);
+        if (!box) launch_grid_setup(ctx->st, -1.0, s);   // box scenes: set up by the trace
         launch_hist_f(pb, ctx->st, -1, as<uint32_t>(ctx->count), as<uint2>(ctx->keyrank), g8, s);
         launch_scan(as<uint32_t>(ctx->count), ctx->st, as<uint32_t>(ctx->block_sums), as<uint32_t>(ctx->start), CELL_CAP, s,
                     grid_blocks(ctx, 8));
@@ -1541,7 +1541,9 @@ static int enqueue_pass(ppm_ctx *ctx, bool capture) {
                     grid_blocks(ctx, 8));
         launch_scatter_d(pb, ctx->st, -1, as<uint32_t>(ctx->start), as<uint2>(ctx->keyrank), g8, s);
     }
-    kernels += (box ? 3 : 4) + kernels_per_scan();
+    // [bounds, grid set-up,] histogram, scan, scatter; the FP64 path sets its
+    // grid up in a kernel of its own for box scenes too
+    kernels += (box ? (mixed ? 2 : 3) : 4) + kernels_per_scan();
     if (ev) CK(cudaEventRecord(ev[2], s));
     CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
     if (ev) CK(cudaEventRecord(ev[7], s));

@@ -250,6 +250,72 @@ __device__ __forceinline__ uint32_t tag(double4 v) { return (uint32_t)__double_a
 
 // photon ray queue: a = (pos, emission index), b = (dir, wl | (medium+1) << 8)
 
+// Grid over the photon bounds with cells of c = r/k * (1 + 1/128) in y and z
+// (k = cells per radius) and c / sx in x.  The margin keeps |p - q| <= r  =>
+// |cell(p) - cell(q)| <= ext (extx in x) under FP32 rounding of the cell
+// coordinate (<= 3 ulp of <= 8192 cells per axis).
+__device__ __forceinline__ void grid_setup_state(PassState *st, double r2_override) {
+    double r2 = r2_override > 0.0 ? r2_override : st->r2;
+    double r = sqrt(r2);
+    double lo[3], hi[3];
+    bool empty = false;
+    for (int a = 0; a < 3; a++) {
+        lo[a] = ord_dec(st->bb_lo[a]);
+        hi[a] = ord_dec(st->bb_hi[a]);
+        if (!(lo[a] <= hi[a])) empty = true;
+    }
+    for (int a = 0; a < 3; a++)
+        if (!(hi[a] - lo[a] >= 0.0 && hi[a] - lo[a] < 1e30)) empty = true;
+    if (empty) for (int a = 0; a < 3; a++) { lo[a] = 0.0; hi[a] = 0.0; }
+    double k = st->cell_factor > 0.0 ? st->cell_factor : 1.0;
+    const int sx = st->cell_sx >= 1 ? st->cell_sx : 1;
+    // One thread, and FP64 is a narrow, long-latency pipe on this GPU: two
+    // divisions, the rest multiplications by the reciprocal (the same
+    // product form cell_of uses, so the last cell holds hi exactly).
+    double c = r * ((1.0 + 1.0 / 128.0) / k);
+    if (!(c > 0.0 && c < 1e30)) c = 1.0;
+    double inv = 1.0 / c;
+    long long dim[3] = {1, 1, 1};
+    for (int it = 0; it < 400; it++) {
+        bool ok = true;
+        long long tot = 1;
+        for (int a = 0; a < 3; a++) {
+            double f = floor((hi[a] - lo[a]) * (a == 0 ? inv * sx : inv));
+            if (!(f >= 0.0 && f < 8192.0)) { ok = false; dim[a] = 8193; }
+            else dim[a] = (long long)f + 1;
+            tot *= dim[a];
+        }
+        if (ok && tot <= st->cell_cap) break;
+        c *= 1.25;
+        inv = 1.0 / c;
+        if (it == 399) { dim[0] = dim[1] = dim[2] = 1; c = 1e30; inv = 1e-30; }
+    }
+    GridParams g;
+    for (int a = 0; a < 3; a++) {
+        g.org[a] = lo[a];
+        g.orgf[a] = (float)lo[a];
+        g.dim[a] = (int32_t)dim[a];
+    }
+    const double invx = inv * sx;
+    g.cell = c;
+    g.inv = inv;
+    g.invf = (float)inv;
+    g.invx = invx;
+    g.invxf = (float)invx;
+    double ef = ceil(r * inv + 3e-3);
+    int ext = ef >= 1.0 && ef <= 8.0 ? (int)ef : (ef > 8.0 ? 8 : 1);
+    g.ext = ext < 1 ? 1 : (ext > 8 ? 8 : ext);
+    double efx = ceil(r * invx + 3e-3);
+    g.extx = efx >= 1.0 && efx <= 64.0 ? (int)efx : (efx > 64.0 ? 64 : 1);
+    g.ncell = dim[0] * dim[1] * dim[2];
+    g.nkeys = g.ncell;
+    g.r2f = (float)r2;
+    g.r2_lo = __double2float_rd(r2 * (1.0 - 1e-6));
+    g.r2_hi = __double2float_ru(r2 * (1.0 + 1e-6));
+    g.cellf = (float)c;
+    st->grid = g;
+}
+
 // Scene tables of a box scene (no hierarchy) copied to shared memory by each
 // eye-level block: a level after the first has few vertices per SM, and a
 // vertex's intersection is then a chain of object loads from L2 (the table
@@ -351,6 +417,12 @@ __global__ void __launch_bounds__(TRACE_THREADS, TraceBlocks<T>::value) k_trace(
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) rays += __shfl_xor_sync(0xffffffffu, rays, o);
     if (lane == 0 && rays) atomicAdd(&st->photon_rays, (unsigned long long)rays);
+    // FP32 box scenes: the pass's grid spans the scene's box, which the
+    // photons do not change, so one thread sets it up here (after its loop,
+    // out of the loop's register budget) and the map build follows the
+    // trace with no set-up kernel between them
+    if constexpr (sizeof(T) == 4)
+        if (blockIdx.x == 0 && threadIdx.x == 0 && st->scene_box) grid_setup_state(st, -1.0);
     grid_dependents_launch();   // the map build may be scheduled once every block is here
 }
 
@@ -1265,8 +1337,6 @@ __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, cons
             }
         }
     }
-    a0 = warp_sum(a0); a1 = warp_sum(a1); a2 = warp_sum(a2);
-    b0 = warp_sum(b0); b1 = warp_sum(b1); b2 = warp_sum(b2);
     if (COUNT) {
         for (int o = 16; o > 0; o >>= 1) {
             c_slots += __shfl_xor_sync(0xffffffffu, c_slots, o);
@@ -1279,7 +1349,37 @@ __device__ __forceinline__ bool gather_pair(const GridParams &g, double r2, cons
             atomicAdd(out.count + 2, c_slots);
         }
     }
-    if (DUMP) {
+    if (!DUMP) {
+        // Six sums over the warp in 15 shuffles: one exchange leaves hit a's
+        // three partial sums (lanes l and l + 16) on lanes 0-15 and hit b's
+        // on lanes 16-31, then each half sums its three; lanes 0 and 16
+        // scale by their hit point's weights and add to its pixel.
+        const bool upper = lane >= 16u;
+        float s0 = upper ? b0 : a0, s1 = upper ? b1 : a1, s2 = upper ? b2 : a2;
+        s0 += __shfl_xor_sync(0xffffffffu, upper ? a0 : b0, 16);
+        s1 += __shfl_xor_sync(0xffffffffu, upper ? a1 : b1, 16);
+        s2 += __shfl_xor_sync(0xffffffffu, upper ? a2 : b2, 16);
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) {
+            s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+            s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        }
+        if ((lane & 15u) == 0u) {
+            // weights and pixel re-read here (cached) rather than held through the walk
+            const HitPoint<float> h = load_hit(hp + (lane >> 4));
+            float *px = out.gathered + 3 * (size_t)h.pixel;
+            atomicAdd(px, h.w[0] * s0);
+            atomicAdd(px + 1, h.w[1] * s1);
+            atomicAdd(px + 2, h.w[2] * s2);
+        }
+        return true;
+    }
+    // the parity export: every sum reduced on every lane, written with the
+    // pair's in-radius counts and checksums
+    a0 = warp_sum(a0); a1 = warp_sum(a1); a2 = warp_sum(a2);
+    b0 = warp_sum(b0); b1 = warp_sum(b1); b2 = warp_sum(b2);
+    {
         for (int o = 16; o > 0; o >>= 1) {
             na_in += __shfl_xor_sync(0xffffffffu, na_in, o);
             nb_in += __shfl_xor_sync(0xffffffffu, nb_in, o);
