@@ -303,18 +303,39 @@ void launch_pass_end(PassState *st, cudaStream_t s) { k_pass_end<<<1, 32, 0, s>>
 // pass state, computed once at pass begin, and each thread takes several
 // elements, so the FP64 work per element is the two conversions, one fused
 // multiply-add and the running-sum add.)
+// Four elements per thread per step: 16-byte loads of the FP32 images and of
+// the running sum, 16-byte stores (the buffers are cudaMalloc'd, so element
+// 4q is 16-byte aligned for floats and 32-byte aligned for doubles); the
+// last n mod 4 elements one at a time.
+__device__ __forceinline__ double accum_one(float d, float g, double kk) { return (double)d + (double)g * kk; }
+
 __global__ void k_accum_mixed(const float *direct, const float *gathered, const PassState *st, double pw,
                               double *pass_img, double *sum, long long n) {
     grid_dependency_wait();
     const double kk = pw * st->inv_pi_r2;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        double v = (double)direct[i] + (double)gathered[i] * kk;
+    const long long n4 = n / 4, stride = (long long)gridDim.x * blockDim.x;
+    const float4 *d4 = reinterpret_cast<const float4 *>(direct), *g4 = reinterpret_cast<const float4 *>(gathered);
+    double2 *p2 = reinterpret_cast<double2 *>(pass_img), *s2 = reinterpret_cast<double2 *>(sum);
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += stride) {
+        const float4 d = d4[q], g = g4[q];
+        const double2 sa = s2[2 * q], sb = s2[2 * q + 1];
+        const double v0 = accum_one(d.x, g.x, kk), v1 = accum_one(d.y, g.y, kk);
+        const double v2 = accum_one(d.z, g.z, kk), v3 = accum_one(d.w, g.w, kk);
+        p2[2 * q] = make_double2(v0, v1);
+        p2[2 * q + 1] = make_double2(v2, v3);
+        s2[2 * q] = make_double2(sa.x + v0, sa.y + v1);
+        s2[2 * q + 1] = make_double2(sb.x + v2, sb.y + v3);
+    }
+    for (long long i = 4 * n4 + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double v = accum_one(direct[i], gathered[i], kk);
         pass_img[i] = v;
         sum[i] += v;
-    }}
+    }
+}
 void launch_accum_mixed(const float *direct, const float *gathered, const PassState *st, double pw, double *pass_img,
                         double *sum, long long n, cudaStream_t s) {
-    launch_pdl(k_accum_mixed, dim3((unsigned)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024)), dim3(256), s, direct,
+    const long long q = (n + 3) / 4;
+    launch_pdl(k_accum_mixed, dim3((unsigned)((q + 255) / 256 < 1024 ? (q + 255) / 256 : 1024)), dim3(256), s, direct,
                gathered, st, pw, pass_img, sum, n);
 }
 

@@ -498,13 +498,18 @@ static int enqueue_eye(ppm_ctx *ctx, HitPoint<T> *hits, Level level_fn, cudaStre
     EyeQueue<T> qa{as<V>(ctx->eqb[0]), as<V>(ctx->eqb[1]), as<V>(ctx->eqb[2])};
     EyeQueue<T> qb{as<V>(ctx->eqb[3]), as<V>(ctx->eqb[4]), as<V>(ctx->eqb[5])};
     // Level 0 has one thread per pixel slot (pixels in tiles of 32, see
-    // eye_slots).  The deeper levels' sizes are only known on the device;
-    // their grids stride over the queue: two blocks per SM beside the photon
-    // trace (one runs in the room the trace leaves, the other once it ends),
-    // four otherwise.
+    // eye_slots), striding over them.  Beside the photon trace its grid is
+    // three blocks per SM, so the trace's blocks start at once on the rest
+    // of each SM instead of waiting for a wave of sixteen eye blocks to
+    // drain.  The deeper levels' sizes are only known on the device; their
+    // grids stride over the queue: two blocks per SM beside the trace (one
+    // runs in the room the trace leaves, the other once it ends), four
+    // otherwise.
+    const bool beside = eye_beside_trace(ctx, sizeof(T) == 4);
     const long long slots = eye_slots(ctx->cam.xreso, ctx->cam.yreso);
-    const int g0 = (int)std::max(1LL, std::min<long long>((slots + 127) / 128, (long long)ctx->sm_count * 16));
-    const int gl = grid_blocks(ctx, eye_beside_trace(ctx, sizeof(T) == 4) ? 2 : 4);
+    const long long g0_cap = (long long)ctx->sm_count * (beside ? 3 : 16);
+    const int g0 = (int)std::max(1LL, std::min<long long>((slots + 127) / 128, g0_cap));
+    const int gl = grid_blocks(ctx, beside ? 2 : 4);
     for (int l = 0; l < MAX_TRACE; l++)
         level_fn(l, (l & 1) ? qb : qa, (l & 1) ? qa : qb, (unsigned long long)ctx->eq_cap, hits, l == 0 ? g0 : gl,
                  s);
