@@ -499,7 +499,7 @@ static int enqueue_eye(ppm_ctx *ctx, HitPoint<T> *hits, Level level_fn, cudaStre
     EyeQueue<T> qb{as<V>(ctx->eqb[3]), as<V>(ctx->eqb[4]), as<V>(ctx->eqb[5])};
     // Level 0 has one thread per pixel slot (pixels in tiles of 32, see
     // eye_slots), striding over them.  Beside the photon trace its grid is
-    // three blocks per SM, so the trace's blocks start at once on the rest
+    // two blocks per SM, so the trace's blocks start at once on the rest
     // of each SM instead of waiting for a wave of sixteen eye blocks to
     // drain.  The deeper levels' sizes are only known on the device; their
     // grids stride over the queue: two blocks per SM beside the trace (one
@@ -507,7 +507,7 @@ static int enqueue_eye(ppm_ctx *ctx, HitPoint<T> *hits, Level level_fn, cudaStre
     // otherwise.
     const bool beside = eye_beside_trace(ctx, sizeof(T) == 4);
     const long long slots = eye_slots(ctx->cam.xreso, ctx->cam.yreso);
-    const long long g0_cap = (long long)ctx->sm_count * (beside ? 3 : 16);
+    const long long g0_cap = (long long)ctx->sm_count * (beside ? 2 : 16);
     const int g0 = (int)std::max(1LL, std::min<long long>((slots + 127) / 128, g0_cap));
     const int gl = grid_blocks(ctx, beside ? 2 : 4);
     for (int l = 0; l < MAX_TRACE; l++)
