@@ -131,3 +131,23 @@ def test_bvh_on_spheres_and_quads_matches_oracle(ctx, n_prims, leaf):
     assert np.array_equal(obj, oobj) and np.array_equal(t, ot) and np.array_equal(nrm, onrm)
     assert (obj >= 5).mean() > 0.05
     ctx.set_bvh_leaf(1)
+
+
+def test_render_through_the_loop_and_the_hierarchy_agree(ctx):
+    """A scene of 45 objects rendered with the loop over its objects (a table
+    too large for the eye levels' shared-memory copy, so they read it from
+    global memory) and through the hierarchy: the same first hits, so the
+    same image up to the order of FP32 sums."""
+    from ppmpa_gb300 import workloads as W
+    sc = W.batch_scene(np.random.default_rng(40), 40)
+    assert sc.n_objects > 32
+    ctx.upload_scene(sc)
+    ctx.set_camera(S.box_camera(128))
+    imgs = []
+    for mode in (LOOP, BVH):
+        ctx.set_accel(mode)
+        imgs.append(ctx.render(RenderConfig(nphoton=100_000, passes=2, radius0=0.05, alpha=0.7, precision=MIXED,
+                                            seed=3)))
+    ctx.set_accel(0)
+    assert np.isfinite(imgs[0]).all() and imgs[0].mean() > 0
+    assert np.allclose(imgs[0], imgs[1], rtol=1e-4, atol=1e-6 * imgs[0].max())
