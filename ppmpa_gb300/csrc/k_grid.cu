@@ -97,7 +97,8 @@ __device__ __forceinline__ void scan_reduce_tile(const uint32_t *count, long lon
     __syncthreads();
 }
 
-// exclusive scan of nb <= 4096 tile sums by a block of 1024 threads
+// exclusive scan of nb <= 4096 tile sums by a block of 1024 threads (the
+// batch's per-job scan)
 __device__ __forceinline__ void scan_top_block(uint32_t *block_sums, int nb, uint32_t *sh) {
     // each thread owns up to 4 consecutive tile sums
     uint32_t v[4], t = 0;
@@ -180,11 +181,41 @@ __global__ void __launch_bounds__(256) k_scan_reduce(const uint32_t *count, cons
     grid_dependents_launch();
 }
 
-__global__ void __launch_bounds__(1024) k_scan_top(uint32_t *block_sums, const PassState *st, long long fixed) {
+// exclusive scan of nb <= 4096 tile sums by one block of 256 threads, 16
+// consecutive sums per thread: warp shuffles and one block barrier
+__device__ __forceinline__ void scan_top_256(uint32_t *block_sums, int nb, uint32_t *sh) {
+    constexpr int PER = 4096 / 256;
+    uint32_t v[PER], t = 0;
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        const int i = threadIdx.x * PER + j;
+        v[j] = i < nb ? block_sums[i] : 0u;
+        t += v[j];
+    }
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (unsigned)o) incl += u;
+    }
+    if (lane == 31) sh[warp] = incl;
+    __syncthreads();
+    uint32_t run = incl - t;
+    for (unsigned w = 0; w < warp; w++) run += sh[w];
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        const int i = threadIdx.x * PER + j;
+        if (i < nb) block_sums[i] = run;
+        run += v[j];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_scan_top(uint32_t *block_sums, const PassState *st, long long fixed) {
     grid_dependency_wait();
     const long long n = scan_keys(st, fixed);
-    __shared__ uint32_t sh[1024];
-    scan_top_block(block_sums, (int)((n + SCAN_TILE - 1) / SCAN_TILE), sh);
+    __shared__ uint32_t sh[8];
+    scan_top_256(block_sums, (int)((n + SCAN_TILE - 1) / SCAN_TILE), sh);
     grid_dependents_launch();
 }
 
@@ -288,7 +319,7 @@ void launch_scan(uint32_t *count, const PassState *st, uint32_t *block_sums, uin
     const long long tiles = (cap + SCAN_TILE - 1) / SCAN_TILE;
     const int nb = (int)(tiles < grid ? tiles : grid);
     launch_pdl(k_scan_reduce, dim3(nb), dim3(256), s, count, st, fixed_keys, block_sums);
-    launch_pdl(k_scan_top, dim3(1), dim3(1024), s, block_sums, st, fixed_keys);
+    launch_pdl(k_scan_top, dim3(1), dim3(256), s, block_sums, st, fixed_keys);
     launch_pdl(k_scan_down, dim3(nb), dim3(256), s, count, st, fixed_keys, block_sums, start);
 }
 int kernels_per_scan() { return 3; }
