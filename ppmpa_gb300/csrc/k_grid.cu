@@ -19,6 +19,7 @@ __device__ __forceinline__ void pass_begin_state(PassState *st) {
     st->tile_items = 0;
     st->tile_next = 0;
     st->emit_next = 0;
+    st->trace_done = 0;
     st->photon_rays = 0;
     for (int l = 0; l < MAX_TRACE + 2; l++) st->eq[l] = 0;
     st->inv_pi_r2 = ONE_PI_D / st->r2;

@@ -70,7 +70,7 @@ struct PassState {
     unsigned long long tile_items;          // tile gather: items queued this pass
     unsigned long long tile_next;           // and the next one to take
     int32_t scene_box;                      // 1: every object is bounded; the grid spans their box
-    int32_t pad3;
+    uint32_t trace_done;                    // photon-trace blocks finished this pass
     double scene_lo[3], scene_hi[3];        // the scene's box (photons and hit points lie on its objects)
 };
 
@@ -418,11 +418,15 @@ __global__ void __launch_bounds__(TRACE_THREADS, TraceBlocks<T>::value) k_trace(
     for (int o = 16; o > 0; o >>= 1) rays += __shfl_xor_sync(0xffffffffu, rays, o);
     if (lane == 0 && rays) atomicAdd(&st->photon_rays, (unsigned long long)rays);
     // FP32 box scenes: the pass's grid spans the scene's box, which the
-    // photons do not change, so one thread sets it up here (after its loop,
-    // out of the loop's register budget) and the map build follows the
-    // trace with no set-up kernel between them
+    // photons do not change, so the first block to finish sets it up here
+    // (after its loop, out of the loop's register budget, while the other
+    // blocks still trace) and the map build follows the trace with no
+    // set-up kernel between them
     if constexpr (sizeof(T) == 4)
-        if (blockIdx.x == 0 && threadIdx.x == 0 && st->scene_box) grid_setup_state(st, -1.0);
+        if (st->scene_box) {   // uniform over the block
+            __syncthreads();
+            if (threadIdx.x == 0 && atomicAdd(&st->trace_done, 1u) == 0u) grid_setup_state(st, -1.0);
+        }
     grid_dependents_launch();   // the map build may be scheduled once every block is here
 }
 
