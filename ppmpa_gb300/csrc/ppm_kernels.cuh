@@ -367,8 +367,8 @@ constexpr int TRACE_BLOCKS_BESIDE_EYE = 13;
 // (emission index, pass, level) as in the wavefront form, so the stored
 // photons are the same set (their order in the buffer differs).
 template <typename T, bool B>
-__global__ void __launch_bounds__(TRACE_THREADS, TraceBlocks<T>::value) k_trace(SceneView<T, B> sc, EmitPlan plan, uint64_t seed,
-                                                                       PassState *st, int uc, PhotonBuf<T> photons) {
+__global__ void __launch_bounds__(TRACE_THREADS, TraceBlocks<T>::value)
+    k_trace(SceneView<T, B> sc, EmitPlan plan, uint64_t seed, PassState *st, int uc, PhotonBuf<T> photons) {
     const uint32_t pass = (uint32_t)st->pass;
     const unsigned long long n_emit = (unsigned long long)plan.first[plan.n_lights];
     const unsigned long long pcap = st->photon_cap;
